@@ -1,0 +1,382 @@
+"""Benchmark: DOF-updates/s of the TreeMesh DGSEM rhs on GB300.
+
+Workload (the 2D Euler configuration the metric is quoted on): compressible
+Euler (gamma 1.4) on a periodic TreeMesh [-2,2]^2 at refinement level 7
+(128^2 = 16384 elements), polydeg 3 (16 nodes/element, 262144 DOFs x 4
+variables), flux-differencing volume integral with flux_ranocha and
+flux_ranocha surface flux, seeded smooth Fourier initial condition.  A step is
+one CarpenterKennedy2N54 time step = 5 fused rhs + RK-stage launches through
+the C ABI (trixi_rk_stage).  DOF-updates per step = 5 * 262144.
+
+`value` is the FP32-mixed path (rhs in FP32, RK state in FP64) timed on the
+device with CUDA events around each stage launch, with L2 flushed (a 256 MB
+write) before every timed step.  The FP64 path is reported beside it, with
+the L2 difference of the two solutions after 100 steps ("equal L2 error").
+`e2e` times the public API call (trixicuda.rk_steps) with the state copied
+from pinned host memory before and back after every step.
+
+`--impl reference` times the CPU restatement of the reference algorithm
+(oracle/, OpenMP on all host cores): the reference itself (Julia + Trixi.jl)
+cannot run on this machine.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for p in (ROOT, ROOT / "trixicuda.jl_gb300"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+METRIC = "DOF-updates/s"
+LEVEL, POLYDEG = 7, 3
+WORKLOAD = ("2D compressible Euler, TreeMesh [-2,2]^2 periodic level 7 (16384 elements), polydeg 3, "
+            "flux-differencing flux_ranocha volume + flux_ranocha surface, CarpenterKennedy2N54 step")
+L2_BYTES = 256 << 20
+
+
+def build_problem(precision: str):
+    import trixicuda as T
+
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEMGPU(polydeg=POLYDEG, surface_flux=T.flux_ranocha,
+                        volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((-2.0, -2.0), (2.0, 2.0), initial_refinement_level=LEVEL)
+    ic = T.initial_condition_fourier_euler(eq, seed=20261203, kmax=8)
+    return mesh, eq, ic, solver
+
+
+def stable_dt(semi) -> float:
+    """CFL 0.5 time step from the initial state (max |v| + c)."""
+    u = semi.compute_coefficients_host().reshape(-1, semi.equations.nvariables).T
+    rho, v, p = semi.equations.cons2prim(u)
+    lam = np.max(np.sqrt(np.sum(v * v, axis=0)) + np.sqrt(semi.equations.gamma * p / rho))
+    h = 4.0 / 2**LEVEL
+    return 0.5 * h / (POLYDEG + 1) / lam
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                except ValueError:
+                    continue
+                for n, val in zip(names, parts[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def time_gpu_path(precision, steps, warmup, device, flush):
+    """Device-timed CK2N54 steps through trixi_rk_stage (ping-pong buffers).
+    Returns per-step ms, per-launch ms of the fused kernel, the semi, final u."""
+    import torch
+
+    import trixicuda as T
+    from trixicuda.time_integration import CK2N54_A, CK2N54_B
+
+    mesh, eq, ic, solver = build_problem(precision)
+    semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, precision=precision)
+    dt = stable_dt(semi)
+    u0 = semi.compute_coefficients()
+    bufs = [u0.clone(), torch.empty_like(u0)]
+    k = torch.zeros_like(u0)
+    stream = torch.cuda.current_stream()
+    lib = T._lib.load()
+    sh = C.c_void_p(stream.cuda_stream)
+    h = semi.handle
+    cur = 0
+
+    def stage(s):
+        nonlocal cur
+        st = lib.trixi_rk_stage(h, C.c_void_p(bufs[1 - cur].data_ptr()), C.c_void_p(bufs[cur].data_ptr()),
+                                C.c_void_p(k.data_ptr()), CK2N54_A[s], CK2N54_B[s], dt, 0.0, sh)
+        T._lib.check(st, h)
+        cur = 1 - cur
+
+    for _ in range(warmup):
+        for s in range(5):
+            stage(s)
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        for s in range(5):
+            ev[i][s].record(stream)
+            stage(s)
+        ev[i][5].record(stream)
+    torch.cuda.synchronize()
+    T.synchronize(semi)
+    step_ms = [ev[i][0].elapsed_time(ev[i][5]) for i in range(steps)]
+    launch_ms = [ev[i][s].elapsed_time(ev[i][s + 1]) for i in range(steps) for s in range(5)]
+    return step_ms, launch_ms, semi, bufs[cur], dt
+
+
+def e2e_path(precision, steps, warmup, device):
+    """The public API call with host buffers: H2D(u) -> rk_steps(1 step) -> D2H(u)."""
+    import torch
+
+    import trixicuda as T
+
+    mesh, eq, ic, solver = build_problem(precision)
+    semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, precision=precision)
+    dt = stable_dt(semi)
+    host = torch.from_numpy(semi.compute_coefficients_host()).pin_memory()
+    u = torch.empty(host.shape, dtype=torch.float64, device=device)
+    k = torch.zeros_like(u)
+    out = torch.empty_like(host).pin_memory()
+    for _ in range(warmup):
+        u.copy_(host, non_blocking=True)
+        T.rk_steps(u, k, 0.0, dt, 1, semi)
+        out.copy_(u, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(steps):
+        u.copy_(host, non_blocking=True)
+        T.rk_steps(u, k, 0.0, dt, 1, semi)
+        out.copy_(u, non_blocking=True)
+    t1.record()
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / steps
+    nbytes = host.numel() * 8
+    return ms, nbytes, semi.ndofs()
+
+
+def cpu_baseline(seconds_target=8.0, nthreads=None):
+    """The oracle (CPU restatement, OpenMP) on a bounded sample of the same
+    workload: whole CK2N54 steps of the full level-7 mesh."""
+    import trixicuda as T
+    from oracle import oracle as O
+
+    nthreads = nthreads or os.cpu_count() or 1
+    O.set_threads(nthreads)
+    mesh, eq, ic, solver = build_problem("fp64")
+    cont = mesh.build_containers(solver.basis.nodes)
+
+    class _S:
+        pass
+
+    s = _S()
+    s.equations, s.solver, s.containers = eq, solver, cont
+    orc = O.Oracle.from_semi(s)
+    x = cont.node_coordinates.reshape(-1, 2).T
+    u = np.ascontiguousarray(ic(x, 0.0, eq).T.reshape((cont.nelements, 4, 4, 4)))
+    orc.rhs(u)  # warm-up
+    t = time.perf_counter()
+    orc.rk_ck2n54(u, 0.0, 1e-4, 1)
+    one = time.perf_counter() - t
+    nsteps = max(1, int(seconds_target / max(one, 1e-6)))
+    t = time.perf_counter()
+    orc.rk_ck2n54(u, 0.0, 1e-4, nsteps)
+    el = time.perf_counter() - t
+    dofs = cont.nelements * (POLYDEG + 1) ** 2
+    return {"value": 5 * dofs * nsteps / el, "unit": METRIC, "cores": nthreads, "kind": "port",
+            "sample": f"{nsteps} CarpenterKennedy2N54 steps (5 rhs each) of the full level-7 workload, FP64, "
+                      f"oracle/trixi_oracle.c (CPU restatement of the reference algorithm, not Trixi.jl)",
+            "seconds": el}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(seconds_target=0.5, nthreads=nthreads)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(seconds_target=min(10.0, 60.0 / max(1, args.steps)), nthreads=nthreads))
+    value = statistics.median(v["value"] for v in vals)
+    ms = 5 * 16384 * 16 / value * 1e3
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Fourier initial condition)",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "elements": 16384, "dofs": 262144, "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": nthreads, "kind": "port",
+                         "sample": vals[0]["sample"]},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "Julia/Trixi.jl are not installed; the reference arm times the CPU restatement of its algorithm",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import trixicuda as T
+
+    flush = torch.empty(L2_BYTES // 4, dtype=torch.float32, device=device)
+    peaks = {}
+    mp = ROOT / "MEASURED_PEAKS.json"
+    if mp.exists():
+        peaks = json.loads(mp.read_text())
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    lib = T._lib.load()
+    fp64_peak = C.c_double()
+    fp32_peak = C.c_double()
+    T._lib.check(lib.trixi_probe_fma_peak(0, 4096, C.byref(fp64_peak), None))
+    T._lib.check(lib.trixi_probe_fma_peak(1, 16384, C.byref(fp32_peak), None))
+
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        step_ms, launch_ms, semi, u_mixed, dt = time_gpu_path("mixed", args.steps, args.warmup, device, flush)
+        step64, launch64, semi64, u64, _ = time_gpu_path("fp64", max(3, args.steps // 4), args.warmup, device, flush)
+    clocks = clk.summary()
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    dofs = semi.ndofs()
+    nv = semi.equations.nvariables
+    E = semi.nelements
+    per_step_updates = 5 * dofs
+    value = world * per_step_updates * args.steps / (total_ms * 1e-3)
+    ms_per_step = total_ms / args.steps
+    # algorithmic bytes of one fused RK-stage launch: read u, k; write u_out, k
+    # (stage 1 does not read k), plus J^{-1} and the face table
+    nval = dofs * nv
+    bytes_launch = [nval * 8 * (3 if s == 0 else 4) + E * 8 + E * 4 * 4 for s in range(5)]
+    mean_bytes = sum(bytes_launch) / 5
+    mean_launch_ms = statistics.mean(launch_ms)
+    achieved = mean_bytes / (mean_launch_ms * 1e-3) / 1e9
+    value64 = per_step_updates / (statistics.mean(step64) * 1e-3)
+    # equal-L2 check: 100 steps of mixed vs FP64 from the same state
+    l2 = l2_mixed_vs_fp64(semi, semi64, dt, nsteps=100)
+    e2e_ms, nbytes, _ = e2e_path("mixed", max(3, args.steps // 2), 3, device)
+    cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline()
+    traffic = None
+    prof = ROOT / "profiles" / "traffic_fused_rk_stage_euler2d_l7.json"
+    if prof.exists():
+        traffic = json.loads(prof.read_text()).get("mixed_bytes_per_launch")
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Fourier initial condition)",
+        "config": {"workload": WORKLOAD, "elements": E, "dofs": dofs, "nvars": nv,
+                   "precision": "mixed: rhs FP32, RK state FP64", "l2_flush": "256 MB write before each step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "kernel": "dg_fused_kernel (RK stage)", "algorithmic_bytes_per_launch": mean_bytes,
+                     "mean_launch_ms": mean_launch_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "fp64": {"value": value64, "unit": METRIC, "ms_per_step": statistics.mean(step64),
+                 "mean_launch_ms": statistics.mean(launch64),
+                 "fp64_fma_peak_tflops": fp64_peak.value / 1e12, "fp32_fma_peak_tflops": fp32_peak.value / 1e12},
+        "equal_l2": l2,
+        "e2e": {"value": per_step_updates / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "api": "trixicuda.rk_steps (C ABI trixi_rk_steps)"},
+        "cpu_baseline": cpu,
+        "gpu_launches": 5 * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def l2_mixed_vs_fp64(semi_mixed, semi64, dt, nsteps):
+    import torch
+
+    import trixicuda as T
+
+    u0 = semi64.compute_coefficients()
+    ua, ka = u0.clone(), torch.zeros_like(u0)
+    ub, kb = u0.clone(), torch.zeros_like(u0)
+    T.rk_steps(ua, ka, 0.0, dt, nsteps, semi64)
+    T.rk_steps(ub, kb, 0.0, dt, nsteps, semi_mixed)
+    torch.cuda.synchronize()
+    diff = (ua - ub).reshape(-1, semi64.equations.nvariables)
+    ref = ua.reshape(-1, semi64.equations.nvariables)
+    l2 = torch.sqrt(torch.mean(diff * diff, dim=0)).cpu().numpy()
+    linf = torch.max(torch.abs(diff), dim=0).values.cpu().numpy()
+    scale = torch.sqrt(torch.mean(ref * ref, dim=0)).cpu().numpy()
+    return {"steps": nsteps, "dt": dt, "l2_diff_per_var": l2.tolist(), "linf_diff_per_var": linf.tolist(),
+            "rel_l2": (l2 / scale).tolist(), "within_1e-6": bool(np.all(l2 < 1e-6))}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

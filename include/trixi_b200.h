@@ -1,0 +1,207 @@
+/*
+ * trixi_b200.h -- C ABI of libtrixi_b200.so, the GB300 (sm_103a) TreeMesh
+ * DGSEM right-hand side behind TrixiCUDA.jl's public API.
+ *
+ * The library replaces the device side of TrixiCUDA.jl's `rhs_gpu!` path
+ * (the `cuda_*` stage launchers and their CUDA.jl kernels).  Julia keeps its
+ * `DGSEMGPU` / `SemidiscretizationHyperbolicGPU` / `semidiscretizeGPU` API and
+ * calls these entry points with `ccall`; the binding is shown in
+ * INTEGRATION.md.  All arrays use the reference's layouts (column-major,
+ * first index fastest, integer tables 1-based Int64):
+ *
+ *   u, du, k             [nvars, N, (N, (N,)) nelements]           src/solvers/dg.jl:14-20
+ *   interfaces u         [2, nvars, (N, (N,)) ninterfaces]         src/solvers/containers_2d.jl:58
+ *   surface_flux_values  [nvars, (N, (N,)) 2*ndims, nelements]     src/solvers/containers_2d.jl:9
+ *   interface neighbor_ids [2, ninterfaces], orientations [ninterfaces]
+ *   mortar neighbor_ids  [2^(ndims-1)+1, nmortars]: small elements
+ *                        (2D: lower, upper; 3D: lower_left, lower_right,
+ *                        upper_left, upper_right) then the large element;
+ *                        large_sides [nmortars] (1: large element on the
+ *                        left), orientations [nmortars]
+ *
+ * Conventions.
+ *  - Every function returns a trixi_status (0 = TRIXI_OK).  No exceptions or
+ *    aborts cross the ABI.  trixi_last_error() describes the last failure.
+ *  - Device pointers (u, du, k, alpha) are owned by the caller (a Julia
+ *    CuArray or a torch tensor) and must live on the handle's device.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *    stream).  All compute calls are asynchronous on that stream; create and
+ *    destroy are synchronous.
+ *  - A handle is bound to the device current at trixi_create and is not
+ *    thread-safe; distinct handles may be used concurrently.
+ *  - No compute call allocates device memory after the first call that
+ *    needs a given buffer (the reference allocates per call,
+ *    src/solvers/dg_2d.jl:349,610).
+ */
+#ifndef TRIXI_B200_H
+#define TRIXI_B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TRIXI_ABI_VERSION 1
+
+typedef struct trixi_handle trixi_handle;
+
+typedef enum trixi_status {
+  TRIXI_OK = 0,
+  TRIXI_ERR_INVALID_ARGUMENT = 1, /* null/misaligned pointer, bad size, bad enum */
+  TRIXI_ERR_UNSUPPORTED = 2,      /* (ndims, polydeg, equation, flux) not built */
+  TRIXI_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+  TRIXI_ERR_DEVICE_FLAG = 4,      /* a kernel raised the device-side error word */
+  TRIXI_ERR_TIMEOUT = 5,          /* a bounded device wait ran out */
+  TRIXI_ERR_OUT_OF_MEMORY = 6,
+  TRIXI_ERR_BAD_CONNECTIVITY = 7  /* connectivity tables inconsistent */
+} trixi_status;
+
+typedef enum trixi_equation_kind {
+  TRIXI_EQ_LINEAR_ADVECTION = 0,   /* LinearScalarAdvectionEquation{1,2,3}D */
+  TRIXI_EQ_COMPRESSIBLE_EULER = 1  /* CompressibleEulerEquations{1,2,3}D */
+} trixi_equation_kind;
+
+typedef enum trixi_volume_integral_kind {
+  TRIXI_VOLUME_WEAK_FORM = 0,            /* VolumeIntegralWeakForm */
+  TRIXI_VOLUME_FLUX_DIFFERENCING = 1,    /* VolumeIntegralFluxDifferencing(volume_flux) */
+  TRIXI_VOLUME_SHOCK_CAPTURING_HG = 2    /* VolumeIntegralShockCapturingHG(indicator; dg, fv) */
+} trixi_volume_integral_kind;
+
+typedef enum trixi_flux_kind {
+  TRIXI_FLUX_LAX_FRIEDRICHS = 0,        /* flux_lax_friedrichs, Davis wave speed max(|v|+c) */
+  TRIXI_FLUX_RANOCHA = 1,               /* flux_ranocha */
+  TRIXI_FLUX_CENTRAL = 2,               /* flux_central */
+  TRIXI_FLUX_LAX_FRIEDRICHS_NAIVE = 3   /* LLF with max(|v_ll|,|v_rr|) + max(c_ll,c_rr) */
+} trixi_flux_kind;
+
+typedef enum trixi_precision_kind {
+  TRIXI_PRECISION_FP64 = 0,  /* everything in FP64 */
+  TRIXI_PRECISION_MIXED = 1  /* rhs in FP32, RK state and mortar projections in FP64 */
+} trixi_precision_kind;
+
+/* Problem description: the fields of DGSEMGPU + SemidiscretizationHyperbolicGPU
+ * plus the connectivity containers built by Trixi's init_* functions
+ * (src/solvers/cache.jl:60-88, src/solvers/containers_{1,2,3}d.jl).  Host
+ * pointers; the library copies what it needs. */
+typedef struct trixi_problem_desc {
+  int32_t struct_size;          /* sizeof(trixi_problem_desc) */
+  int32_t ndims;                /* 1, 2, 3 */
+  int32_t polydeg;              /* 1..5 */
+  int32_t nvars;                /* 1 (advection) or ndims+2 (Euler) */
+  int32_t equation;             /* trixi_equation_kind */
+  int32_t volume_integral;      /* trixi_volume_integral_kind */
+  int32_t volume_flux;          /* DG volume flux (flux differencing / shock capturing) */
+  int32_t surface_flux;         /* surface flux (interfaces, mortars) */
+  int32_t volume_flux_fv;       /* FV subcell flux (shock capturing) */
+  int32_t precision;            /* trixi_precision_kind */
+  double gamma;                 /* Euler ratio of specific heats */
+  double advection_velocity[3]; /* advection */
+  double alpha_max, alpha_min;  /* IndicatorHennemannGassner */
+  int32_t alpha_smooth;
+  int32_t indicator_variable;   /* 0 = density_pressure */
+  int64_t nelements;
+  const double *inverse_jacobian;        /* [nelements] */
+  int64_t ninterfaces;
+  const int64_t *interface_neighbor_ids; /* [2, ninterfaces] */
+  const int64_t *interface_orientations; /* [ninterfaces] */
+  int64_t nboundaries;                   /* must be 0: periodic TreeMesh */
+  int64_t nmortars;
+  const int64_t *mortar_neighbor_ids;    /* [2^(ndims-1)+1, nmortars] */
+  const int64_t *mortar_large_sides;     /* [nmortars] */
+  const int64_t *mortar_orientations;    /* [nmortars] */
+  /* Optional basis overrides (NULL = computed by the library), N x N
+   * column-major as in LobattoLegendreBasisGPU / MortarL2GPU
+   * (src/solvers/basis_lobatto_legendre.jl:60-100, 155-173). */
+  const double *weights;
+  const double *derivative_split;
+  const double *derivative_dhat;
+  const double *inverse_vandermonde_legendre;
+  const double *forward_upper, *forward_lower, *reverse_upper, *reverse_lower;
+} trixi_problem_desc;
+
+/* Library version string ("trixi_b200 <semver> sm_103a"). */
+const char *trixi_version(void);
+int trixi_abi_version(void);
+
+/* Builds the device-side cache.  Replaces SemidiscretizationHyperbolicGPU's
+ * create_cache_gpu (src/semidiscretization/semidiscretization_hyperbolic.jl:60-87,
+ * src/solvers/cache.jl:60-88) and the GPU basis of DGSEMGPU
+ * (src/solvers/dgsem_gpu.jl:43-53). */
+int trixi_create(const trixi_problem_desc *desc, trixi_handle **out);
+int trixi_destroy(trixi_handle *h);
+
+/* Message of the last failure of this handle (or of the calling thread when
+ * h == NULL).  Always NUL-terminates; returns the status of that failure. */
+int trixi_last_error(const trixi_handle *h, char *buf, size_t len);
+
+/* du = rhs(u, t), fully fused.  Replaces rhs_gpu!(du, u, t, mesh, ...)
+ * (src/solvers/dg_1d.jl:523-548, dg_2d.jl:760-790, dg_3d.jl:895-925) and its
+ * ODE-level wrapper rhs_gpu!(du_ode, u_ode, semi, t) (src/solvers/solvers.jl:18-31). */
+int trixi_rhs(trixi_handle *h, double *du, const double *u, double t, void *stream);
+
+/* One 2N low-storage RK stage, fused with the rhs:
+ *   k <- a*k + dt*rhs(u_in, t);  u_out <- u_in + b*k.
+ * u_out must not alias u_in (neighbour traces are read from u_in).  When
+ * a == 0, k is not read.  Replaces the OrdinaryDiffEq CarpenterKennedy2N54
+ * broadcast update around rhs_gpu! (examples/advection_basic_1d.jl:55). */
+int trixi_rk_stage(trixi_handle *h, double *u_out, const double *u_in, double *k,
+                   double a, double b, double dt, double t, void *stream);
+
+/* nsteps CarpenterKennedy2N54 steps of size dt from time t, in place in u
+ * (k is the 2N register).  Ping-pongs with a library-owned buffer. */
+int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt,
+                   int64_t nsteps, void *stream);
+
+/* Stage entry points with the reference's stage split (the de-facto API used
+ * by the reference tests, src/solvers/dg.jl:181-301, docs/src/reference.md:14-30).
+ * They compute in FP64 and fill the library-owned containers below. */
+int trixi_volume_integral(trixi_handle *h, double *du, const double *u, void *stream);  /* cuda_volume_integral! */
+int trixi_prolong2interfaces(trixi_handle *h, const double *u, void *stream);          /* cuda_prolong2interfaces! */
+int trixi_interface_flux(trixi_handle *h, void *stream);                               /* cuda_interface_flux! */
+int trixi_prolong2boundaries(trixi_handle *h, const double *u, void *stream);          /* cuda_prolong2boundaries! (periodic: no-op) */
+int trixi_boundary_flux(trixi_handle *h, double t, void *stream);                      /* cuda_boundary_flux! (periodic: no-op) */
+int trixi_prolong2mortars(trixi_handle *h, const double *u, void *stream);             /* cuda_prolong2mortars! */
+int trixi_mortar_flux(trixi_handle *h, void *stream);                                  /* cuda_mortar_flux! */
+int trixi_surface_integral(trixi_handle *h, double *du, void *stream);                 /* cuda_surface_integral! */
+int trixi_jacobian(trixi_handle *h, double *du, void *stream);                         /* cuda_jacobian! */
+int trixi_sources(trixi_handle *h, double *du, const double *u, double t, void *stream); /* cuda_sources! (none: no-op) */
+
+/* Library-owned containers (device pointers), mirroring cache_gpu fields. */
+typedef enum trixi_container_id {
+  TRIXI_CONTAINER_INTERFACES_U = 0,        /* cache.interfaces.u */
+  TRIXI_CONTAINER_SURFACE_FLUX_VALUES = 1, /* cache.elements.surface_flux_values */
+  TRIXI_CONTAINER_MORTARS_U = 2,           /* 2D: +0 u_upper, +1 u_lower; 3D: +0 u_upper_left,
+                                              +1 u_upper_right, +2 u_lower_left, +3 u_lower_right */
+  TRIXI_CONTAINER_ALPHA = 8,               /* shock-capturing blending factor [nelements] */
+  TRIXI_CONTAINER_INVERSE_JACOBIAN = 9
+} trixi_container_id;
+int trixi_container(trixi_handle *h, int which, void **dev_ptr, int64_t *count);
+
+/* Hennemann-Gassner indicator on the GPU: alpha[nelements] (device) from u,
+ * smoothed as configured.  Replaces the host round trip
+ * `indicator(Array(u), ...)` of src/solvers/dg_3d.jl:187 (indicators.jl:7-42). */
+int trixi_indicator(trixi_handle *h, const double *u, double *alpha, void *stream);
+
+/* Copies a basis operator to host memory: 0 nodes, 1 weights, 2 derivative_split,
+ * 3 derivative_dhat, 4 inverse_vandermonde_legendre, 5 forward_upper,
+ * 6 forward_lower, 7 reverse_upper, 8 reverse_lower, 9 derivative_matrix. */
+int trixi_basis(const trixi_handle *h, int which, double *host_out, int64_t count);
+
+/* Same operators without a handle (pure host code, no GPU needed). */
+int trixi_lgl_basis(int polydeg, int which, double *host_out, int64_t count);
+
+/* Diagnostic without a counterpart in the reference: measures the CUDA-core
+ * FMA throughput (FLOP/s, 2 per FMA) of the current device in FP64
+ * (TRIXI_PRECISION_FP64) or FP32 (TRIXI_PRECISION_MIXED), the roofline of
+ * the flux-differencing kernels.  Synchronizes the stream. */
+int trixi_probe_fma_peak(int precision, int iters, double *flops_per_s, void *stream);
+
+/* Waits for the handle's stream work, then checks the device error word. */
+int trixi_synchronize(trixi_handle *h, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRIXI_B200_H */

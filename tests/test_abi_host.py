@@ -1,0 +1,110 @@
+"""C ABI: the library loads, exports every entry point declared in
+include/trixi_b200.h, and its host-side validation rejects bad input with
+the documented status codes -- all without touching a GPU."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from trixicuda import _lib
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "trixi_b200.h"
+
+
+def declared_functions():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(trixi_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load(build_if_missing=True)
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(_lib.SIGNATURES), "ctypes signatures out of sync with the header"
+
+
+def test_version():
+    lib = _lib.load()
+    assert lib.trixi_version().decode().startswith("trixi_b200")
+    assert lib.trixi_abi_version() == 1
+
+
+def test_struct_size_matches_c():
+    # the C struct size is checked by trixi_create; a mismatch is INVALID_ARGUMENT
+    lib = _lib.load()
+    d = _lib.ProblemDesc()
+    d.struct_size = 12
+    h = C.c_void_p()
+    st = lib.trixi_create(C.byref(d), C.byref(h))
+    assert st == 1 and "struct_size" in _lib.last_error()
+
+
+def _desc_from_mesh(level=2, polydeg=3):
+    import trixicuda as T
+    from trixicuda.semidiscretization import build_problem_desc
+
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEMGPU(polydeg=polydeg, surface_flux=T.flux_ranocha,
+                        volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((-2, -2), (2, 2), initial_refinement_level=level)
+    return build_problem_desc(mesh, eq, solver)
+
+
+def _create(d):
+    h = C.c_void_p()
+    st = _lib.load().trixi_create(C.byref(d), C.byref(h))
+    return st, _lib.last_error()
+
+
+@pytest.mark.parametrize("field,value,status", [
+    ("ndims", 4, 1), ("polydeg", 9, 2), ("nvars", 3, 1), ("equation", 7, 1),
+    ("volume_integral", 5, 1), ("surface_flux", 9, 1), ("precision", 3, 1), ("nboundaries", 4, 2),
+    ("gamma", 1.0, 1), ("nelements", 0, 1),
+])
+def test_create_rejects_bad_fields(field, value, status):
+    d, keep, _ = _desc_from_mesh()
+    setattr(d, field, value)
+    st, msg = _create(d)
+    assert st == status, msg
+    assert msg
+
+
+def test_create_rejects_corrupted_connectivity():
+    d, keep, _ = _desc_from_mesh()
+    keep["if_nid"][3, 1] = 10_000          # neighbour id out of range
+    st, msg = _create(d)
+    assert st == 7 and "out of range" in msg
+    d, keep, _ = _desc_from_mesh()
+    keep["if_nid"][5] = keep["if_nid"][4]  # duplicated interface -> face connected twice
+    st, msg = _create(d)
+    assert st == 7 and "already connected" in msg
+    d, keep, _ = _desc_from_mesh()
+    d.ninterfaces = d.ninterfaces - 1      # a face left open (non-periodic)
+    st, msg = _create(d)
+    assert st == 7 and "has no interface" in msg
+    d, keep, _ = _desc_from_mesh()
+    keep["if_ori"][0] = 3                  # orientation out of range in 2D
+    st, msg = _create(d)
+    assert st == 7
+
+
+def test_null_arguments():
+    lib = _lib.load()
+    assert lib.trixi_create(None, None) == 1
+    assert lib.trixi_rhs(None, None, None, 0.0, None) == 1
+    assert lib.trixi_destroy(None) == 0
+    buf = C.create_string_buffer(4)
+    lib.trixi_last_error(None, buf, 4)
+    assert len(buf.value) <= 3  # truncated and NUL-terminated
+
+
+def test_lgl_basis_entry_point_rejects_bad_input():
+    lib = _lib.load()
+    out = np.zeros(4)
+    assert lib.trixi_lgl_basis(0, 0, out.ctypes.data_as(C.POINTER(C.c_double)), 4) == 1
+    assert lib.trixi_lgl_basis(3, 2, out.ctypes.data_as(C.POINTER(C.c_double)), 4) == 1  # 16 needed
+    assert lib.trixi_lgl_basis(3, 0, out.ctypes.data_as(C.POINTER(C.c_double)), 4) == 0

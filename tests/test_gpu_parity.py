@@ -1,0 +1,188 @@
+"""GPU parity: libtrixi_b200.so (through the C ABI) against the CPU oracle on
+identical inputs.  FP64 results must agree to 1e-12 relative (max norm,
+scaled by the largest oracle value); the FP32-mixed path to 5e-5.
+Mirrors the reference's stage-by-stage tests (test/tree_dgsem_2d/euler_ec.jl:60-122)."""
+import numpy as np
+import pytest
+
+import trixicuda as T
+from conftest import assert_rel
+from problems import semi_and_oracle
+
+pytestmark = pytest.mark.gpu
+
+RTOL64 = 1e-12
+RTOL_MIXED = 5e-5
+
+RHS_CASES = [
+    # kind, ndims, level, polydeg, refined, extra
+    ("adv_weak", 1, 4, 3, False, {}),                     # C1 set-up
+    ("adv_weak", 2, 3, 3, False, {}),
+    ("adv_weak", 2, 3, 3, True, {}),
+    ("adv_weak", 3, 2, 3, False, {}),
+    ("adv_weak", 3, 2, 3, True, {}),
+    ("adv_fd", 2, 3, 3, False, {}),
+    ("adv_weak", 2, 2, 3, False, dict(surface_flux=T.flux_central)),
+    ("euler_fd", 1, 4, 3, False, {}),
+    ("euler_fd", 2, 3, 3, False, {}),                     # C2 physics
+    ("euler_fd", 2, 3, 3, True, {}),
+    ("euler_fd", 3, 2, 3, False, {}),
+    ("euler_fd", 3, 2, 3, True, {}),
+    ("euler_fd", 2, 3, 3, False, dict(surface_flux=T.flux_lax_friedrichs)),
+    ("euler_fd", 2, 3, 3, False, dict(surface_flux=T.flux_lax_friedrichs_naive)),
+    ("euler_fd", 2, 3, 3, False, dict(surface_flux=T.flux_central, volume_flux=T.flux_central)),
+    ("euler_fd", 3, 2, 3, True, dict(surface_flux=T.flux_lax_friedrichs)),
+    ("euler_weak", 2, 3, 3, False, dict(surface_flux=T.flux_lax_friedrichs)),
+    ("euler_weak", 3, 2, 3, True, dict(surface_flux=T.flux_lax_friedrichs)),
+    ("euler_sc", 1, 5, 3, False, {}),
+    ("euler_sc", 2, 4, 3, False, {}),
+    ("euler_sc", 2, 3, 3, True, {}),
+    ("euler_sc", 3, 3, 3, False, {}),                     # C3 physics
+    ("euler_sc", 3, 2, 3, True, {}),
+    ("euler_sc", 3, 2, 3, False, dict(fv_flux=T.flux_ranocha, surface_flux=T.flux_ranocha)),
+    ("euler_sc", 2, 3, 3, False, dict(alpha_smooth=False)),
+] + [("euler_fd", 2, 2, p, False, {}) for p in (1, 2, 4, 5)] \
+  + [("adv_weak", 3, 1, p, True, {}) for p in (1, 2, 4, 5)] \
+  + [("euler_sc", 3, 2, p, False, {}) for p in (2, 4, 5)] \
+  + [("euler_fd", 3, 1, p, True, {}) for p in (2, 4, 5)]
+
+
+def _ids(c):
+    kind, d, lvl, p, ref, extra = c
+    return f"{kind}-{d}d-L{lvl}-p{p}{'-ref' if ref else ''}{'-' + '-'.join(map(str, extra.values())) if extra else ''}"
+
+
+def _u0(semi, cuda):
+    u_host = semi.compute_coefficients_host()
+    return u_host, cuda.from_numpy(u_host).to(semi.device)
+
+
+@pytest.mark.parametrize("case", RHS_CASES, ids=[_ids(c) for c in RHS_CASES])
+def test_rhs_matches_oracle(case, cuda):
+    kind, d, level, p, refined, extra = case
+    semi, orc = semi_and_oracle(kind, d, level, polydeg=p, refined=refined, **extra)
+    u_host, u = _u0(semi, cuda)
+    du = cuda.empty_like(u)
+    T.rhs_gpu(du, u, semi, 0.0)
+    T.synchronize(semi)
+    assert_rel(du.cpu().numpy(), orc.rhs(u_host), RTOL64, "rhs")
+
+
+MIXED_CASES = [("adv_weak", 2, 3, 3, True, {}), ("euler_fd", 2, 3, 3, False, {}), ("euler_fd", 3, 2, 3, True, {}),
+               ("euler_sc", 3, 3, 3, False, {}), ("euler_weak", 2, 3, 3, False, dict(surface_flux=T.flux_lax_friedrichs))]
+
+
+@pytest.mark.parametrize("case", MIXED_CASES, ids=[_ids(c) for c in MIXED_CASES])
+def test_mixed_rhs_close_to_oracle(case, cuda):
+    kind, d, level, p, refined, extra = case
+    semi, orc = semi_and_oracle(kind, d, level, polydeg=p, refined=refined, precision="mixed", **extra)
+    u_host, u = _u0(semi, cuda)
+    du = cuda.empty_like(u)
+    T.rhs_gpu(du, u, semi, 0.0)
+    T.synchronize(semi)
+    assert_rel(du.cpu().numpy(), orc.rhs(u_host), RTOL_MIXED, "mixed rhs")
+
+
+STAGE_CASES = [("adv_weak", 2, 3, 3, True, {}), ("euler_fd", 2, 3, 3, True, {}), ("euler_fd", 3, 2, 3, True, {}),
+               ("euler_sc", 3, 2, 3, True, {}), ("euler_fd", 1, 3, 3, False, {}),
+               ("euler_weak", 3, 2, 3, True, dict(surface_flux=T.flux_lax_friedrichs))]
+
+
+@pytest.mark.parametrize("case", STAGE_CASES, ids=[_ids(c) for c in STAGE_CASES])
+def test_stages_match_oracle(case, cuda):
+    """Stage-by-stage, as the reference tests do (volume integral,
+    prolong2interfaces, interface flux, mortars, surface integral, jacobian)."""
+    kind, d, level, p, refined, extra = case
+    semi, orc = semi_and_oracle(kind, d, level, polydeg=p, refined=refined, **extra)
+    u_host, u = _u0(semi, cuda)
+    du = cuda.empty_like(u)
+    alpha = orc.indicator(u_host) if kind == "euler_sc" else None
+    T.cuda_volume_integral(du, u, semi)
+    du_o = orc.volume_integral(u_host, alpha)
+    assert_rel(du.cpu().numpy(), du_o, RTOL64, "volume integral")
+    T.cuda_prolong2interfaces(u, semi)
+    iu_o = orc.prolong2interfaces(u_host)
+    iu = semi.container(T._lib.CONTAINER_INTERFACES_U)
+    assert_rel(iu.cpu().numpy(), iu_o, 0.0, "interfaces.u")
+    T.cuda_interface_flux(semi)
+    sfv_o = orc.interface_flux(iu_o)
+    T.cuda_prolong2boundaries(u, semi)
+    T.cuda_boundary_flux(0.0, semi)
+    T.cuda_prolong2mortars(u, semi)
+    if semi.containers.nmortars:
+        arrs_o = orc.prolong2mortars(u_host)
+        nc = 2 ** (d - 1)
+        order = [1, 0] if d == 2 else [2, 3, 0, 1]  # reference container order -> child index
+        for j in range(nc):
+            got = semi.container(T._lib.CONTAINER_MORTARS_U + j).cpu().numpy()
+            assert_rel(got, arrs_o[order[j]], 1e-14, f"mortar u {j}")
+        orc.mortar_flux(arrs_o, sfv_o)
+    T.cuda_mortar_flux(semi)
+    sfv = semi.container(T._lib.CONTAINER_SURFACE_FLUX_VALUES)
+    assert_rel(sfv.cpu().numpy(), sfv_o, RTOL64, "surface_flux_values")
+    T.cuda_surface_integral(du, semi)
+    du_o = orc.surface_integral(du_o, sfv_o)
+    assert_rel(du.cpu().numpy(), du_o, RTOL64, "surface integral")
+    T.cuda_jacobian(du, semi)
+    du_o = orc.jacobian(du_o)
+    assert_rel(du.cpu().numpy(), du_o, RTOL64, "jacobian")
+    T.cuda_sources(du, u, 0.0, semi)
+    T.synchronize(semi)
+    assert_rel(du.cpu().numpy(), orc.rhs(u_host), RTOL64, "staged == fused oracle rhs")
+
+
+@pytest.mark.parametrize("d,level,refined,smooth", [(3, 3, False, True), (2, 4, True, True), (3, 2, True, False)])
+def test_indicator_matches_oracle(d, level, refined, smooth, cuda):
+    semi, orc = semi_and_oracle("euler_sc", d, level, refined=refined, alpha_smooth=smooth)
+    u_host, u = _u0(semi, cuda)
+    alpha = cuda.zeros(semi.nelements, dtype=cuda.float64, device=semi.device)
+    T.cuda_indicator(u, alpha, semi)
+    a_o = orc.indicator(u_host)
+    a = alpha.cpu().numpy()
+    assert np.max(np.abs(a - a_o)) < 1e-12
+    assert np.count_nonzero(a_o) > 0  # the blast wave triggers the indicator
+
+
+@pytest.mark.parametrize("kind,d,level,refined", [("adv_weak", 1, 4, False), ("euler_fd", 2, 3, True),
+                                                  ("euler_sc", 3, 2, False), ("adv_weak", 3, 2, True)])
+def test_rk_steps_match_oracle(kind, d, level, refined, cuda):
+    semi, orc = semi_and_oracle(kind, d, level, refined=refined)
+    u_host, u = _u0(semi, cuda)
+    k = cuda.zeros_like(u)
+    dt = 0.2 / float(np.max(semi.containers.inverse_jacobian)) / 4
+    for nsteps in (1, 2):
+        uu = u.clone()
+        kk = k.clone()
+        T.rk_steps(uu, kk, 0.0, dt, nsteps, semi)
+        T.synchronize(semi)
+        u_o, k_o = orc.rk_ck2n54(u_host, 0.0, dt, nsteps)
+        assert_rel(uu.cpu().numpy(), u_o, 1e-13, f"u after {nsteps} steps")
+        assert_rel(kk.cpu().numpy(), k_o, 1e-11, f"k after {nsteps} steps")
+
+
+def test_rk_stage_semantics(cuda):
+    """k <- a k + dt rhs(u_in); u_out <- u_in + b k."""
+    semi, orc = semi_and_oracle("euler_fd", 2, 3)
+    u_host, u = _u0(semi, cuda)
+    k = cuda.from_numpy(np.random.default_rng(0).standard_normal(u_host.shape)).to(semi.device)
+    k0 = k.cpu().numpy()
+    u_out = cuda.empty_like(u)
+    a, b, dt = -0.4, 0.3, 1e-3
+    T.rk_stage(u_out, u, k, a, b, dt, 0.0, semi)
+    T.synchronize(semi)
+    du_o = orc.rhs(u_host)
+    k_exp = a * k0 + dt * du_o
+    assert_rel(k.cpu().numpy(), k_exp, 1e-12, "k")
+    assert_rel(u_out.cpu().numpy(), u_host + b * k_exp, 1e-14, "u_out")
+
+
+def test_rhs_rejects_bad_pointers(cuda):
+    import ctypes as C
+
+    semi, _ = semi_and_oracle("adv_weak", 2, 2)
+    lib = T._lib.load()
+    u = cuda.zeros(semi.u_shape(), dtype=cuda.float64, device=semi.device)
+    st = lib.trixi_rhs(semi.handle, C.c_void_p(u.data_ptr() + 4), C.c_void_p(u.data_ptr()), 0.0, None)
+    assert st == 1
+    st = lib.trixi_rhs(semi.handle, C.c_void_p(u.data_ptr()), C.c_void_p(u.data_ptr()), 0.0, None)
+    assert st == 1  # du aliases u

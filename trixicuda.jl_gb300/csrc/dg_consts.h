@@ -1,0 +1,23 @@
+// dg_consts.h -- enumerations shared by host code and kernels.  The numeric
+// values equal the public trixi_* enums of include/trixi_b200.h.
+#pragma once
+
+namespace trixi {
+
+constexpr int EQ_ADV = 0;    // TRIXI_EQ_LINEAR_ADVECTION
+constexpr int EQ_EULER = 1;  // TRIXI_EQ_COMPRESSIBLE_EULER
+
+constexpr int FLUX_LLF = 0;        // TRIXI_FLUX_LAX_FRIEDRICHS
+constexpr int FLUX_RANOCHA = 1;    // TRIXI_FLUX_RANOCHA
+constexpr int FLUX_CENTRAL = 2;    // TRIXI_FLUX_CENTRAL
+constexpr int FLUX_LLF_NAIVE = 3;  // TRIXI_FLUX_LAX_FRIEDRICHS_NAIVE
+
+constexpr int VOL_WEAK = 0;  // TRIXI_VOLUME_WEAK_FORM
+constexpr int VOL_FD = 1;    // TRIXI_VOLUME_FLUX_DIFFERENCING
+constexpr int VOL_SC = 2;    // TRIXI_VOLUME_SHOCK_CAPTURING_HG
+
+constexpr int MODE_VOLUME = 0;  // du = volume integral only (stage API)
+constexpr int MODE_RHS = 1;     // du = full rhs
+constexpr int MODE_RK = 2;      // k = a k + dt rhs; u_out = u_in + b k
+
+}  // namespace trixi

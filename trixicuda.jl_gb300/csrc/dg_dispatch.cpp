@@ -1,0 +1,25 @@
+// dg_dispatch.cpp -- selects the compiled fused-kernel instantiation.
+#include "dg_host.h"
+
+namespace trixi {
+
+bool fused_supported(int dim, int N, int eq, int vol, int vflux) {
+  if (dim < 1 || dim > 3 || N < 2 || N > HOST_NMAX) return false;
+  if (eq == 0) return vol == 0 || (vol == 1 && vflux == 2);  // advection: weak form, central flux differencing
+  if (vol == 0) return true;
+  if (vol == 1 || vol == 2) return vflux == 1 || vflux == 2;  // flux_ranocha, flux_central
+  return false;
+}
+
+cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed, const FusedHost &h,
+                         cudaStream_t s) {
+  if (!fused_supported(dim, N, eq, vol, vflux)) return cudaErrorNotSupported;
+  switch (dim) {
+    case 1: return mixed ? launch_fused_1d_f32(N, eq, vol, vflux, h, s) : launch_fused_1d_f64(N, eq, vol, vflux, h, s);
+    case 2: return mixed ? launch_fused_2d_f32(N, eq, vol, vflux, h, s) : launch_fused_2d_f64(N, eq, vol, vflux, h, s);
+    case 3: return mixed ? launch_fused_3d_f32(N, eq, vol, vflux, h, s) : launch_fused_3d_f64(N, eq, vol, vflux, h, s);
+  }
+  return cudaErrorNotSupported;
+}
+
+}  // namespace trixi

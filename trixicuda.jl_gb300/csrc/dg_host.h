@@ -1,0 +1,106 @@
+// dg_host.h -- host-side interface between the C ABI layer and the kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dg_consts.h"
+
+namespace trixi {
+
+constexpr int HOST_NMAX = 6;  // largest N = polydeg + 1 with compiled kernels
+
+// Launch arguments of the fused kernel, precision independent.
+struct FusedHost {
+  const double *u_in = nullptr;
+  double *out = nullptr;
+  double *k = nullptr;
+  const int32_t *face_table = nullptr;
+  const double *mortar_flux = nullptr;
+  const double *inv_jac = nullptr;
+  const double *alpha = nullptr;
+  int *err = nullptr;
+  int64_t nelements = 0;
+  int mode = 1;
+  int surface_flux = 0, fv_flux = 0;
+  double rk_a = 0, rk_b = 0, dt = 0, atol = 0;
+  double gamma = 1.4;
+  double adv[3] = {0, 0, 0};
+  int N = 0;
+  double dsplit[HOST_NMAX * HOST_NMAX] = {};  // row-major, diagonal zeroed
+  double dhat[HOST_NMAX * HOST_NMAX] = {};    // row-major
+  double invw[HOST_NMAX] = {};
+  double lhat_l = 0, lhat_r = 0;
+  int epb = 0;  // elements per block, 0 = default
+};
+
+// Returns cudaErrorNotSupported when the combination is not compiled.
+cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed, const FusedHost &h,
+                         cudaStream_t s);
+bool fused_supported(int dim, int N, int eq, int vol, int vflux);
+int fused_default_epb(int dim, int N, int eq);
+
+cudaError_t launch_fused_1d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_2d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_3d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_1d_f32(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_2d_f32(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_3d_f32(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+
+// Auxiliary kernels (dg_aux.cu).
+struct MortarHost {
+  int dim = 2, N = 0, eq = 0, nv = 1;
+  int64_t nmortars = 0;
+  const double *u = nullptr;
+  const int64_t *neighbor_ids = nullptr;  // [nchild+1, M] 1-based
+  const int64_t *large_sides = nullptr;
+  const int64_t *orientations = nullptr;
+  double *mortar_flux = nullptr;           // [M*(nchild+1)][NF][NV]
+  int surface_flux = 0;
+  bool mixed = false;
+  double gamma = 1.4, adv[3] = {0, 0, 0};
+  double fwd_up[HOST_NMAX * HOST_NMAX] = {}, fwd_lo[HOST_NMAX * HOST_NMAX] = {};  // row-major [j][i]
+  double rev_up[HOST_NMAX * HOST_NMAX] = {}, rev_lo[HOST_NMAX * HOST_NMAX] = {};  // row-major [k][j]
+  int *err = nullptr;
+};
+cudaError_t launch_mortar_flux(const MortarHost &m, cudaStream_t s);
+
+struct IndicatorHost {
+  int dim = 2, N = 0, nv = 4;
+  int64_t nelements = 0;
+  const double *u = nullptr;
+  double *alpha_raw = nullptr;
+  double *alpha = nullptr;                 // smoothed output
+  const int32_t *face_table = nullptr;     // [E][2*DIM]
+  const int32_t *slot_neighbors = nullptr; // [slot][4] element ids (-1 padded) for mortar faces
+  int smooth = 1;
+  double gamma = 1.4;
+  double alpha_max = 0.5, alpha_min = 0.001;
+  double threshold = 0, parameter_s = 0;
+  double ivdm[HOST_NMAX * HOST_NMAX] = {};  // row-major inverse Vandermonde
+};
+cudaError_t launch_indicator(const IndicatorHost &ih, cudaStream_t s);
+
+// Stage kernels with the reference's stage split (FP64).
+struct StageHost {
+  int dim = 2, N = 0, nv = 1, eq = 0;
+  int64_t nelements = 0, ninterfaces = 0, nmortars = 0;
+  const int64_t *if_neighbor_ids = nullptr, *if_orientations = nullptr;
+  const int64_t *mo_neighbor_ids = nullptr, *mo_large_sides = nullptr, *mo_orientations = nullptr;
+  double *interfaces_u = nullptr;
+  double *sfv = nullptr;
+  double *mortar_u[4] = {nullptr, nullptr, nullptr, nullptr};
+  int surface_flux = 0;
+  double gamma = 1.4, adv[3] = {0, 0, 0};
+  double fwd_up[HOST_NMAX * HOST_NMAX] = {}, fwd_lo[HOST_NMAX * HOST_NMAX] = {};
+  double rev_up[HOST_NMAX * HOST_NMAX] = {}, rev_lo[HOST_NMAX * HOST_NMAX] = {};
+  double lhat_l = 0, lhat_r = 0;
+  const double *inv_jac = nullptr;
+};
+cudaError_t stage_prolong2interfaces(const StageHost &sh, const double *u, cudaStream_t s);
+cudaError_t stage_interface_flux(const StageHost &sh, cudaStream_t s);
+cudaError_t stage_prolong2mortars(const StageHost &sh, const double *u, cudaStream_t s);
+cudaError_t stage_mortar_flux(const StageHost &sh, cudaStream_t s);
+cudaError_t stage_surface_integral(const StageHost &sh, double *du, cudaStream_t s);
+cudaError_t stage_jacobian(const StageHost &sh, double *du, cudaStream_t s);
+
+}  // namespace trixi

@@ -1,0 +1,107 @@
+// dg_launch.cuh -- instantiation and launch of the fused kernel for one
+// (dimension, compute precision).  Included by fused_{1,2,3}d_{f64,f32}.cu,
+// which are compiled in parallel.
+#pragma once
+#include <algorithm>
+
+#include "dg_fused.cuh"
+#include "dg_host.h"
+
+namespace trixi {
+
+inline int default_epb(int dim, int N, int nv) {
+  // aim at ~128-256 line threads per block
+  int nf = 1;
+  for (int d = 1; d < dim; ++d) nf *= N;
+  const int lines = dim * nf;
+  int epb = std::max(1, 192 / lines);
+  (void)nv;
+  return std::min(epb, 32);
+}
+
+template <int DIM, int N, int EQ, typename R, int VOL, int VF>
+cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
+  using K = FusedKernel<DIM, N, EQ, R, VOL, VF>;
+  FusedParams<R> p;
+  p.u_in = h.u_in;
+  p.out = h.out;
+  p.k = h.k;
+  p.face_table = h.face_table;
+  p.mortar_flux = h.mortar_flux;
+  p.inv_jac = h.inv_jac;
+  p.alpha = h.alpha;
+  p.err = h.err;
+  p.nelements = h.nelements;
+  p.mode = h.mode;
+  p.surface_flux = h.surface_flux;
+  p.fv_flux = h.fv_flux;
+  p.rk_a = h.rk_a;
+  p.rk_b = h.rk_b;
+  p.dt = h.dt;
+  p.atol = h.atol;
+  p.pp.gamma = R(h.gamma);
+  p.pp.gm1 = R(h.gamma - 1.0);
+  p.pp.inv_gm1 = R(1.0 / (h.gamma - 1.0));
+  for (int d = 0; d < 3; ++d) p.pp.a[d] = R(h.adv[d]);
+  for (int i = 0; i < NMAXT * NMAXT; ++i) {
+    p.dsplit[i] = R(0);
+    p.dhat[i] = R(0);
+  }
+  for (int i = 0; i < N * N; ++i) {
+    p.dsplit[i] = R(h.dsplit[i]);
+    p.dhat[i] = R(h.dhat[i]);
+  }
+  for (int i = 0; i < NMAXT; ++i) p.invw[i] = R(i < N ? h.invw[i] : 0.0);
+  p.lhat_l = R(h.lhat_l);
+  p.lhat_r = R(h.lhat_r);
+  int epb = h.epb > 0 ? h.epb : default_epb(DIM, N, K::NV);
+  p.epb = epb;
+  const int threads_needed = epb * K::LINES;
+  int block = ((threads_needed + 31) / 32) * 32;
+  block = std::max(64, std::min(256, block));
+  const size_t smem = K::smem_bytes(epb);
+  // opt in once per instantiation to the large dynamic shared-memory carve-out
+  static const cudaError_t attr = cudaFuncSetAttribute(dg_fused_kernel<DIM, N, EQ, R, VOL, VF>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  if (attr != cudaSuccess) return attr;
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  const int64_t grid = (h.nelements + epb - 1) / epb;
+  if (grid <= 0) return cudaSuccess;
+  if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+  dg_fused_kernel<DIM, N, EQ, R, VOL, VF><<<(unsigned)grid, block, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <int DIM, int N, typename R>
+cudaError_t launch_n(int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s) {
+  if (eq == EQ_ADV) {
+    if (vol == VOL_WEAK) return launch_one<DIM, N, EQ_ADV, R, VOL_WEAK, FLUX_CENTRAL>(h, s);
+    if (vol == VOL_FD) return launch_one<DIM, N, EQ_ADV, R, VOL_FD, FLUX_CENTRAL>(h, s);
+    return cudaErrorNotSupported;
+  }
+  if (vol == VOL_WEAK) return launch_one<DIM, N, EQ_EULER, R, VOL_WEAK, FLUX_CENTRAL>(h, s);
+  if (vol == VOL_FD) {
+    if (vflux == FLUX_RANOCHA) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_RANOCHA>(h, s);
+    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_CENTRAL>(h, s);
+    return cudaErrorNotSupported;
+  }
+  if (vol == VOL_SC) {
+    if (vflux == FLUX_RANOCHA) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_RANOCHA>(h, s);
+    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_CENTRAL>(h, s);
+  }
+  return cudaErrorNotSupported;
+}
+
+template <int DIM, typename R>
+cudaError_t launch_dim(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s) {
+  switch (N) {
+    case 2: return launch_n<DIM, 2, R>(eq, vol, vflux, h, s);
+    case 3: return launch_n<DIM, 3, R>(eq, vol, vflux, h, s);
+    case 4: return launch_n<DIM, 4, R>(eq, vol, vflux, h, s);
+    case 5: return launch_n<DIM, 5, R>(eq, vol, vflux, h, s);
+    case 6: return launch_n<DIM, 6, R>(eq, vol, vflux, h, s);
+    default: return cudaErrorNotSupported;
+  }
+}
+
+}  // namespace trixi

@@ -1,0 +1,685 @@
+// trixi_api.cu -- the C ABI of libtrixi_b200.so (declared in include/trixi_b200.h).
+//
+// Host runtime: validates the problem description and connectivity, builds
+// the per-element face table (one int32 per element face: the neighbour
+// element, or a mortar-flux slot), uploads tables and basis operators, owns
+// scratch buffers, and sequences the kernels of one rhs / RK stage on the
+// caller's stream.  Every entry point returns a trixi_status; nothing throws
+// across the ABI.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/trixi_b200.h"
+#include "basis.h"
+#include "dg_host.h"
+
+using namespace trixi;
+
+namespace {
+
+thread_local std::string g_last_error;
+thread_local int g_last_status = TRIXI_OK;
+
+// CarpenterKennedy2N54 coefficients (Carpenter & Kennedy 1994, NASA TM-109112).  The
+// stage times t + c_s dt are not needed: the semidiscretization is autonomous
+// (periodic boundaries, no source terms).
+const double kCK_A[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                         -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+const double kCK_B[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                         1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                         2277821191437.0 / 14882151754819.0};
+
+}  // namespace
+
+struct trixi_handle {
+  int device = 0;
+  int dim = 0, N = 0, nv = 0, NN = 0, NF = 0, nchild = 1;
+  int eq = 0, vol = 0, vflux = 0, sflux = 0, fvflux = 0;
+  bool mixed = false;
+  double gamma = 1.4, adv[3] = {0, 0, 0};
+  double alpha_max = 0.5, alpha_min = 0.001;
+  int alpha_smooth = 1;
+  int64_t E = 0, I = 0, M = 0;
+  Basis basis;
+  // device tables
+  int32_t *d_face_table = nullptr;
+  int32_t *d_slot_nbrs = nullptr;
+  double *d_inv_jac = nullptr;
+  int64_t *d_if_nid = nullptr, *d_if_ori = nullptr;
+  int64_t *d_mo_nid = nullptr, *d_mo_ls = nullptr, *d_mo_ori = nullptr;
+  double *d_mortar_flux = nullptr;
+  double *d_alpha_raw = nullptr, *d_alpha = nullptr;
+  int *d_err = nullptr;
+  double *d_scratch_u = nullptr;
+  // stage containers (allocated on first use)
+  double *d_interfaces_u = nullptr, *d_sfv = nullptr, *d_mortar_u[4] = {nullptr, nullptr, nullptr, nullptr};
+  int epb = 0;
+  FusedHost fused;
+  std::string last_error;
+  int last_status = TRIXI_OK;
+};
+
+namespace {
+
+int fail(trixi_handle *h, int status, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  g_last_status = status;
+  if (h) {
+    h->last_error = buf;
+    h->last_status = status;
+  }
+  return status;
+}
+
+int cuda_fail(trixi_handle *h, cudaError_t e, const char *what) {
+  if (e == cudaErrorNotSupported) return fail(h, TRIXI_ERR_UNSUPPORTED, "%s: combination not compiled", what);
+  if (e == cudaErrorMemoryAllocation) return fail(h, TRIXI_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  return fail(h, TRIXI_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define TRIXI_CUDA(h, expr, what)                     \
+  do {                                                \
+    cudaError_t e_ = (expr);                          \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
+  } while (0)
+
+bool aligned8(const void *p) { return p && ((uintptr_t)p % 8 == 0); }
+
+template <typename T>
+cudaError_t upload(T **dst, const T *src, size_t n) {
+  if (n == 0) {
+    *dst = nullptr;
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaMalloc((void **)dst, n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void free_all(trixi_handle *h) {
+  void *ptrs[] = {h->d_face_table, h->d_slot_nbrs, h->d_inv_jac, h->d_if_nid, h->d_if_ori, h->d_mo_nid,
+                  h->d_mo_ls, h->d_mo_ori, h->d_mortar_flux, h->d_alpha_raw, h->d_alpha, h->d_err,
+                  h->d_scratch_u, h->d_interfaces_u, h->d_sfv, h->d_mortar_u[0], h->d_mortar_u[1],
+                  h->d_mortar_u[2], h->d_mortar_u[3]};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+}
+
+// row-major copies of the column-major basis for the kernels
+void to_row_major(const std::vector<double> &cm, int n, double *rm) {
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) rm[i * n + j] = cm[i + (size_t)n * j];
+}
+
+int64_t ipow64(int64_t b, int e) {
+  int64_t r = 1;
+  while (e-- > 0) r *= b;
+  return r;
+}
+
+int check_u_args(trixi_handle *h, const void *a, const char *name) {
+  if (!aligned8(a)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "%s is null or not 8-byte aligned", name);
+  return TRIXI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *trixi_version(void) { return "trixi_b200 0.1.0 sm_103a"; }
+int trixi_abi_version(void) { return TRIXI_ABI_VERSION; }
+
+int trixi_last_error(const trixi_handle *h, char *buf, size_t len) {
+  const std::string &msg = h ? h->last_error : g_last_error;
+  if (buf && len > 0) {
+    size_t n = std::min(len - 1, msg.size());
+    std::memcpy(buf, msg.data(), n);
+    buf[n] = '\0';
+  }
+  return h ? h->last_status : g_last_status;
+}
+
+int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
+  if (!out) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "out is null");
+  *out = nullptr;
+  if (!d) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "desc is null");
+  if (d->struct_size != (int32_t)sizeof(trixi_problem_desc))
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "desc.struct_size %d != %d", d->struct_size,
+                (int)sizeof(trixi_problem_desc));
+  if (d->ndims < 1 || d->ndims > 3) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "ndims %d", d->ndims);
+  if (d->polydeg < 1 || d->polydeg + 1 > HOST_NMAX)
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "polydeg %d (supported 1..%d)", d->polydeg, HOST_NMAX - 1);
+  if (d->equation != TRIXI_EQ_LINEAR_ADVECTION && d->equation != TRIXI_EQ_COMPRESSIBLE_EULER)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "equation %d", d->equation);
+  const int nv_expect = d->equation == TRIXI_EQ_LINEAR_ADVECTION ? 1 : d->ndims + 2;
+  if (d->nvars != nv_expect)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "nvars %d, equation needs %d", d->nvars, nv_expect);
+  if (d->volume_integral < 0 || d->volume_integral > 2)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "volume_integral %d", d->volume_integral);
+  for (int f : {d->volume_flux, d->surface_flux, d->volume_flux_fv})
+    if (f < 0 || f > 3) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux enum %d", f);
+  if (d->precision != TRIXI_PRECISION_FP64 && d->precision != TRIXI_PRECISION_MIXED)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "precision %d", d->precision);
+  if (d->nelements <= 0 || d->nelements > INT32_MAX)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "nelements %lld", (long long)d->nelements);
+  if (!d->inverse_jacobian) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "inverse_jacobian is null");
+  if (d->ninterfaces < 0 || (d->ninterfaces > 0 && (!d->interface_neighbor_ids || !d->interface_orientations)))
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "interface tables");
+  if (d->nboundaries != 0)
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "non-periodic boundaries (nboundaries=%lld)", (long long)d->nboundaries);
+  if (d->nmortars < 0 || (d->nmortars > 0 && (!d->mortar_neighbor_ids || !d->mortar_large_sides || !d->mortar_orientations)))
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "mortar tables");
+  if (d->nmortars > 0 && d->ndims == 1) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "mortars in 1D");
+  if (d->equation == TRIXI_EQ_COMPRESSIBLE_EULER && !(d->gamma > 1.0))
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "gamma %g", d->gamma);
+
+  trixi_handle *h = new trixi_handle();
+  h->dim = d->ndims;
+  h->N = d->polydeg + 1;
+  h->nv = d->nvars;
+  h->NF = (int)ipow64(h->N, h->dim - 1);
+  h->NN = h->NF * h->N;
+  h->nchild = 1 << (h->dim - 1);
+  h->eq = d->equation == TRIXI_EQ_LINEAR_ADVECTION ? EQ_ADV : EQ_EULER;
+  h->vol = d->volume_integral;
+  h->vflux = d->volume_flux;
+  h->sflux = d->surface_flux;
+  h->fvflux = d->volume_flux_fv;
+  // the entropy-conservative flux of linear advection is the central flux
+  if (h->eq == EQ_ADV && h->vflux == TRIXI_FLUX_RANOCHA) h->vflux = TRIXI_FLUX_CENTRAL;
+  h->mixed = d->precision == TRIXI_PRECISION_MIXED;
+  h->gamma = d->gamma;
+  for (int i = 0; i < 3; ++i) h->adv[i] = d->advection_velocity[i];
+  h->alpha_max = d->alpha_max;
+  h->alpha_min = d->alpha_min;
+  h->alpha_smooth = d->alpha_smooth;
+  h->E = d->nelements;
+  h->I = d->ninterfaces;
+  h->M = d->nmortars;
+  if (!fused_supported(h->dim, h->N, h->eq, h->vol, h->vflux)) {
+    int st = fail(nullptr, TRIXI_ERR_UNSUPPORTED, "volume integral %d with volume flux %d for equation %d",
+                  h->vol, h->vflux, h->eq);
+    delete h;
+    return st;
+  }
+  if (!compute_basis(d->polydeg, h->basis)) {
+    delete h;
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "basis for polydeg %d", d->polydeg);
+  }
+  {  // optional overrides with the caller's (e.g. Trixi.jl's) operators
+    const size_t nn = (size_t)h->N * h->N;
+    auto take = [&](const double *src, std::vector<double> &dst, size_t n) {
+      if (src) dst.assign(src, src + n);
+    };
+    take(d->weights, h->basis.weights, h->N);
+    take(d->derivative_split, h->basis.dsplit, nn);
+    take(d->derivative_dhat, h->basis.dhat, nn);
+    take(d->inverse_vandermonde_legendre, h->basis.ivdm, nn);
+    take(d->forward_upper, h->basis.fwd_up, nn);
+    take(d->forward_lower, h->basis.fwd_lo, nn);
+    take(d->reverse_upper, h->basis.rev_up, nn);
+    take(d->reverse_lower, h->basis.rev_lo, nn);
+  }
+
+  // face table: one entry per element face (direction 2*(o-1) = -o face,
+  // 2*(o-1)+1 = +o face, the surface_flux_values direction order)
+  const int nfaces = 2 * h->dim;
+  const int nc = h->nchild;
+  std::vector<int32_t> ft((size_t)h->E * nfaces, INT32_MIN);
+  std::vector<int32_t> slot_nbrs((size_t)std::max<int64_t>(1, h->M * (nc + 1)) * 4, -1);
+  auto bad = [&](const char *fmt, long long a, long long b) {
+    int st = fail(nullptr, TRIXI_ERR_BAD_CONNECTIVITY, fmt, a, b);
+    delete h;
+    return st;
+  };
+  for (int64_t k = 0; k < h->I; ++k) {
+    const int64_t l = d->interface_neighbor_ids[2 * k], r = d->interface_neighbor_ids[2 * k + 1];
+    const int64_t o = d->interface_orientations[k];
+    if (l < 1 || l > h->E || r < 1 || r > h->E) return bad("interface %lld: neighbour id out of range (%lld)", (long long)k + 1, (long long)(l < 1 || l > h->E ? l : r));
+    if (o < 1 || o > h->dim) return bad("interface %lld: orientation %lld", (long long)k + 1, (long long)o);
+    int32_t &fl = ft[(size_t)(l - 1) * nfaces + 2 * (o - 1) + 1];
+    int32_t &fr = ft[(size_t)(r - 1) * nfaces + 2 * (o - 1)];
+    if (fl != INT32_MIN || fr != INT32_MIN) return bad("interface %lld: face already connected (orientation %lld)", (long long)k + 1, (long long)o);
+    fl = (int32_t)(r - 1);
+    fr = (int32_t)(l - 1);
+  }
+  for (int64_t m = 0; m < h->M; ++m) {
+    const int64_t o = d->mortar_orientations[m], ls = d->mortar_large_sides[m];
+    if (o < 1 || o > h->dim) return bad("mortar %lld: orientation %lld", (long long)m + 1, (long long)o);
+    if (ls != 1 && ls != 2) return bad("mortar %lld: large side %lld", (long long)m + 1, (long long)ls);
+    const int small_dir = (int)(2 * (o - 1) + (ls - 1));
+    const int large_dir = (int)(2 * (o - 1) + (ls == 1 ? 1 : 0));
+    const int64_t large = d->mortar_neighbor_ids[nc + (nc + 1) * m];
+    if (large < 1 || large > h->E) return bad("mortar %lld: large id %lld", (long long)m + 1, (long long)large);
+    const int64_t base = m * (nc + 1);
+    for (int c = 0; c < nc; ++c) {
+      const int64_t s = d->mortar_neighbor_ids[c + (nc + 1) * m];
+      if (s < 1 || s > h->E) return bad("mortar %lld: small id %lld", (long long)m + 1, (long long)s);
+      int32_t &f = ft[(size_t)(s - 1) * nfaces + small_dir];
+      if (f != INT32_MIN) return bad("mortar %lld: small face already connected (element %lld)", (long long)m + 1, (long long)s);
+      f = (int32_t)(-(base + c) - 1);
+      slot_nbrs[(size_t)(base + c) * 4] = (int32_t)(large - 1);
+      slot_nbrs[(size_t)(base + nc) * 4 + c] = (int32_t)(s - 1);
+    }
+    int32_t &f = ft[(size_t)(large - 1) * nfaces + large_dir];
+    if (f != INT32_MIN) return bad("mortar %lld: large face already connected (element %lld)", (long long)m + 1, (long long)large);
+    f = (int32_t)(-(base + nc) - 1);
+  }
+  for (size_t i = 0; i < ft.size(); ++i)
+    if (ft[i] == INT32_MIN)
+      return bad("element %lld face %lld has no interface or mortar (non-periodic meshes are not supported)",
+                 (long long)(i / nfaces) + 1, (long long)(i % nfaces) + 1);
+
+  // all host-side validation is done; from here on the device is touched
+  cudaGetDevice(&h->device);
+  cudaError_t e = cudaSuccess;
+  auto ok = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  ok(upload(&h->d_face_table, ft.data(), ft.size()));
+  ok(upload(&h->d_slot_nbrs, slot_nbrs.data(), slot_nbrs.size()));
+  ok(upload(&h->d_inv_jac, d->inverse_jacobian, (size_t)h->E));
+  ok(upload(&h->d_if_nid, d->interface_neighbor_ids, (size_t)(2 * h->I)));
+  ok(upload(&h->d_if_ori, d->interface_orientations, (size_t)h->I));
+  ok(upload(&h->d_mo_nid, d->mortar_neighbor_ids, (size_t)((nc + 1) * h->M)));
+  ok(upload(&h->d_mo_ls, d->mortar_large_sides, (size_t)h->M));
+  ok(upload(&h->d_mo_ori, d->mortar_orientations, (size_t)h->M));
+  if (h->M > 0) ok(cudaMalloc(&h->d_mortar_flux, sizeof(double) * (size_t)(h->M * (nc + 1) * h->NF * h->nv)));
+  if (h->vol == TRIXI_VOLUME_SHOCK_CAPTURING_HG) {
+    ok(cudaMalloc(&h->d_alpha_raw, sizeof(double) * (size_t)h->E));
+    ok(cudaMalloc(&h->d_alpha, sizeof(double) * (size_t)h->E));
+    if (h->d_alpha) ok(cudaMemset(h->d_alpha, 0, sizeof(double) * (size_t)h->E));
+  }
+  ok(cudaMalloc(&h->d_err, sizeof(int)));
+  if (h->d_err) ok(cudaMemset(h->d_err, 0, sizeof(int)));
+  if (e != cudaSuccess) {
+    int st = cuda_fail(nullptr, e, "trixi_create");
+    free_all(h);
+    delete h;
+    return st;
+  }
+
+  // fused-kernel launch template
+  FusedHost &f = h->fused;
+  f.face_table = h->d_face_table;
+  f.mortar_flux = h->d_mortar_flux;
+  f.inv_jac = h->d_inv_jac;
+  f.alpha = h->d_alpha;
+  f.err = h->d_err;
+  f.nelements = h->E;
+  f.surface_flux = h->sflux;
+  f.fv_flux = h->fvflux;
+  const double eps = 2.220446049250313e-16;
+  f.atol = std::max(100 * eps, std::pow(eps, 0.75));  // src/solvers/dg_2d.jl:173
+  f.gamma = h->gamma;
+  for (int i = 0; i < 3; ++i) f.adv[i] = h->adv[i];
+  f.N = h->N;
+  to_row_major(h->basis.dsplit, h->N, f.dsplit);
+  for (int i = 0; i < h->N; ++i) f.dsplit[i * h->N + i] = 0.0;  // zeroed diagonal (dg_2d_kernel.jl:189-190)
+  to_row_major(h->basis.dhat, h->N, f.dhat);
+  for (int i = 0; i < h->N; ++i) f.invw[i] = 1.0 / h->basis.weights[i];
+  f.lhat_l = 1.0 / h->basis.weights[0];          // boundary_interpolation[1, 1]
+  f.lhat_r = 1.0 / h->basis.weights[h->N - 1];   // boundary_interpolation[N, 2]
+  *out = h;
+  return TRIXI_OK;
+}
+
+int trixi_destroy(trixi_handle *h) {
+  if (!h) return TRIXI_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != h->device) cudaSetDevice(h->device);
+  free_all(h);
+  if (cur != h->device) cudaSetDevice(cur);
+  delete h;
+  return TRIXI_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+void fill_mortar(const trixi_handle *h, MortarHost &mh, const double *u) {
+  mh.dim = h->dim;
+  mh.N = h->N;
+  mh.eq = h->eq;
+  mh.nv = h->nv;
+  mh.nmortars = h->M;
+  mh.u = u;
+  mh.neighbor_ids = h->d_mo_nid;
+  mh.large_sides = h->d_mo_ls;
+  mh.orientations = h->d_mo_ori;
+  mh.mortar_flux = h->d_mortar_flux;
+  mh.surface_flux = h->sflux;
+  mh.mixed = h->mixed;
+  mh.gamma = h->gamma;
+  for (int i = 0; i < 3; ++i) mh.adv[i] = h->adv[i];
+  to_row_major(h->basis.fwd_up, h->N, mh.fwd_up);
+  to_row_major(h->basis.fwd_lo, h->N, mh.fwd_lo);
+  to_row_major(h->basis.rev_up, h->N, mh.rev_up);
+  to_row_major(h->basis.rev_lo, h->N, mh.rev_lo);
+  mh.err = h->d_err;
+}
+
+int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStream_t s) {
+  IndicatorHost ih;
+  ih.dim = h->dim;
+  ih.N = h->N;
+  ih.nv = h->nv;
+  ih.nelements = h->E;
+  ih.u = u;
+  ih.alpha_raw = h->d_alpha_raw;
+  ih.alpha = alpha_out;
+  ih.face_table = h->d_face_table;
+  ih.slot_neighbors = h->d_slot_nbrs;
+  ih.smooth = h->alpha_smooth;
+  ih.gamma = h->gamma;
+  ih.alpha_max = h->alpha_max;
+  ih.alpha_min = h->alpha_min;
+  // src/solvers/indicators.jl:22-24
+  ih.threshold = 0.5 * std::pow(10.0, -1.8 * std::pow((double)h->N, 0.25));
+  ih.parameter_s = std::log((1 - 0.0001) / 0.0001);
+  to_row_major(h->basis.ivdm, h->N, ih.ivdm);
+  TRIXI_CUDA(h, launch_indicator(ih, s), "indicator");
+  return TRIXI_OK;
+}
+
+// Kernels of one rhs evaluation (mode RHS/RK/VOLUME) on u_in.
+int run_rhs(trixi_handle *h, int mode, const double *u_in, double *out, double *k, double a, double b, double dt,
+            cudaStream_t s) {
+  if (h->vol == TRIXI_VOLUME_SHOCK_CAPTURING_HG) {
+    int st = run_indicator(h, u_in, h->d_alpha, s);
+    if (st) return st;
+  }
+  if (h->M > 0 && mode != MODE_VOLUME) {
+    MortarHost mh;
+    fill_mortar(h, mh, u_in);
+    TRIXI_CUDA(h, launch_mortar_flux(mh, s), "mortar flux");
+  }
+  FusedHost f = h->fused;
+  f.u_in = u_in;
+  f.out = out;
+  f.k = k;
+  f.mode = mode;
+  f.rk_a = a;
+  f.rk_b = b;
+  f.dt = dt;
+  f.epb = h->epb;
+  TRIXI_CUDA(h, launch_fused(h->dim, h->N, h->eq, h->vol, h->vflux, h->mixed, f, s), "fused rhs");
+  return TRIXI_OK;
+}
+
+StageHost stage_of(trixi_handle *h) {
+  StageHost sh;
+  sh.dim = h->dim;
+  sh.N = h->N;
+  sh.nv = h->nv;
+  sh.eq = h->eq;
+  sh.nelements = h->E;
+  sh.ninterfaces = h->I;
+  sh.nmortars = h->M;
+  sh.if_neighbor_ids = h->d_if_nid;
+  sh.if_orientations = h->d_if_ori;
+  sh.mo_neighbor_ids = h->d_mo_nid;
+  sh.mo_large_sides = h->d_mo_ls;
+  sh.mo_orientations = h->d_mo_ori;
+  sh.interfaces_u = h->d_interfaces_u;
+  sh.sfv = h->d_sfv;
+  for (int c = 0; c < 4; ++c) sh.mortar_u[c] = h->d_mortar_u[c];
+  sh.surface_flux = h->sflux;
+  sh.gamma = h->gamma;
+  for (int i = 0; i < 3; ++i) sh.adv[i] = h->adv[i];
+  to_row_major(h->basis.fwd_up, h->N, sh.fwd_up);
+  to_row_major(h->basis.fwd_lo, h->N, sh.fwd_lo);
+  to_row_major(h->basis.rev_up, h->N, sh.rev_up);
+  to_row_major(h->basis.rev_lo, h->N, sh.rev_lo);
+  sh.lhat_l = 1.0 / h->basis.weights[0];
+  sh.lhat_r = 1.0 / h->basis.weights[h->N - 1];
+  sh.inv_jac = h->d_inv_jac;
+  return sh;
+}
+
+// Stage containers are created on first use and then reused.
+int ensure_stage_containers(trixi_handle *h) {
+  if (h->d_sfv) return TRIXI_OK;
+  const size_t iu = (size_t)std::max<int64_t>(1, 2 * h->nv * h->NF * h->I);
+  const size_t sfv = (size_t)(h->nv * h->NF * 2 * h->dim * h->E);
+  TRIXI_CUDA(h, cudaMalloc(&h->d_interfaces_u, sizeof(double) * iu), "alloc interfaces_u");
+  TRIXI_CUDA(h, cudaMemset(h->d_interfaces_u, 0, sizeof(double) * iu), "init interfaces_u");
+  TRIXI_CUDA(h, cudaMalloc(&h->d_sfv, sizeof(double) * sfv), "alloc surface_flux_values");
+  TRIXI_CUDA(h, cudaMemset(h->d_sfv, 0, sizeof(double) * sfv), "init surface_flux_values");
+  if (h->M > 0)
+    for (int c = 0; c < h->nchild; ++c) {
+      const size_t n = (size_t)(2 * h->nv * h->NF * h->M);
+      TRIXI_CUDA(h, cudaMalloc(&h->d_mortar_u[c], sizeof(double) * n), "alloc mortar u");
+      TRIXI_CUDA(h, cudaMemset(h->d_mortar_u[c], 0, sizeof(double) * n), "init mortar u");
+    }
+  return TRIXI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int trixi_rhs(trixi_handle *h, double *du, const double *u, double t, void *stream) {
+  (void)t;  // autonomous: no source terms, periodic boundaries
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, du, "du")) return st;
+  if (int st = check_u_args(h, u, "u")) return st;
+  if ((const void *)du == (const void *)u) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "du aliases u");
+  return run_rhs(h, MODE_RHS, u, du, nullptr, 0, 0, 0, (cudaStream_t)stream);
+}
+
+int trixi_rk_stage(trixi_handle *h, double *u_out, const double *u_in, double *k, double a, double b, double dt,
+                   double t, void *stream) {
+  (void)t;
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u_out, "u_out")) return st;
+  if (int st = check_u_args(h, u_in, "u_in")) return st;
+  if (int st = check_u_args(h, k, "k")) return st;
+  if ((const void *)u_out == (const void *)u_in) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "u_out aliases u_in");
+  if (!std::isfinite(a) || !std::isfinite(b) || !std::isfinite(dt))
+    return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "non-finite RK coefficient");
+  return run_rhs(h, MODE_RK, u_in, u_out, k, a, b, dt, (cudaStream_t)stream);
+}
+
+int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt, int64_t nsteps, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = check_u_args(h, k, "k")) return st;
+  if (nsteps < 0 || !std::isfinite(dt)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "nsteps %lld / dt", (long long)nsteps);
+  if (nsteps == 0) return TRIXI_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = sizeof(double) * (size_t)(h->E * h->NN * h->nv);
+  if (!h->d_scratch_u) TRIXI_CUDA(h, cudaMalloc(&h->d_scratch_u, bytes), "alloc RK scratch");
+  double *cur = u, *nxt = h->d_scratch_u;
+  for (int64_t step = 0; step < nsteps; ++step) {
+    for (int st = 0; st < 5; ++st) {
+      int r = run_rhs(h, MODE_RK, cur, nxt, k, kCK_A[st], kCK_B[st], dt, s);
+      if (r) return r;
+      std::swap(cur, nxt);
+    }
+    t += dt;
+  }
+  if (cur != u) TRIXI_CUDA(h, cudaMemcpyAsync(u, cur, bytes, cudaMemcpyDeviceToDevice, s), "RK copy back");
+  return TRIXI_OK;
+}
+
+int trixi_volume_integral(trixi_handle *h, double *du, const double *u, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, du, "du")) return st;
+  if (int st = check_u_args(h, u, "u")) return st;
+  return run_rhs(h, MODE_VOLUME, u, du, nullptr, 0, 0, 0, (cudaStream_t)stream);
+}
+
+int trixi_prolong2interfaces(trixi_handle *h, const double *u, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = ensure_stage_containers(h)) return st;
+  TRIXI_CUDA(h, stage_prolong2interfaces(stage_of(h), u, (cudaStream_t)stream), "prolong2interfaces");
+  return TRIXI_OK;
+}
+
+int trixi_interface_flux(trixi_handle *h, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = ensure_stage_containers(h)) return st;
+  TRIXI_CUDA(h, stage_interface_flux(stage_of(h), (cudaStream_t)stream), "interface_flux");
+  return TRIXI_OK;
+}
+
+int trixi_prolong2boundaries(trixi_handle *h, const double *u, void *stream) {
+  (void)u;
+  (void)stream;
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  return TRIXI_OK;  // periodic TreeMesh: no boundaries (src/solvers/dg_2d.jl:419-422)
+}
+
+int trixi_boundary_flux(trixi_handle *h, double t, void *stream) {
+  (void)t;
+  (void)stream;
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  return TRIXI_OK;  // periodic TreeMesh: no boundaries (src/solvers/dg_2d.jl:447-450)
+}
+
+int trixi_prolong2mortars(trixi_handle *h, const double *u, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = ensure_stage_containers(h)) return st;
+  TRIXI_CUDA(h, stage_prolong2mortars(stage_of(h), u, (cudaStream_t)stream), "prolong2mortars");
+  return TRIXI_OK;
+}
+
+int trixi_mortar_flux(trixi_handle *h, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = ensure_stage_containers(h)) return st;
+  TRIXI_CUDA(h, stage_mortar_flux(stage_of(h), (cudaStream_t)stream), "mortar_flux");
+  return TRIXI_OK;
+}
+
+int trixi_surface_integral(trixi_handle *h, double *du, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, du, "du")) return st;
+  if (int st = ensure_stage_containers(h)) return st;
+  TRIXI_CUDA(h, stage_surface_integral(stage_of(h), du, (cudaStream_t)stream), "surface_integral");
+  return TRIXI_OK;
+}
+
+int trixi_jacobian(trixi_handle *h, double *du, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, du, "du")) return st;
+  TRIXI_CUDA(h, stage_jacobian(stage_of(h), du, (cudaStream_t)stream), "jacobian");
+  return TRIXI_OK;
+}
+
+int trixi_sources(trixi_handle *h, double *du, const double *u, double t, void *stream) {
+  (void)du;
+  (void)u;
+  (void)t;
+  (void)stream;
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  return TRIXI_OK;  // source_terms = nothing (src/solvers/dg_2d.jl:741-743)
+}
+
+int trixi_container(trixi_handle *h, int which, void **dev_ptr, int64_t *count) {
+  if (!h || !dev_ptr || !count) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "null argument");
+  if (which == TRIXI_CONTAINER_ALPHA) {
+    *dev_ptr = h->d_alpha;
+    *count = h->d_alpha ? h->E : 0;
+    return TRIXI_OK;
+  }
+  if (which == TRIXI_CONTAINER_INVERSE_JACOBIAN) {
+    *dev_ptr = h->d_inv_jac;
+    *count = h->E;
+    return TRIXI_OK;
+  }
+  if (int st = ensure_stage_containers(h)) return st;
+  if (which == TRIXI_CONTAINER_INTERFACES_U) {
+    *dev_ptr = h->d_interfaces_u;
+    *count = 2 * h->nv * h->NF * h->I;
+    return TRIXI_OK;
+  }
+  if (which == TRIXI_CONTAINER_SURFACE_FLUX_VALUES) {
+    *dev_ptr = h->d_sfv;
+    *count = h->nv * h->NF * 2 * h->dim * h->E;
+    return TRIXI_OK;
+  }
+  if (which >= TRIXI_CONTAINER_MORTARS_U && which < TRIXI_CONTAINER_MORTARS_U + h->nchild && h->dim > 1) {
+    // reference order: 2D u_upper, u_lower; 3D u_upper_left, u_upper_right, u_lower_left, u_lower_right
+    static const int map2[2] = {1, 0};
+    static const int map3[4] = {2, 3, 0, 1};
+    const int j = which - TRIXI_CONTAINER_MORTARS_U;
+    const int c = (h->dim == 2) ? map2[j] : map3[j];
+    *dev_ptr = h->d_mortar_u[c];
+    *count = h->M > 0 ? 2 * h->nv * h->NF * h->M : 0;
+    return TRIXI_OK;
+  }
+  return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "container %d", which);
+}
+
+int trixi_indicator(trixi_handle *h, const double *u, double *alpha, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (h->eq != EQ_EULER) return fail(h, TRIXI_ERR_UNSUPPORTED, "indicator on density_pressure needs Euler");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = check_u_args(h, alpha, "alpha")) return st;
+  if (!h->d_alpha_raw) {
+    TRIXI_CUDA(h, cudaMalloc(&h->d_alpha_raw, sizeof(double) * (size_t)h->E), "alloc alpha");
+  }
+  return run_indicator(h, u, alpha, (cudaStream_t)stream);
+}
+
+static int copy_basis_item(const Basis &b, int which, double *host_out, int64_t count) {
+  if (!host_out) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "null argument");
+  const std::vector<double> *src = nullptr;
+  switch (which) {
+    case 0: src = &b.nodes; break;
+    case 1: src = &b.weights; break;
+    case 2: src = &b.dsplit; break;
+    case 3: src = &b.dhat; break;
+    case 4: src = &b.ivdm; break;
+    case 5: src = &b.fwd_up; break;
+    case 6: src = &b.fwd_lo; break;
+    case 7: src = &b.rev_up; break;
+    case 8: src = &b.rev_lo; break;
+    case 9: src = &b.dmat; break;
+    default: return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "basis item %d", which);
+  }
+  if (count < (int64_t)src->size())
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "count %lld < %lld", (long long)count, (long long)src->size());
+  std::memcpy(host_out, src->data(), sizeof(double) * src->size());
+  return TRIXI_OK;
+}
+
+int trixi_basis(const trixi_handle *h, int which, double *host_out, int64_t count) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  return copy_basis_item(h->basis, which, host_out, count);
+}
+
+int trixi_lgl_basis(int polydeg, int which, double *host_out, int64_t count) {
+  Basis b;
+  if (polydeg < 1 || polydeg > 15 || !compute_basis(polydeg, b))
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "polydeg %d", polydeg);
+  return copy_basis_item(b, which, host_out, count);
+}
+
+int trixi_synchronize(trixi_handle *h, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  TRIXI_CUDA(h, cudaStreamSynchronize((cudaStream_t)stream), "synchronize");
+  int flag = 0;
+  TRIXI_CUDA(h, cudaMemcpy(&flag, h->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read error word");
+  if (flag) return fail(h, TRIXI_ERR_DEVICE_FLAG, "device error word %d", flag);
+  return TRIXI_OK;
+}
+
+}  // extern "C"

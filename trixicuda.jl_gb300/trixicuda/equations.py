@@ -1,0 +1,220 @@
+"""Equation systems, numerical-flux selectors and initial conditions.
+
+The equation and flux names follow Trixi.jl's, which the reference uses
+through `using Trixi` (src/TrixiCUDA.jl:12-55): LinearScalarAdvectionEquation
+{1,2,3}D, CompressibleEulerEquations{1,2,3}D, flux, flux_ranocha, flux_central,
+flux_lax_friedrichs.  The arithmetic itself runs in libtrixi_b200.so; these
+objects only select it.  Initial conditions are evaluated on the host with
+numpy (vectorised over nodes) and copied to the device once.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+
+
+# --- numerical fluxes ---------------------------------------------------------
+@dataclass(frozen=True)
+class NumericalFlux:
+    name: str
+    code: int
+
+    def __repr__(self) -> str:
+        return self.name
+
+
+flux_lax_friedrichs = NumericalFlux("flux_lax_friedrichs", _lib.FLUX_LAX_FRIEDRICHS)
+flux_ranocha = NumericalFlux("flux_ranocha", _lib.FLUX_RANOCHA)
+flux_central = NumericalFlux("flux_central", _lib.FLUX_CENTRAL)
+flux_lax_friedrichs_naive = NumericalFlux("flux_lax_friedrichs_naive", _lib.FLUX_LAX_FRIEDRICHS_NAIVE)
+flux = NumericalFlux("flux", -1)  # physical flux (weak form)
+
+
+# --- equations ------------------------------------------------------------------
+class AbstractEquations:
+    ndims: int
+    nvariables: int
+    code: int
+
+    def cons2prim(self, u):
+        return u
+
+
+class _LinearScalarAdvection(AbstractEquations):
+    code = _lib.EQ_LINEAR_ADVECTION
+    nvariables = 1
+
+    def __init__(self, advection_velocity):
+        a = np.atleast_1d(np.asarray(advection_velocity, dtype=np.float64))
+        if a.shape != (self.ndims,):
+            raise ValueError(f"advection velocity needs {self.ndims} components")
+        self.advection_velocity = a
+        self.gamma = 1.4
+
+    def __repr__(self):
+        return f"LinearScalarAdvectionEquation{self.ndims}D({tuple(self.advection_velocity)})"
+
+
+class LinearScalarAdvectionEquation1D(_LinearScalarAdvection):
+    ndims = 1
+
+
+class LinearScalarAdvectionEquation2D(_LinearScalarAdvection):
+    ndims = 2
+
+
+class LinearScalarAdvectionEquation3D(_LinearScalarAdvection):
+    ndims = 3
+
+
+class _CompressibleEuler(AbstractEquations):
+    code = _lib.EQ_COMPRESSIBLE_EULER
+
+    def __init__(self, gamma: float = 1.4):
+        self.gamma = float(gamma)
+        self.nvariables = self.ndims + 2
+        self.advection_velocity = np.zeros(self.ndims)
+
+    def __repr__(self):
+        return f"CompressibleEulerEquations{self.ndims}D({self.gamma})"
+
+    def prim2cons(self, rho, v, p):
+        """rho (n,), v (ndims, n), p (n,) -> u (nvars, n)."""
+        rho = np.asarray(rho, dtype=np.float64)
+        v = np.asarray(v, dtype=np.float64).reshape(self.ndims, -1)
+        u = np.empty((self.nvariables,) + rho.shape)
+        u[0] = rho
+        u[1:1 + self.ndims] = rho * v
+        u[-1] = p / (self.gamma - 1) + 0.5 * rho * np.sum(v * v, axis=0)
+        return u
+
+    def cons2prim(self, u):
+        rho = u[0]
+        v = u[1:1 + self.ndims] / rho
+        p = (self.gamma - 1) * (u[-1] - 0.5 * np.sum(u[1:1 + self.ndims] * v, axis=0))
+        return rho, v, p
+
+
+class CompressibleEulerEquations1D(_CompressibleEuler):
+    ndims = 1
+
+
+class CompressibleEulerEquations2D(_CompressibleEuler):
+    ndims = 2
+
+
+class CompressibleEulerEquations3D(_CompressibleEuler):
+    ndims = 3
+
+
+# --- initial conditions (x: (ndims, n) array) -----------------------------------
+def initial_condition_convergence_test(x, t, equations):
+    """Advection: c + A sin(omega (sum(x) - t*sum(a)))... per dimension as in
+    Trixi's linear-advection convergence test: u = 1 + 0.5 sin(pi * (x - a t))
+    summed over dimensions with a 2-periodic domain."""
+    x = np.atleast_2d(x)
+    if isinstance(equations, _LinearScalarAdvection):
+        c, A, L = 1.0, 0.5, 2.0
+        omega = 2 * np.pi / L
+        xt = x - equations.advection_velocity[:, None] * t
+        return (c + A * np.sin(omega * np.sum(xt, axis=0)))[None, :]
+    # Euler manufactured solution (source terms are not part of the hot path)
+    c, A, L = 2.0, 0.1, 2.0
+    omega = 2 * np.pi / L
+    ini = c + A * np.sin(omega * (np.sum(x, axis=0) - t))
+    rho = ini
+    v = np.ones((equations.ndims,) + rho.shape)
+    rho_e = ini * ini
+    u = np.empty((equations.nvariables,) + rho.shape)
+    u[0] = rho
+    u[1:1 + equations.ndims] = rho * v
+    u[-1] = rho_e
+    return u
+
+
+def initial_condition_constant(x, t, equations, rho=1.0, v=None, p=1.0):
+    x = np.atleast_2d(x)
+    n = x.shape[1]
+    if isinstance(equations, _LinearScalarAdvection):
+        return np.full((1, n), 1.0)
+    v = np.zeros(equations.ndims) if v is None else np.asarray(v, dtype=np.float64)
+    return equations.prim2cons(np.full(n, rho), np.repeat(v[:, None], n, axis=1), np.full(n, p))
+
+
+def initial_condition_weak_blast_wave(x, t, equations):
+    """Weak blast wave (Trixi's `initial_condition_weak_blast_wave`): inside
+    r < 0.5 rho=1.1691, radial velocity 0.1882, p=1.245; outside rho=1, v=0, p=1."""
+    x = np.atleast_2d(x)
+    d = equations.ndims
+    r = np.sqrt(np.sum(x * x, axis=0))
+    rho = np.where(r > 0.5, 1.0, 1.1691)
+    p = np.where(r > 0.5, 1.0, 1.245)
+    v = np.zeros((d,) + r.shape)
+    if d == 1:
+        v[0] = np.where(r > 0.5, 0.0, 0.1882 * np.sign(x[0]))
+    elif d == 2:
+        phi = np.arctan2(x[1], x[0])
+        v[0] = np.where(r > 0.5, 0.0, 0.1882 * np.cos(phi))
+        v[1] = np.where(r > 0.5, 0.0, 0.1882 * np.sin(phi))
+    else:
+        phi = np.arctan2(x[1], x[0])
+        theta = np.where(r == 0, 0.0, np.arccos(np.clip(x[2] / np.where(r == 0, 1.0, r), -1, 1)))
+        v[0] = np.where(r > 0.5, 0.0, 0.1882 * np.cos(phi) * np.sin(theta))
+        v[1] = np.where(r > 0.5, 0.0, 0.1882 * np.sin(phi) * np.sin(theta))
+        v[2] = np.where(r > 0.5, 0.0, 0.1882 * np.cos(theta))
+    return equations.prim2cons(rho, v, p)
+
+
+class FourierField:
+    """Seeded smooth periodic field: sum of random Fourier modes with integer
+    wave vectors 0 < |k| <= kmax on the box [xmin, xmax]^d, scaled so that
+    max |field| <= 1 (coefficients normalised by the sum of their magnitudes)."""
+
+    def __init__(self, ndims, kmax, seed, xmin, xmax):
+        rng = np.random.default_rng(seed)
+        ks = [k for k in np.ndindex(*([2 * kmax + 1] * ndims))]
+        ks = np.array(ks, dtype=np.int64) - kmax
+        norm = np.sqrt(np.sum(ks * ks, axis=1))
+        ks = ks[(norm > 0) & (norm <= kmax)]
+        self.k = ks.astype(np.float64)
+        a = rng.standard_normal(len(ks))
+        b = rng.standard_normal(len(ks))
+        s = np.sum(np.abs(a) + np.abs(b))
+        self.a, self.b = a / s, b / s
+        self.xmin = float(xmin)
+        self.L = float(xmax) - float(xmin)
+
+    def __call__(self, x):
+        x = np.atleast_2d(x)
+        phase = 2 * np.pi * (self.k @ (x - self.xmin)) / self.L  # (nk, n)
+        return self.a @ np.cos(phase) + self.b @ np.sin(phase)
+
+
+def initial_condition_fourier_euler(equations, seed=20261203, kmax=8, xmin=-2.0, xmax=2.0,
+                                    amplitude=0.1, v0=(0.1, 0.2, 0.05), v_amp=0.02):
+    """rho = 1 + amplitude * F_0(x), v = v0 + v_amp * F_{1..d}(x), p = 1 with
+    independent seeded Fourier fields F (the synthetic 2D Euler workload)."""
+    d = equations.ndims
+    f_rho = FourierField(d, kmax, seed, xmin, xmax)
+    f_v = [FourierField(d, kmax, seed + 1 + i, xmin, xmax) for i in range(d)]
+
+    def ic(x, t, eq):
+        x = np.atleast_2d(x)
+        rho = 1.0 + amplitude * f_rho(x)
+        v = np.stack([v0[i] + v_amp * f_v[i](x) for i in range(d)])
+        p = np.ones_like(rho)
+        return eq.prim2cons(rho, v, p)
+
+    return ic
+
+
+def initial_condition_fourier_advection(equations, seed=20261203, kmax=8, xmin=-2.0, xmax=2.0, amplitude=0.1):
+    f = FourierField(equations.ndims, kmax, seed, xmin, xmax)
+
+    def ic(x, t, eq):
+        return (1.0 + amplitude * f(np.atleast_2d(x)))[None, :]
+
+    return ic

@@ -1,0 +1,325 @@
+"""SemidiscretizationHyperbolicGPU, semidiscretizeGPU, rhs_gpu and the stage
+functions -- the host side of the reference's public API, backed by
+libtrixi_b200.so.
+
+Reference interfaces mirrored here:
+  SemidiscretizationHyperbolicGPU  src/semidiscretization/semidiscretization_hyperbolic.jl:60-87
+  semidiscretizeGPU                src/solvers/solvers.jl:43-56
+  rhs_gpu!(du_ode, u_ode, semi, t) src/solvers/solvers.jl:18-31
+  wrap_array                       src/solvers/dg.jl:14-20
+  cuda_* stage functions           src/solvers/dg_{1,2,3}d.jl, docstrings dg.jl:164-325
+
+Device arrays are torch CUDA tensors (float64) in the reference layout
+[nvars, N, ..., nelements] column-major, i.e. C-order shape
+(nelements, N, ..., nvars).  Compute calls go through the C ABI on the
+current torch stream; none of them has a CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .equations import AbstractEquations, flux_lax_friedrichs
+from .mesh import Containers, TreeMesh
+from .solver import DGSEMGPU, VolumeIntegralShockCapturingHG, VolumeIntegralFluxDifferencing
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _ptr_d(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a.size else None
+
+
+def _ptr_i(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int64)) if a.size else None
+
+
+def _stream_handle(stream=None):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver: DGSEMGPU,
+                       precision: str = "fp64"):
+    """trixi_problem_desc for a mesh (or prebuilt containers).  Returns the
+    ctypes struct and the numpy arrays it points into (keep them alive)."""
+    if isinstance(mesh_or_containers, Containers):
+        cont = mesh_or_containers
+    else:
+        cont = mesh_or_containers.build_containers(solver.basis.nodes)
+    d = _lib.ProblemDesc()
+    d.struct_size = C.sizeof(_lib.ProblemDesc)
+    d.ndims = cont.ndims
+    d.polydeg = solver.polydeg
+    d.nvars = equations.nvariables
+    d.equation = equations.code
+    vi = solver.volume_integral
+    d.volume_integral = vi.code
+    d.volume_flux = _lib.FLUX_CENTRAL
+    d.volume_flux_fv = _lib.FLUX_LAX_FRIEDRICHS
+    d.alpha_max, d.alpha_min, d.alpha_smooth = 0.5, 0.001, 1
+    if isinstance(vi, VolumeIntegralFluxDifferencing):
+        d.volume_flux = vi.volume_flux.code
+    if isinstance(vi, VolumeIntegralShockCapturingHG):
+        d.volume_flux = vi.volume_flux_dg.code
+        d.volume_flux_fv = vi.volume_flux_fv.code
+        d.alpha_max = vi.indicator.alpha_max
+        d.alpha_min = vi.indicator.alpha_min
+        d.alpha_smooth = int(bool(vi.indicator.alpha_smooth))
+    d.surface_flux = solver.surface_flux.code
+    if precision not in ("fp64", "mixed"):
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    d.precision = _lib.PRECISION_MIXED if precision == "mixed" else _lib.PRECISION_FP64
+    d.gamma = float(getattr(equations, "gamma", 1.4))
+    av = np.zeros(3)
+    av[: equations.ndims] = getattr(equations, "advection_velocity", np.zeros(equations.ndims))
+    for i in range(3):
+        d.advection_velocity[i] = av[i]
+    d.indicator_variable = 0
+    keep = dict(
+        inverse_jacobian=np.ascontiguousarray(cont.inverse_jacobian, dtype=np.float64),
+        if_nid=np.ascontiguousarray(cont.interface_neighbor_ids, dtype=np.int64),
+        if_ori=np.ascontiguousarray(cont.interface_orientations, dtype=np.int64),
+        mo_nid=np.ascontiguousarray(cont.mortar_neighbor_ids, dtype=np.int64),
+        mo_ls=np.ascontiguousarray(cont.mortar_large_sides, dtype=np.int64),
+        mo_ori=np.ascontiguousarray(cont.mortar_orientations, dtype=np.int64),
+    )
+    d.nelements = cont.nelements
+    d.inverse_jacobian = _ptr_d(keep["inverse_jacobian"])
+    d.ninterfaces = cont.ninterfaces
+    d.interface_neighbor_ids = _ptr_i(keep["if_nid"])
+    d.interface_orientations = _ptr_i(keep["if_ori"])
+    d.nboundaries = 0
+    d.nmortars = cont.nmortars
+    d.mortar_neighbor_ids = _ptr_i(keep["mo_nid"])
+    d.mortar_large_sides = _ptr_i(keep["mo_ls"])
+    d.mortar_orientations = _ptr_i(keep["mo_ori"])
+    return d, keep, cont
+
+
+class SemidiscretizationHyperbolicGPU:
+    """GPU semidiscretization (reference:
+    src/semidiscretization/semidiscretization_hyperbolic.jl:5-87)."""
+
+    def __init__(self, mesh: TreeMesh, equations: AbstractEquations, initial_condition, solver: DGSEMGPU,
+                 source_terms=None, boundary_conditions="periodic", RealT=np.float64, uEltype=np.float64,
+                 precision: str = "fp64", device=None):
+        if mesh.ndims != equations.ndims:
+            raise ValueError("mesh and equations dimension differ")
+        if source_terms is not None:
+            raise NotImplementedError("source terms are not part of the GB300 hot path")
+        if boundary_conditions not in ("periodic", None):
+            raise NotImplementedError("only periodic boundary conditions are supported")
+        self.mesh = mesh
+        self.equations = equations
+        self.initial_condition = initial_condition
+        self.solver = solver
+        self.source_terms = source_terms
+        self.boundary_conditions = "periodic"
+        self.precision = precision
+        desc, keep, cont = build_problem_desc(mesh, equations, solver, precision)
+        self.containers = cont
+        self._desc, self._keep = desc, keep
+        torch = _torch()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        lib = _lib.load()
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(lib.trixi_create(C.byref(desc), C.byref(h)))
+        self._handle = h
+        self._lib = lib
+
+    # -- sizes -------------------------------------------------------------
+    @property
+    def handle(self):
+        return self._handle
+
+    @property
+    def nnodes(self) -> int:
+        return self.solver.polydeg + 1
+
+    @property
+    def nelements(self) -> int:
+        return self.containers.nelements
+
+    def ndofs(self) -> int:
+        """Nodes per field, Trixi's ndofsglobal (benchmark/euler_ec_2d.jl:65)."""
+        return self.nelements * self.nnodes ** self.mesh.ndims
+
+    def u_shape(self):
+        return (self.nelements,) + (self.nnodes,) * self.mesh.ndims + (self.equations.nvariables,)
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            try:
+                self._lib.trixi_destroy(h)
+            except Exception:
+                pass
+            self._handle = None
+
+    # -- initial data ------------------------------------------------------
+    def compute_coefficients_host(self, t: float = 0.0, func=None) -> np.ndarray:
+        """u0 on the host in the reference layout, evaluating the initial
+        condition at every node (reference: compute_coefficients_kernel!,
+        src/solvers/dg.jl:46-115, including the 1D endpoint nudge of x by one
+        ulp inward, dg.jl:54-57)."""
+        func = func or self.initial_condition
+        d = self.mesh.ndims
+        x = self.containers.node_coordinates.reshape(-1, d).T.copy()
+        if d == 1:
+            N = self.nnodes
+            x1 = x.reshape(1, -1, N)
+            x1[0, :, 0] = np.nextafter(x1[0, :, 0], np.inf)
+            x1[0, :, N - 1] = np.nextafter(x1[0, :, N - 1], -np.inf)
+            x = x1.reshape(1, -1)
+        u = func(x, t, self.equations)  # (nvars, nnodes_total)
+        return np.ascontiguousarray(u.T.reshape(self.u_shape()))
+
+    def compute_coefficients(self, t: float = 0.0, func=None):
+        torch = _torch()
+        return torch.from_numpy(self.compute_coefficients_host(t, func)).to(self.device)
+
+    # -- containers ----------------------------------------------------------
+    def container(self, which: int):
+        """A library-owned device container as a torch tensor view (no copy)."""
+        torch = _torch()
+        ptr, cnt = C.c_void_p(), C.c_int64()
+        _lib.check(self._lib.trixi_container(self._handle, which, C.byref(ptr), C.byref(cnt)), self._handle)
+        if cnt.value == 0 or not ptr.value:
+            return torch.empty(0, dtype=torch.float64, device=self.device)
+        # wrap the device pointer through a DLPack-free route: cupy-less torch view
+        return _device_view(ptr.value, cnt.value, self.device)
+
+
+def _device_view(ptr: int, count: int, device):
+    """Torch tensor aliasing `count` float64 values at device pointer `ptr`."""
+    torch = _torch()
+
+    class _CudaArray:
+        def __init__(self, p, n):
+            self.__cuda_array_interface__ = {
+                "shape": (n,), "typestr": "<f8", "data": (p, False), "version": 2, "strides": None,
+            }
+
+    return torch.as_tensor(_CudaArray(ptr, count), device=device)
+
+
+def wrap_array(u_ode, semi: SemidiscretizationHyperbolicGPU):
+    """Reshape a flat state vector to [nvars, N, ..., nelements] (C-order
+    view (nelements, N, ..., nvars)); reference src/solvers/dg.jl:14-20."""
+    return u_ode.view(semi.u_shape())
+
+
+@dataclass
+class ODEProblem:
+    f: object
+    u0: object
+    tspan: tuple
+    p: SemidiscretizationHyperbolicGPU
+
+
+def _check_state(semi, *arrays):
+    torch = _torch()
+    n = int(np.prod(semi.u_shape()))
+    for a in arrays:
+        if not isinstance(a, torch.Tensor) or a.dtype != torch.float64 or not a.is_cuda:
+            raise TypeError("state arrays must be float64 CUDA tensors")
+        if a.numel() != n or not a.is_contiguous():
+            raise ValueError(f"state array must be contiguous with {n} values")
+
+
+def rhs_gpu(du_ode, u_ode, semi: SemidiscretizationHyperbolicGPU, t: float, stream=None):
+    """du = rhs(u, t) on the GPU, in place (reference rhs_gpu!, solvers.jl:18-31)."""
+    _check_state(semi, du_ode, u_ode)
+    _lib.check(semi._lib.trixi_rhs(semi._handle, C.c_void_p(du_ode.data_ptr()), C.c_void_p(u_ode.data_ptr()),
+                                   float(t), _stream_handle(stream)), semi._handle)
+
+
+def semidiscretizeGPU(semi: SemidiscretizationHyperbolicGPU, tspan):
+    """ODE problem with u0 on the GPU (reference semidiscretizeGPU, solvers.jl:43-56)."""
+    u0 = semi.compute_coefficients(float(tspan[0])).reshape(-1)
+    return ODEProblem(rhs_gpu, u0, (float(tspan[0]), float(tspan[1])), semi)
+
+
+# -- stage functions (reference cuda_* launchers) ---------------------------------
+def _call(semi, fn, *args, stream=None):
+    _lib.check(fn(semi._handle, *args, _stream_handle(stream)), semi._handle)
+
+
+def cuda_volume_integral(du, u, semi, stream=None):
+    _check_state(semi, du, u)
+    _call(semi, semi._lib.trixi_volume_integral, C.c_void_p(du.data_ptr()), C.c_void_p(u.data_ptr()), stream=stream)
+
+
+def cuda_prolong2interfaces(u, semi, stream=None):
+    _check_state(semi, u)
+    _call(semi, semi._lib.trixi_prolong2interfaces, C.c_void_p(u.data_ptr()), stream=stream)
+
+
+def cuda_interface_flux(semi, stream=None):
+    _call(semi, semi._lib.trixi_interface_flux, stream=stream)
+
+
+def cuda_prolong2boundaries(u, semi, stream=None):
+    _check_state(semi, u)
+    _call(semi, semi._lib.trixi_prolong2boundaries, C.c_void_p(u.data_ptr()), stream=stream)
+
+
+def cuda_boundary_flux(t, semi, stream=None):
+    _call(semi, semi._lib.trixi_boundary_flux, float(t), stream=stream)
+
+
+def cuda_prolong2mortars(u, semi, stream=None):
+    _check_state(semi, u)
+    _call(semi, semi._lib.trixi_prolong2mortars, C.c_void_p(u.data_ptr()), stream=stream)
+
+
+def cuda_mortar_flux(semi, stream=None):
+    _call(semi, semi._lib.trixi_mortar_flux, stream=stream)
+
+
+def cuda_surface_integral(du, semi, stream=None):
+    _check_state(semi, du)
+    _call(semi, semi._lib.trixi_surface_integral, C.c_void_p(du.data_ptr()), stream=stream)
+
+
+def cuda_jacobian(du, semi, stream=None):
+    _check_state(semi, du)
+    _call(semi, semi._lib.trixi_jacobian, C.c_void_p(du.data_ptr()), stream=stream)
+
+
+def cuda_sources(du, u, t, semi, stream=None):
+    _check_state(semi, du, u)
+    _call(semi, semi._lib.trixi_sources, C.c_void_p(du.data_ptr()), C.c_void_p(u.data_ptr()), float(t),
+          stream=stream)
+
+
+def cuda_indicator(u, alpha, semi, stream=None):
+    """Hennemann-Gassner blending factors on the GPU into `alpha` (float64, nelements)."""
+    _check_state(semi, u)
+    _call(semi, semi._lib.trixi_indicator, C.c_void_p(u.data_ptr()), C.c_void_p(alpha.data_ptr()), stream=stream)
+
+
+def rk_stage(u_out, u_in, k, a, b, dt, t, semi, stream=None):
+    _check_state(semi, u_out, u_in, k)
+    _call(semi, semi._lib.trixi_rk_stage, C.c_void_p(u_out.data_ptr()), C.c_void_p(u_in.data_ptr()),
+          C.c_void_p(k.data_ptr()), float(a), float(b), float(dt), float(t), stream=stream)
+
+
+def rk_steps(u, k, t, dt, nsteps, semi, stream=None):
+    _check_state(semi, u, k)
+    _call(semi, semi._lib.trixi_rk_steps, C.c_void_p(u.data_ptr()), C.c_void_p(k.data_ptr()), float(t),
+          float(dt), int(nsteps), stream=stream)
+
+
+def synchronize(semi, stream=None):
+    _call(semi, semi._lib.trixi_synchronize, stream=stream)
