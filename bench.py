@@ -265,6 +265,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+                    help="run only the device-timed loop of one precision (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -297,6 +299,12 @@ def main():
     T._lib.check(lib.trixi_probe_fma_peak(0, 4096, C.byref(fp64_peak), None))
     T._lib.check(lib.trixi_probe_fma_peak(1, 16384, C.byref(fp32_peak), None))
 
+    if args.profile:
+        step_ms, launch_ms, semi, _, _ = time_gpu_path(args.profile, args.steps, args.warmup, device, flush)
+        print(json.dumps({"profile": args.profile, "ms_per_step": statistics.mean(step_ms),
+                          "mean_launch_ms": statistics.mean(launch_ms), "fp64_fma_peak_tflops": fp64_peak.value / 1e12,
+                          "fp32_fma_peak_tflops": fp32_peak.value / 1e12}))
+        return 0
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:

@@ -17,15 +17,27 @@ def pytest_configure(config):
 
 
 def rel_err(a, b):
+    """Relative error in the 2-norm, the definition of Julia's isapprox that
+    the reference's @test_approx uses (test/test_macros.jl:39)."""
+    a = np.asarray(a, dtype=np.float64).reshape(-1)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    scale = max(np.linalg.norm(a), np.linalg.norm(b), 1e-300)
+    return float(np.linalg.norm(a - b) / scale)
+
+
+def rel_err_max(a, b):
+    """Pointwise error scaled by the largest value (a stricter, max-norm view)."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
-    scale = max(np.max(np.abs(b)), 1e-300)
-    return float(np.max(np.abs(a - b)) / scale)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
-def assert_rel(a, b, rtol, what=""):
+def assert_rel(a, b, rtol, what="", max_factor=10.0):
+    """2-norm relative error <= rtol, and max-norm relative error <= max_factor*rtol."""
     e = rel_err(a, b)
-    assert e <= rtol, f"{what}: relative error {e:.3e} > {rtol:.1e}"
+    assert e <= rtol, f"{what}: relative 2-norm error {e:.3e} > {rtol:.1e}"
+    em = rel_err_max(a, b)
+    assert em <= max_factor * rtol, f"{what}: relative max-norm error {em:.3e} > {max_factor * rtol:.1e}"
 
 
 @pytest.fixture(scope="session")

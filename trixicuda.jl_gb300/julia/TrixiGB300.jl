@@ -1,0 +1,156 @@
+# TrixiGB300.jl -- ccall glue that routes TrixiCUDA.jl's rhs path to
+# libtrixi_b200.so (the GB300 / sm_103a C ABI declared in include/trixi_b200.h).
+#
+# This file is the Julia side of the drop-in boundary: it keeps the
+# reference's public API (`DGSEMGPU`, `SemidiscretizationHyperbolicGPU`,
+# `semidiscretizeGPU`, `rhs_gpu!`, src/TrixiCUDA.jl:70-73) and replaces the
+# bodies of `rhs_gpu!` (src/solvers/solvers.jl:18-31) and of the `cuda_*`
+# stage launchers (src/solvers/dg_{1,2,3}d.jl) by calls into the library.
+# Julia is not installed where this library is built and tested, so this file
+# has not been executed; the same entry points are exercised from Python
+# (trixicuda/_lib.py) by the test suite.
+module TrixiGB300
+
+using CUDA
+using Trixi
+
+const libtrixi = get(ENV, "TRIXI_B200_LIB", joinpath(@__DIR__, "..", "_build", "libtrixi_b200.so"))
+
+# enum values of include/trixi_b200.h
+const EQ_LINEAR_ADVECTION = Int32(0)
+const EQ_COMPRESSIBLE_EULER = Int32(1)
+const VOLUME_WEAK_FORM = Int32(0)
+const VOLUME_FLUX_DIFFERENCING = Int32(1)
+const VOLUME_SHOCK_CAPTURING_HG = Int32(2)
+const FLUX_LAX_FRIEDRICHS = Int32(0)
+const FLUX_RANOCHA = Int32(1)
+const FLUX_CENTRAL = Int32(2)
+
+# mirror of trixi_problem_desc (field order and types must match the C struct)
+mutable struct ProblemDesc
+    struct_size::Int32
+    ndims::Int32
+    polydeg::Int32
+    nvars::Int32
+    equation::Int32
+    volume_integral::Int32
+    volume_flux::Int32
+    surface_flux::Int32
+    volume_flux_fv::Int32
+    precision::Int32
+    gamma::Float64
+    advection_velocity::NTuple{3, Float64}
+    alpha_max::Float64
+    alpha_min::Float64
+    alpha_smooth::Int32
+    indicator_variable::Int32
+    nelements::Int64
+    inverse_jacobian::Ptr{Float64}
+    ninterfaces::Int64
+    interface_neighbor_ids::Ptr{Int64}
+    interface_orientations::Ptr{Int64}
+    nboundaries::Int64
+    nmortars::Int64
+    mortar_neighbor_ids::Ptr{Int64}
+    mortar_large_sides::Ptr{Int64}
+    mortar_orientations::Ptr{Int64}
+    weights::Ptr{Float64}
+    derivative_split::Ptr{Float64}
+    derivative_dhat::Ptr{Float64}
+    inverse_vandermonde_legendre::Ptr{Float64}
+    forward_upper::Ptr{Float64}
+    forward_lower::Ptr{Float64}
+    reverse_upper::Ptr{Float64}
+    reverse_lower::Ptr{Float64}
+end
+
+flux_code(::typeof(Trixi.flux_ranocha)) = FLUX_RANOCHA
+flux_code(::typeof(Trixi.flux_central)) = FLUX_CENTRAL
+flux_code(::Trixi.FluxLaxFriedrichs) = FLUX_LAX_FRIEDRICHS
+
+function check(status)
+    status == 0 && return nothing
+    buf = Vector{UInt8}(undef, 1024)
+    ccall((:trixi_last_error, libtrixi), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), C_NULL, buf, length(buf))
+    error("libtrixi_b200: status $status: " * unsafe_string(pointer(buf)))
+end
+
+"""
+    create_handle(mesh, equations, solver, cache_cpu; precision = 0)
+
+Builds the library handle from the CPU cache that `SemidiscretizationHyperbolicGPU`
+already creates with Trixi's `init_*` (semidiscretization_hyperbolic.jl:69-72):
+the connectivity containers are passed as host pointers in their Julia layout,
+together with Trixi's own basis matrices (so both sides use identical operators).
+"""
+function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
+    elements, interfaces, mortars = cache_cpu.elements, cache_cpu.interfaces, cache_cpu.mortars
+    basis = solver.basis
+    vi = solver.volume_integral
+    vol, vflux, fvflux = VOLUME_WEAK_FORM, FLUX_CENTRAL, FLUX_LAX_FRIEDRICHS
+    amax, amin, asmooth = 0.5, 0.001, Int32(1)
+    if vi isa Trixi.VolumeIntegralFluxDifferencing
+        vol, vflux = VOLUME_FLUX_DIFFERENCING, flux_code(vi.volume_flux)
+    elseif vi isa Trixi.VolumeIntegralShockCapturingHG
+        vol, vflux, fvflux = VOLUME_SHOCK_CAPTURING_HG, flux_code(vi.volume_flux_dg), flux_code(vi.volume_flux_fv)
+        amax, amin, asmooth = vi.indicator.alpha_max, vi.indicator.alpha_min, Int32(vi.indicator.alpha_smooth)
+    end
+    eq = equations isa Trixi.AbstractCompressibleEulerEquations ? EQ_COMPRESSIBLE_EULER : EQ_LINEAR_ADVECTION
+    adv = eq == EQ_LINEAR_ADVECTION ? (Float64.(equations.advection_velocity)..., 0.0, 0.0, 0.0)[1:3] : (0.0, 0.0, 0.0)
+    gamma = eq == EQ_COMPRESSIBLE_EULER ? Float64(equations.gamma) : 1.4
+    # keep the host arrays alive for the duration of the call
+    dsplit = Matrix{Float64}(Array(basis.derivative_split))
+    dhat = Matrix{Float64}(Array(basis.derivative_dhat))
+    weights = Vector{Float64}(basis.weights)
+    desc = ProblemDesc(0, ndims(mesh), Trixi.polydeg(basis), nvariables(equations), eq, vol, vflux,
+                       flux_code(solver.surface_integral.surface_flux), fvflux, Int32(precision), gamma, adv,
+                       amax, amin, asmooth, Int32(0),
+                       nelements(elements), pointer(elements.inverse_jacobian),
+                       ninterfaces(interfaces), pointer(interfaces.neighbor_ids), pointer(interfaces.orientations),
+                       0, Trixi.nmortars(mortars), pointer(mortars.neighbor_ids), pointer(mortars.large_sides),
+                       pointer(mortars.orientations), pointer(weights), pointer(dsplit), pointer(dhat),
+                       C_NULL, C_NULL, C_NULL, C_NULL, C_NULL)
+    desc.struct_size = Int32(sizeof(ProblemDesc))
+    handle = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve elements interfaces mortars dsplit dhat weights desc begin
+        check(ccall((:trixi_create, libtrixi), Cint, (Ref{ProblemDesc}, Ref{Ptr{Cvoid}}), desc, handle))
+    end
+    h = handle[]
+    return h
+end
+
+stream_ptr() = reinterpret(Ptr{Cvoid}, CUDA.stream().handle)
+
+# rhs_gpu!(du_ode, u_ode, semi, t) -- src/solvers/solvers.jl:18-31
+function rhs_gpu!(du_ode::CuArray{Float64}, u_ode::CuArray{Float64}, handle::Ptr{Cvoid}, t)
+    check(ccall((:trixi_rhs, libtrixi), Cint, (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Float64, Ptr{Cvoid}),
+                handle, pointer(du_ode), pointer(u_ode), Float64(t), stream_ptr()))
+    return nothing
+end
+
+# one fused CarpenterKennedy2N54 stage: k <- a k + dt rhs(u_in); u_out <- u_in + b k
+function rk_stage!(u_out, u_in, k, a, b, dt, t, handle)
+    check(ccall((:trixi_rk_stage, libtrixi), Cint,
+                (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, CuPtr{Float64}, Float64, Float64, Float64, Float64, Ptr{Cvoid}),
+                handle, pointer(u_out), pointer(u_in), pointer(k), a, b, dt, t, stream_ptr()))
+end
+
+# stage functions of the reference (cuda_volume_integral!, ...), e.g.
+cuda_volume_integral!(du, u, handle) =
+    check(ccall((:trixi_volume_integral, libtrixi), Cint, (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Ptr{Cvoid}),
+                handle, pointer(du), pointer(u), stream_ptr()))
+cuda_prolong2interfaces!(u, handle) =
+    check(ccall((:trixi_prolong2interfaces, libtrixi), Cint, (Ptr{Cvoid}, CuPtr{Float64}, Ptr{Cvoid}),
+                handle, pointer(u), stream_ptr()))
+cuda_interface_flux!(handle) =
+    check(ccall((:trixi_interface_flux, libtrixi), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), handle, stream_ptr()))
+cuda_surface_integral!(du, handle) =
+    check(ccall((:trixi_surface_integral, libtrixi), Cint, (Ptr{Cvoid}, CuPtr{Float64}, Ptr{Cvoid}),
+                handle, pointer(du), stream_ptr()))
+cuda_jacobian!(du, handle) =
+    check(ccall((:trixi_jacobian, libtrixi), Cint, (Ptr{Cvoid}, CuPtr{Float64}, Ptr{Cvoid}),
+                handle, pointer(du), stream_ptr()))
+
+destroy!(handle) = ccall((:trixi_destroy, libtrixi), Cint, (Ptr{Cvoid},), handle)
+
+end # module
