@@ -198,6 +198,13 @@ int trixi_lgl_basis(int polydeg, int which, double *host_out, int64_t count);
  * the flux-differencing kernels.  Synchronizes the stream. */
 int trixi_probe_fma_peak(int precision, int iters, double *flops_per_s, void *stream);
 
+/* Diagnostic without a counterpart in the reference: the mixed-precision
+ * kernels' integer-pipe conversions (double -> float, round to nearest even;
+ * float -> double, exact) applied elementwise to device arrays of length n,
+ * so that tests can compare them bit for bit with the hardware conversions. */
+int trixi_probe_convert(const double *in_d, float *out_f, const float *in_f, double *out_d, int64_t n,
+                        void *stream);
+
 /* Waits for the handle's stream work, then checks the device error word. */
 int trixi_synchronize(trixi_handle *h, void *stream);
 

@@ -9,23 +9,26 @@
 //   and optionally the 2N low-storage RK stage update (OrdinaryDiffEq's
 //   CarpenterKennedy2N54 broadcast, outside the reference).
 //
-// Work decomposition ("lines"): a tensor-product element is a set of 1D lines
-// of N nodes along each dimension.  One thread owns one line: it keeps the N
-// nodal states in registers, evaluates each symmetric two-point flux once
-// (N(N-1)/2 pairs instead of the reference's N^2), and computes the two
-// surface fluxes at the line's ends itself, reading the neighbouring
-// element's adjacent node straight from u ("owner computes": no
-// interfaces.u or surface_flux_values round trip through HBM).  Faces on a
-// mortar take their flux from a small per-mortar buffer filled by
-// dg_mortar_kernel.  Each line writes its partial du for its direction to
-// shared memory; the node phase sums the directions, scales by -J^{-1} and
-// either stores du or performs the RK update with coalesced global accesses.
+// Work decomposition: one thread per two-point flux.  Phase A stages the
+// tile's states in shared memory (conservative and primitive variables, in
+// the compute precision).  Phase B evaluates every flux the tile needs, each
+// exactly once per element: the symmetric volume fluxes f#(u_i, u_m), i < m,
+// on every line (N(N-1)/2 per line instead of the reference's N^2), the
+// surface fluxes on the element's 2*ndims faces (the neighbour's adjacent
+// node is read straight from u -- "owner computes", no interfaces.u or
+// surface_flux_values round trip through HBM; mortar faces read the flux
+// prepared by the mortar kernel), and for shock capturing the LGL subcell
+// FV fluxes.  Phase C gives one thread per (node, variable): it sums
+// D_split / D_hat times the staged fluxes along each dimension, adds the
+// surface terms, scales by -J^{-1}, and stores du or performs the RK update,
+// with coalesced global accesses in the reference layout.
 #pragma once
+#include "dg_convert.cuh"
 #include "dg_physics.cuh"
 
 namespace trixi {
 
-constexpr int NMAXT = 6;        // largest N = polydeg + 1 compiled
+constexpr int NMAXT = 6;  // largest N = polydeg + 1 compiled
 
 template <typename R>
 struct FusedParams {
@@ -50,19 +53,47 @@ struct FusedParams {
   R lhat_l, lhat_r;                         // 1/w_1, 1/w_N (boundary_interpolation)
 };
 
-// Offset of the first node of line t (face index t) along orientation O.
+// Node index of the point at position a along orientation O on line t (the
+// face index of the line: remaining coordinates in increasing order).
 template <int DIM, int N, int O>
-__device__ __forceinline__ int line_offset(int t) {
+__device__ __forceinline__ int line_node(int t, int a) {
   if constexpr (DIM == 1) {
-    return 0;
+    return a;
   } else if constexpr (DIM == 2) {
-    return (O == 0) ? t * N : t;
+    return (O == 0) ? a + t * N : t + a * N;
   } else {
     const int t1 = t % N, t2 = t / N;
-    if constexpr (O == 0) return t1 * N + t2 * N * N;
-    else if constexpr (O == 1) return t1 + t2 * N * N;
-    else return t1 + t2 * N;
+    if constexpr (O == 0) return a + t1 * N + t2 * N * N;
+    else if constexpr (O == 1) return t1 + a * N + t2 * N * N;
+    else return t1 + t2 * N + a * N * N;
   }
+}
+
+// index of the pair (a, b), a != b, among the N(N-1)/2 pairs of a line
+template <int N>
+__device__ __forceinline__ int pair_index(int a, int b) {
+  const int lo = a < b ? a : b, hi = a < b ? b : a;
+  return lo * (2 * N - lo - 1) / 2 + (hi - lo - 1);
+}
+
+// (i, m) of pair p, packed 4 bits per pair into one 64-bit constant each
+template <int N>
+struct PairBits {
+  static constexpr unsigned long long pack(bool second) {
+    unsigned long long bits = 0;
+    int p = 0;
+    for (int a = 0; a < N; ++a)
+      for (int b = a + 1; b < N; ++b, ++p) bits |= (unsigned long long)(second ? b : a) << (4 * p);
+    return bits;
+  }
+  static constexpr unsigned long long I = pack(false);
+  static constexpr unsigned long long M = pack(true);
+};
+
+template <int N>
+__device__ __forceinline__ void pair_nodes(int p, int &i, int &m) {
+  i = (int)((PairBits<N>::I >> (4 * p)) & 0xfull);
+  m = (int)((PairBits<N>::M >> (4 * p)) & 0xfull);
 }
 
 template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX>
@@ -71,239 +102,336 @@ struct FusedKernel {
   static constexpr int NV = P::NV;
   static constexpr int NN = ipow(N, DIM);
   static constexpr int NF = ipow(N, DIM - 1);
-  static constexpr int LINES = DIM * NF;
+  static constexpr int NP = N * (N - 1) / 2;
+  // staged fluxes per element and direction
+  static constexpr int VOL_PER_DIR = (VOL == VOL_WEAK) ? NN : NF * NP;
+  static constexpr int SURF_PER_EL = 2 * DIM * NF;
+  static constexpr int FV_PER_DIR = (VOL == VOL_SC) ? NF * (N - 1) : 0;
+  static constexpr int ITEMS_PER_EL = DIM * VOL_PER_DIR + SURF_PER_EL + DIM * FV_PER_DIR;
+  static constexpr int F_PER_EL = ITEMS_PER_EL * NV;
+  static constexpr int BLOCK = 256;
+  static constexpr size_t smem_for(int epb) {
+    return sizeof(R) * ((size_t)epb * (2 * NV * NN + F_PER_EL) + 2 * epb + 2 * N * N + N);
+  }
+  // elements per block: ~2 flux items per thread, <= 48 KB of shared memory
+  static constexpr int epb_pick() {
+    int e = (2 * BLOCK + ITEMS_PER_EL - 1) / ITEMS_PER_EL;
+    if (e < 1) e = 1;
+    if (e > 32) e = 32;
+    while (e > 1 && smem_for(e) > 48 * 1024) --e;
+    return e;
+  }
+  static constexpr int EPB = epb_pick();
+  static size_t smem_bytes() { return smem_for(EPB); }
 
-  static size_t smem_bytes(int epb) {
-    return sizeof(R) * ((size_t)(2 + DIM) * epb * NV * NN + epb);
+  struct Smem {
+    R *cons, *prim, *fvol, *fsurf, *ffv, *alpha, *scale, *dsplit, *dhat, *invw;
+    // [el][v][node]
+    __device__ __forceinline__ R &c(int el, int v, int n) const { return cons[(el * NV + v) * NN + n]; }
+    __device__ __forceinline__ R &w(int el, int v, int n) const { return prim[(el * NV + v) * NN + n]; }
+    // [el][dir][slot][v]
+    __device__ __forceinline__ R *vol(int el, int d, int slot) const {
+      return fvol + ((el * DIM + d) * VOL_PER_DIR + slot) * NV;
+    }
+    // [el][face][t][v]
+    __device__ __forceinline__ R *surf(int el, int face, int t) const {
+      return fsurf + ((el * 2 * DIM + face) * NF + t) * NV;
+    }
+    // [el][dir][t][a][v]
+    __device__ __forceinline__ R *fv(int el, int d, int t, int a) const {
+      return ffv + (((el * DIM + d) * NF + t) * (N - 1) + a) * NV;
+    }
+  };
+
+  __device__ __forceinline__ static void load_node(const Smem &s, int el, int n, R *u, R *w) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      u[v] = s.c(el, v, n);
+      w[v] = s.w(el, v, n);
+    }
   }
 
+  // volume item: one symmetric pair (FD / SC) or one nodal physical flux (weak form)
   template <int O>
-  __device__ __forceinline__ static void line(const FusedParams<R> &p, int el, int t, int64_t e0, const R *s_cons,
-                                              const R *s_prim, R *s_du, const R *s_alpha) {
-    constexpr int S = ipow(N, O);
-    const int off = line_offset<DIM, N, O>(t);
-    const int64_t e = e0 + el;
-    const PhysParams<R> &pp = p.pp;
-    const bool surface = (p.mode != MODE_VOLUME);
-
-    // issue the neighbour-trace loads first; their latency overlaps the volume work
-    int32_t nbl = 0, nbr = 0;
-    double gl[NV], gr[NV];
-    if (surface) {
-      nbl = p.face_table[e * (2 * DIM) + 2 * O];
-      nbr = p.face_table[e * (2 * DIM) + 2 * O + 1];
-      if (nbl >= 0) {
-        const double *src = p.u_in + ((int64_t)nbl * NN + off + (N - 1) * S) * NV;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) gl[v] = src[v];
-      } else {
-        const double *src = p.mortar_flux + ((int64_t)(-nbl - 1) * NF + t) * NV;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) gl[v] = src[v];
-      }
-      if (nbr >= 0) {
-        const double *src = p.u_in + ((int64_t)nbr * NN + off) * NV;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) gr[v] = src[v];
-      } else {
-        const double *src = p.mortar_flux + ((int64_t)(-nbr - 1) * NF + t) * NV;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) gr[v] = src[v];
-      }
-    }
-
-    R w[N][NV];
-    R acc[N][NV];
-#pragma unroll
-    for (int a = 0; a < N; ++a)
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        w[a][v] = s_prim[(el * NV + v) * NN + off + a * S];
-        acc[a][v] = R(0);
-      }
-
+  __device__ __forceinline__ static void volume_item(const FusedParams<R> &p, const Smem &s, int el, int r) {
+    R f[NV];
     if constexpr (VOL == VOL_WEAK) {
-      // du_i = sum_m dhat[i,m] f_O(u_m)
-      R f[N][NV];
-#pragma unroll
-      for (int a = 0; a < N; ++a) {
-        R ua[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) ua[v] = s_cons[(el * NV + v) * NN + off + a * S];
-        P::template flux<O>(ua, w[a], f[a], pp);
-      }
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int m = 0; m < N; ++m)
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[i][v] += p.dhat[i * N + m] * f[m][v];
+      R u[NV], w[NV];
+      load_node(s, el, r, u, w);
+      P::template flux<O>(u, w, f, p.pp);
     } else {
-      // symmetric flux differencing: each pair (i<m) evaluated once,
-      // du_i += dsplit[i,m] f#, du_m += dsplit[m,i] f#
-      constexpr bool need_cons = (VFLUX != FLUX_RANOCHA) || (EQ == EQ_ADV);
-      R uc[need_cons ? N : 1][NV];
-      if constexpr (need_cons) {
-#pragma unroll
-        for (int a = 0; a < N; ++a)
-#pragma unroll
-          for (int v = 0; v < NV; ++v) uc[a][v] = s_cons[(el * NV + v) * NN + off + a * S];
-      }
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int m = i + 1; m < N; ++m) {
-          R f[NV];
-          two_point_flux_t<DIM, EQ, R, O, VFLUX>(need_cons ? uc[need_cons ? i : 0] : w[i], w[i],
-                                                 need_cons ? uc[need_cons ? m : 0] : w[m], w[m], f, pp);
-          const R dim_ = p.dsplit[i * N + m], dmi = p.dsplit[m * N + i];
-#pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            acc[i][v] += dim_ * f[v];
-            acc[m][v] += dmi * f[v];
-          }
-        }
-      if constexpr (VOL == VOL_SC) {
-        const R alpha = s_alpha[el];
-        if (!(dev_fabs(alpha) <= R(p.atol))) {
-          // (1 - alpha) * DG + alpha * FV with LGL subcell fluxes on the line
-#pragma unroll
-          for (int a = 0; a < N; ++a)
-#pragma unroll
-            for (int v = 0; v < NV; ++v) acc[a][v] *= (R(1) - alpha);
-#pragma unroll
-          for (int a = 0; a + 1 < N; ++a) {
-            R ul[NV], ur[NV], g[NV];
-#pragma unroll
-            for (int v = 0; v < NV; ++v) {
-              ul[v] = s_cons[(el * NV + v) * NN + off + a * S];
-              ur[v] = s_cons[(el * NV + v) * NN + off + (a + 1) * S];
-            }
-            two_point_flux<DIM, EQ, R, O>(p.fv_flux, ul, w[a], ur, w[a + 1], g, pp);
-#pragma unroll
-            for (int v = 0; v < NV; ++v) {
-              acc[a][v] += alpha * p.invw[a] * g[v];
-              acc[a + 1][v] -= alpha * p.invw[a + 1] * g[v];
-            }
-          }
-        }
-      }
+      const int t = r / NP, pp_ = r - (r / NP) * NP;
+      int i, m;
+      pair_nodes<N>(pp_, i, m);
+      R ui[NV], wi[NV], um[NV], wm[NV];
+      load_node(s, el, line_node<DIM, N, O>(t, i), ui, wi);
+      load_node(s, el, line_node<DIM, N, O>(t, m), um, wm);
+      two_point_flux_t<DIM, EQ, R, O, VFLUX>(ui, wi, um, wm, f, p.pp);
     }
+    R *dst = s.vol(el, O, r);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dst[v] = f[v];
+  }
 
-    if (surface) {
-      // left end: face -O, u_ll = neighbour, u_rr = own node 0
-      R fs[NV];
-      if (nbl >= 0) {
-        R un[NV], wn[NV], u0[NV];
+  // surface item: face 2*O + side, face node t
+  template <int O>
+  __device__ __forceinline__ static void surface_item(const FusedParams<R> &p, const Smem &s, int64_t e0, int el,
+                                                      int side, int t) {
+    const int64_t e = e0 + el;
+    const int32_t nb = p.face_table[e * (2 * DIM) + 2 * O + side];
+    R f[NV];
+    if (nb >= 0) {
+      const int own = line_node<DIM, N, O>(t, side == 0 ? 0 : N - 1);
+      const int other = line_node<DIM, N, O>(t, side == 0 ? N - 1 : 0);
+      const double *src = p.u_in + ((int64_t)nb * NN + other) * NV;
+      R un[NV], wn[NV], uo[NV], wo[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          un[v] = R(gl[v]);
-          u0[v] = s_cons[(el * NV + v) * NN + off];
-        }
-        P::prim(un, wn, pp);
-        two_point_flux<DIM, EQ, R, O>(p.surface_flux, un, wn, u0, w[0], fs, pp);
-      } else {
+      for (int v = 0; v < NV; ++v) un[v] = from_double<R>(src[v]);
+      P::prim(un, wn, p.pp);
+      load_node(s, el, own, uo, wo);
+      if (side == 0)
+        two_point_flux<DIM, EQ, R, O>(p.surface_flux, un, wn, uo, wo, f, p.pp);
+      else
+        two_point_flux<DIM, EQ, R, O>(p.surface_flux, uo, wo, un, wn, f, p.pp);
+    } else {
+      const double *src = p.mortar_flux + ((int64_t)(-nb - 1) * NF + t) * NV;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) fs[v] = R(gl[v]);
-      }
-#pragma unroll
-      for (int v = 0; v < NV; ++v) acc[0][v] -= p.lhat_l * fs[v];
-      // right end: face +O, u_ll = own node N-1, u_rr = neighbour
-      if (nbr >= 0) {
-        R un[NV], wn[NV], u1[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          un[v] = R(gr[v]);
-          u1[v] = s_cons[(el * NV + v) * NN + off + (N - 1) * S];
-        }
-        P::prim(un, wn, pp);
-        two_point_flux<DIM, EQ, R, O>(p.surface_flux, u1, w[N - 1], un, wn, fs, pp);
-      } else {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) fs[v] = R(gr[v]);
-      }
-#pragma unroll
-      for (int v = 0; v < NV; ++v) acc[N - 1][v] += p.lhat_r * fs[v];
+      for (int v = 0; v < NV; ++v) f[v] = from_double<R>(src[v]);
     }
+    R *dst = s.surf(el, 2 * O + side, t);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dst[v] = f[v];
+  }
 
-    R *dst = s_du + (size_t)O * p.epb * NV * NN;
+  // FV subcell item (shock capturing): flux between nodes a and a+1 of line t
+  template <int O>
+  __device__ __forceinline__ static void fv_item(const FusedParams<R> &p, const Smem &s, int el, int t, int a) {
+    R ul[NV], wl[NV], ur[NV], wr[NV], f[NV];
+    load_node(s, el, line_node<DIM, N, O>(t, a), ul, wl);
+    load_node(s, el, line_node<DIM, N, O>(t, a + 1), ur, wr);
+    two_point_flux<DIM, EQ, R, O>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
+    R *dst = s.fv(el, O, t, a);
 #pragma unroll
-    for (int a = 0; a < N; ++a)
-#pragma unroll
-      for (int v = 0; v < NV; ++v) dst[(el * NV + v) * NN + off + a * S] = acc[a][v];
+    for (int v = 0; v < NV; ++v) dst[v] = f[v];
   }
 
   __device__ __forceinline__ static void run(const FusedParams<R> &p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int epb = p.epb;
-    R *s_cons = reinterpret_cast<R *>(smem_raw);
-    R *s_prim = s_cons + (size_t)epb * NV * NN;
-    R *s_du = s_prim + (size_t)epb * NV * NN;
-    R *s_alpha = s_du + (size_t)DIM * epb * NV * NN;
+    constexpr int epb = EPB;
+    Smem s;
+    s.cons = reinterpret_cast<R *>(smem_raw);
+    s.prim = s.cons + epb * NV * NN;
+    s.fvol = s.prim + epb * NV * NN;
+    s.fsurf = s.fvol + epb * DIM * VOL_PER_DIR * NV;
+    s.ffv = s.fsurf + epb * SURF_PER_EL * NV;
+    s.alpha = s.ffv + epb * DIM * FV_PER_DIR * NV;
+    s.scale = s.alpha + epb;
+    s.dsplit = s.scale + epb;
+    s.dhat = s.dsplit + N * N;
+    s.invw = s.dhat + N * N;
 
     const int64_t e0 = (int64_t)blockIdx.x * epb;
     if (e0 >= p.nelements) return;
     const int ne = (int)min((int64_t)epb, p.nelements - e0);
-    const int64_t base = e0 * NN * NV;
-    const int nval = ne * NN * NV;
+    const int mode = p.mode;
+    const bool surface = (mode != MODE_VOLUME);
 
-    // phase A: coalesced load of the tile (elements are contiguous in u)
-    for (int i = threadIdx.x; i < nval; i += blockDim.x) {
-      const int el = i / (NN * NV);
-      const int r = i - el * (NN * NV);
-      const int node = r / NV;
-      const int v = r - node * NV;
-      s_cons[(el * NV + v) * NN + node] = R(p.u_in[base + i]);
-    }
-    if constexpr (VOL == VOL_SC) {
-      for (int el = threadIdx.x; el < ne; el += blockDim.x) s_alpha[el] = R(p.alpha[e0 + el]);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < ne * NN; i += blockDim.x) {
-      const int el = i / NN, node = i - el * NN;
+    // phase A: one thread per (element, node): load the node's variables,
+    // convert, primitive variables; per-element factors; operators to smem
+    for (int q = threadIdx.x; q < epb * NN; q += BLOCK) {
+      const int el = q / NN, node = q - (q / NN) * NN;
+      if (el >= ne) continue;
+      const double *src = p.u_in + ((e0 + el) * NN + node) * NV;
       R uu[NV], ww[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) uu[v] = s_cons[(el * NV + v) * NN + node];
+      for (int v = 0; v < NV; ++v) uu[v] = from_double<R>(src[v]);
       P::prim(uu, ww, p.pp);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) s_prim[(el * NV + v) * NN + node] = ww[v];
+      for (int v = 0; v < NV; ++v) {
+        s.c(el, v, node) = uu[v];
+        s.w(el, v, node) = ww[v];
+      }
+    }
+    if (threadIdx.x < epb && threadIdx.x < ne) {
+      const int el = threadIdx.x;
+      if constexpr (VOL == VOL_SC) {
+        const double a = p.alpha[e0 + el];
+        s.alpha[el] = (fabs(a) <= p.atol) ? R(0) : from_double<R>(a);
+      }
+      // per-element factor of the node phase: -J^{-1} (rhs) or -J^{-1} dt (RK)
+      const double f = -p.inv_jac[e0 + el] * (mode == MODE_RK ? p.dt : 1.0);
+      s.scale[el] = from_double<R>(f);
+    }
+    for (int q = threadIdx.x; q < N * N; q += BLOCK) {
+      s.dsplit[q] = p.dsplit[q];
+      s.dhat[q] = p.dhat[q];
+    }
+    if (threadIdx.x < N) s.invw[threadIdx.x] = p.invw[threadIdx.x];
+    __syncthreads();
+
+    // phase B: every flux of the tile, sections [volume | surface | FV],
+    // each ordered [direction][element][item] so warps stay on one direction
+    constexpr int PER_VOL = epb * VOL_PER_DIR;
+    constexpr int PER_SURF = epb * 2 * NF;
+    constexpr int PER_FV = epb * FV_PER_DIR;
+    constexpr int N_VOL = DIM * PER_VOL;
+    const int n_surf = surface ? DIM * PER_SURF : 0;
+    const int n_all = N_VOL + n_surf + DIM * PER_FV;
+    for (int w = threadIdx.x; w < n_all; w += BLOCK) {
+      if (w < N_VOL) {
+        const int dir = w / PER_VOL;
+        const int r0 = w - dir * PER_VOL;
+        const int el = r0 / VOL_PER_DIR, r = r0 - (r0 / VOL_PER_DIR) * VOL_PER_DIR;
+        if (el >= ne) continue;
+        if (dir == 0) volume_item<0>(p, s, el, r);
+        if constexpr (DIM > 1) if (dir == 1) volume_item<1>(p, s, el, r);
+        if constexpr (DIM > 2) if (dir == 2) volume_item<2>(p, s, el, r);
+      } else if (w < N_VOL + n_surf) {
+        const int w2 = w - N_VOL;
+        const int dir = w2 / PER_SURF;
+        const int r0 = w2 - dir * PER_SURF;
+        const int el = r0 / (2 * NF);
+        const int r1 = r0 - el * (2 * NF);
+        const int side = r1 / NF, t = r1 - (r1 / NF) * NF;
+        if (el >= ne) continue;
+        if (dir == 0) surface_item<0>(p, s, e0, el, side, t);
+        if constexpr (DIM > 1) if (dir == 1) surface_item<1>(p, s, e0, el, side, t);
+        if constexpr (DIM > 2) if (dir == 2) surface_item<2>(p, s, e0, el, side, t);
+      } else if constexpr (VOL == VOL_SC) {
+        const int w2 = w - N_VOL - n_surf;
+        const int dir = w2 / PER_FV;
+        const int r0 = w2 - dir * PER_FV;
+        const int el = r0 / FV_PER_DIR;
+        const int r1 = r0 - el * FV_PER_DIR;
+        const int t = r1 / (N - 1), a = r1 - (r1 / (N - 1)) * (N - 1);
+        if (el >= ne || s.alpha[el] == R(0)) continue;
+        if (dir == 0) fv_item<0>(p, s, el, t, a);
+        if constexpr (DIM > 1) if (dir == 1) fv_item<1>(p, s, el, t, a);
+        if constexpr (DIM > 2) if (dir == 2) fv_item<2>(p, s, el, t, a);
+      }
     }
     __syncthreads();
 
-    // phase B: one thread per line, items ordered [direction][element][line]
-    const int per_dir = ne * NF;
-    for (int w = threadIdx.x; w < DIM * per_dir; w += blockDim.x) {
-      const int dir = w / per_dir;
-      const int r = w - dir * per_dir;
-      const int el = r / NF, t = r - el * NF;
-      if (dir == 0) line<0>(p, el, t, e0, s_cons, s_prim, s_du, s_alpha);
-      if constexpr (DIM > 1) if (dir == 1) line<1>(p, el, t, e0, s_cons, s_prim, s_du, s_alpha);
-      if constexpr (DIM > 2) if (dir == 2) line<2>(p, el, t, e0, s_cons, s_prim, s_du, s_alpha);
-    }
-    __syncthreads();
-
-    // phase C: sum directions, -J^{-1}, store du or RK update (coalesced)
-    const size_t dstride = (size_t)epb * NV * NN;
-    for (int i = threadIdx.x; i < nval; i += blockDim.x) {
-      const int el = i / (NN * NV);
-      const int r = i - el * (NN * NV);
-      const int node = r / NV;
-      const int v = r - node * NV;
-      const int si = (el * NV + v) * NN + node;
-      R s = s_du[si];
-      if constexpr (DIM > 1) s += s_du[dstride + si];
-      if constexpr (DIM > 2) s += s_du[2 * dstride + si];
-      double d = double(s);
-      if (p.mode == MODE_VOLUME) {
-        p.out[base + i] = d;
-      } else {
-        d *= -p.inv_jac[e0 + el];
-        if (p.mode == MODE_RHS) {
-          p.out[base + i] = d;
+    // phase C: one thread per (element, node), all variables
+    const bool use_k = (mode == MODE_RK) && (p.rk_a != 0.0);
+    for (int q = threadIdx.x; q < epb * NN; q += BLOCK) {
+      const int el = q / NN, node = q - (q / NN) * NN;
+      if (el >= ne) continue;
+      int coord[3] = {0, 0, 0}, tface[3] = {0, 0, 0};
+      {
+        int qq = node;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          coord[d] = qq % N;
+          qq /= N;
+        }
+        if constexpr (DIM == 2) {
+          tface[0] = coord[1];
+          tface[1] = coord[0];
+        } else if constexpr (DIM == 3) {
+          tface[0] = coord[1] + N * coord[2];
+          tface[1] = coord[0] + N * coord[2];
+          tface[2] = coord[0] + N * coord[1];
+        }
+      }
+      R acc[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[v] = R(0);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        const int ci = coord[d];
+        if constexpr (VOL == VOL_WEAK) {
+          constexpr int strides[3] = {1, N, N * N};
+          const int n0 = node - ci * strides[d];
+#pragma unroll
+          for (int m = 0; m < N; ++m) {
+            const R dm = s.dhat[ci * N + m];
+            const R *F = s.vol(el, d, n0 + m * strides[d]);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[v] += dm * F[v];
+          }
         } else {
-          const double kk = (p.rk_a != 0.0 ? p.rk_a * p.k[base + i] : 0.0) + p.dt * d;
-          p.k[base + i] = kk;
-          p.out[base + i] = p.u_in[base + i] + p.rk_b * kk;
+#pragma unroll
+          for (int m = 0; m < N; ++m) {
+            if (m == ci) continue;
+            const R dm = s.dsplit[ci * N + m];
+            const R *F = s.vol(el, d, tface[d] * NP + pair_index<N>(ci, m));
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[v] += dm * F[v];
+          }
+        }
+      }
+      if constexpr (VOL == VOL_SC) {
+        const R alpha = s.alpha[el];
+        if (alpha != R(0)) {
+          R fv[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) fv[v] = R(0);
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            const int ci = coord[d];
+            const R iw = s.invw[ci];
+            if (ci + 1 < N) {
+              const R *F = s.fv(el, d, tface[d], ci);
+#pragma unroll
+              for (int v = 0; v < NV; ++v) fv[v] += iw * F[v];
+            }
+            if (ci > 0) {
+              const R *F = s.fv(el, d, tface[d], ci - 1);
+#pragma unroll
+              for (int v = 0; v < NV; ++v) fv[v] -= iw * F[v];
+            }
+          }
+#pragma unroll
+          for (int v = 0; v < NV; ++v) acc[v] = (R(1) - alpha) * acc[v] + alpha * fv[v];
+        }
+      }
+      if (surface) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          if (coord[d] == 0) {
+            const R *F = s.surf(el, 2 * d, tface[d]);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[v] -= p.lhat_l * F[v];
+          }
+          if (coord[d] == N - 1) {
+            const R *F = s.surf(el, 2 * d + 1, tface[d]);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[v] += p.lhat_r * F[v];
+          }
+        }
+      }
+      const int64_t g0 = ((e0 + el) * NN + node) * NV;
+      if (mode == MODE_VOLUME) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) p.out[g0 + v] = to_double(acc[v]);
+      } else if constexpr (sizeof(R) == sizeof(double)) {
+        const double sc = -p.inv_jac[e0 + el];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const double du = double(acc[v]) * sc;
+          if (mode == MODE_RHS) {
+            p.out[g0 + v] = du;
+          } else {
+            const double kk = (use_k ? p.rk_a * p.k[g0 + v] : 0.0) + p.dt * du;
+            p.k[g0 + v] = kk;
+            p.out[g0 + v] = p.u_in[g0 + v] + p.rk_b * kk;
+          }
+        }
+      } else {
+        // mixed precision: scale in FP32, widen exactly, accumulate the RK
+        // register and the state in FP64 (two FMAs on the FP64 pipe)
+        const R sc = s.scale[el];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const double dd = to_double(acc[v] * sc);
+          if (mode == MODE_RHS) {
+            p.out[g0 + v] = dd;
+          } else {
+            const double kk = use_k ? fma(p.rk_a, p.k[g0 + v], dd) : dd;
+            p.k[g0 + v] = kk;
+            p.out[g0 + v] = fma(p.rk_b, kk, p.u_in[g0 + v]);
+          }
         }
       }
     }

@@ -37,7 +37,6 @@ struct FusedHost {
 cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed, const FusedHost &h,
                          cudaStream_t s);
 bool fused_supported(int dim, int N, int eq, int vol, int vflux);
-int fused_default_epb(int dim, int N, int eq);
 
 cudaError_t launch_fused_1d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 cudaError_t launch_fused_2d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);

@@ -9,16 +9,6 @@
 
 namespace trixi {
 
-inline int default_epb(int dim, int N, int nv) {
-  // aim at ~128-256 line threads per block
-  int nf = 1;
-  for (int d = 1; d < dim; ++d) nf *= N;
-  const int lines = dim * nf;
-  int epb = std::max(1, 192 / lines);
-  (void)nv;
-  return std::min(epb, 32);
-}
-
 template <int DIM, int N, int EQ, typename R, int VOL, int VF>
 cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   using K = FusedKernel<DIM, N, EQ, R, VOL, VF>;
@@ -54,12 +44,10 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   for (int i = 0; i < NMAXT; ++i) p.invw[i] = R(i < N ? h.invw[i] : 0.0);
   p.lhat_l = R(h.lhat_l);
   p.lhat_r = R(h.lhat_r);
-  int epb = h.epb > 0 ? h.epb : default_epb(DIM, N, K::NV);
+  const int epb = K::EPB;  // compile-time tile size (see FusedKernel::epb_pick)
   p.epb = epb;
-  const int threads_needed = epb * K::LINES;
-  int block = ((threads_needed + 31) / 32) * 32;
-  block = std::max(64, std::min(256, block));
-  const size_t smem = K::smem_bytes(epb);
+  const int block = K::BLOCK;
+  const size_t smem = K::smem_bytes();
   // opt in once per instantiation to the large dynamic shared-memory carve-out
   static const cudaError_t attr = cudaFuncSetAttribute(dg_fused_kernel<DIM, N, EQ, R, VOL, VF>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

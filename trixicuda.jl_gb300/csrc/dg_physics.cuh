@@ -32,8 +32,16 @@ struct PhysParams {
   R a[3];                 // advection velocity
 };
 
+// Precision-specific elementary operations.  FP64 keeps IEEE division and
+// log; the FP32 path of the mixed-precision kernels uses the fast hardware
+// approximations (__fdividef: 2 ulp; __logf: absolute error ~2^-21 near 1),
+// well inside its error budget (the rhs in FP32 is accurate to ~1e-6 relative).
 __device__ __forceinline__ double dev_log(double x) { return log(x); }
-__device__ __forceinline__ float dev_log(float x) { return logf(x); }
+__device__ __forceinline__ float dev_log(float x) { return __logf(x); }
+__device__ __forceinline__ double dev_div(double a, double b) { return a / b; }
+__device__ __forceinline__ float dev_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double dev_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float dev_rcp(float x) { return __fdividef(1.0f, x); }
 __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float dev_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double dev_fabs(double x) { return fabs(x); }
@@ -41,20 +49,66 @@ __device__ __forceinline__ float dev_fabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double dev_fmax(double x, double y) { return fmax(x, y); }
 __device__ __forceinline__ float dev_fmax(float x, float y) { return fmaxf(x, y); }
 
-// Ismail-Roe logarithmic mean (x - y)/(log x - log y) with the series
-// 1/(1 + u/3 + u^2/5 + u^3/7) in u = ((x-y)/(x+y))^2 below 1e-4.
+// Ismail-Roe logarithmic mean (x - y)/(log x - log y) and its inverse.
+// With s = x + y and u = ((x - y)/s)^2, ln_mean = (s/2) / g(u) where
+// g(u) = artanh(f)/f = 1 + u/3 + u^2/5 + u^3/7 + ... (Ismail & Roe 2009).
+// Below the threshold the series is used: 1/g(u) = 1 - u/3 - 4u^2/45 -
+// 44u^3/945 + O(u^4) for the mean and g(u) itself for the inverse, so each
+// mean costs one reciprocal of s; above it, log(x/y) is evaluated.  The
+// threshold is 1e-4 in FP64 (truncation ~1e-18) and 1e-2 in FP32
+// (truncation ~1e-10, and log(x/y) is only formed for ratios above ~1.2,
+// where FP32 cancellation is harmless).
+template <typename R>
+struct LnMeanThreshold;
+template <>
+struct LnMeanThreshold<double> {
+  static constexpr double value = 1.0e-4;
+};
+template <>
+struct LnMeanThreshold<float> {
+  static constexpr float value = 1.0e-2f;
+};
+
+template <typename R>
+__device__ __forceinline__ R ln_mean_series(R s, R u) {
+  return R(0.5) * s * (R(1) + u * (R(-1.0 / 3.0) + u * (R(-4.0 / 45.0) + u * R(-44.0 / 945.0))));
+}
+template <typename R>
+__device__ __forceinline__ R inv_ln_mean_series(R r, R u) {
+  return R(2) * r * (R(1) + u * (R(1.0 / 3.0) + u * (R(1.0 / 5.0) + u * R(1.0 / 7.0))));
+}
+
 template <typename R>
 __device__ __forceinline__ R ln_mean(R x, R y) {
-  const R f2 = (x * (x - R(2) * y) + y * y) / (x * (x + R(2) * y) + y * y);
-  if (f2 < R(1.0e-4)) return (x + y) * R(52.5) / (R(105) + f2 * (R(35) + f2 * (R(21) + f2 * R(15))));
-  return (y - x) / dev_log(y / x);
+  const R s = x + y, d = x - y;
+  const R r = dev_rcp(s);
+  const R f = d * r;
+  const R u = f * f;
+  if (u < LnMeanThreshold<R>::value) return ln_mean_series(s, u);
+  return dev_div(d, dev_log(dev_div(x, y)));
 }
 
 template <typename R>
 __device__ __forceinline__ R inv_ln_mean(R x, R y) {
-  const R f2 = (x * (x - R(2) * y) + y * y) / (x * (x + R(2) * y) + y * y);
-  if (f2 < R(1.0e-4)) return (R(105) + f2 * (R(35) + f2 * (R(21) + f2 * R(15)))) / (R(52.5) * (x + y));
-  return dev_log(y / x) / (y - x);
+  const R s = x + y, d = x - y;
+  const R r = dev_rcp(s);
+  const R f = d * r;
+  const R u = f * f;
+  if (u < LnMeanThreshold<R>::value) return inv_ln_mean_series(r, u);
+  return dev_div(dev_log(dev_div(x, y)), d);
+}
+
+// Both means of flux_ranocha, ln_mean(x1, y1) and inv_ln_mean(x2, y2), from a
+// single reciprocal 1/((x1+y1)(x2+y2)).
+template <typename R>
+__device__ __forceinline__ void ranocha_means(R x1, R y1, R x2, R y2, R &mean1, R &inv_mean2) {
+  const R s1 = x1 + y1, d1 = x1 - y1, s2 = x2 + y2, d2 = x2 - y2;
+  const R q = dev_rcp(s1 * s2);
+  const R r1 = s2 * q, r2 = s1 * q;
+  const R f1 = d1 * r1, f2 = d2 * r2;
+  const R u1 = f1 * f1, u2 = f2 * f2;
+  mean1 = (u1 < LnMeanThreshold<R>::value) ? ln_mean_series(s1, u1) : dev_div(d1, dev_log(dev_div(x1, y1)));
+  inv_mean2 = (u2 < LnMeanThreshold<R>::value) ? inv_ln_mean_series(r2, u2) : dev_div(dev_log(dev_div(x2, y2)), d2);
 }
 
 // Physics of one equation system.  States: `u` conservative, `w` primitive
@@ -93,10 +147,11 @@ struct Physics<DIM, EQ_EULER, R> {
   static constexpr int NV = DIM + 2;
   __device__ __forceinline__ static void prim(const R *u, R *w, const PhysParams<R> &pp) {
     const R rho = u[0];
+    const R inv_rho = dev_rcp(rho);
     R kin = R(0);
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-      w[1 + d] = u[1 + d] / rho;
+      w[1 + d] = u[1 + d] * inv_rho;
       kin += u[1 + d] * w[1 + d];
     }
     w[0] = rho;
@@ -126,8 +181,9 @@ struct Physics<DIM, EQ_EULER, R> {
   __device__ __forceinline__ static void ranocha(const R *, const R *wl, const R *, const R *wr, R *f,
                                                  const PhysParams<R> &pp) {
     const R rl = wl[0], rr = wr[0], pl = wl[DIM + 1], pr = wr[DIM + 1];
-    const R rho_mean = ln_mean(rl, rr);
-    const R inv_rho_p_mean = pl * pr * inv_ln_mean(rl * pr, rr * pl);
+    R rho_mean, inv_mean;
+    ranocha_means(rl, rr, rl * pr, rr * pl, rho_mean, inv_mean);
+    const R inv_rho_p_mean = pl * pr * inv_mean;
     R vavg[DIM];
     R v2avg = R(0);
 #pragma unroll
@@ -155,8 +211,8 @@ struct Physics<DIM, EQ_EULER, R> {
   template <int O>
   __device__ __forceinline__ static R max_speed(const R *, const R *wl, const R *, const R *wr, bool naive,
                                                 const PhysParams<R> &pp) {
-    const R cl = dev_sqrt(pp.gamma * wl[DIM + 1] / wl[0]);
-    const R cr = dev_sqrt(pp.gamma * wr[DIM + 1] / wr[0]);
+    const R cl = dev_sqrt(dev_div(pp.gamma * wl[DIM + 1], wl[0]));
+    const R cr = dev_sqrt(dev_div(pp.gamma * wr[DIM + 1], wr[0]));
     if (naive) return dev_fmax(dev_fabs(wl[1 + O]), dev_fabs(wr[1 + O])) + dev_fmax(cl, cr);
     return dev_fmax(dev_fabs(wl[1 + O]) + cl, dev_fabs(wr[1 + O]) + cr);
   }

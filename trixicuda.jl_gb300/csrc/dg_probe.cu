@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "../../include/trixi_b200.h"
+#include "dg_convert.cuh"
 
 namespace {
 
@@ -60,4 +61,21 @@ extern "C" int trixi_probe_fma_peak(int precision, int iters, double *flops_per_
   if (!flops_per_s || iters <= 0) return TRIXI_ERR_INVALID_ARGUMENT;
   if (precision == TRIXI_PRECISION_FP64) return run<double>(iters, flops_per_s, (cudaStream_t)stream);
   return run<float>(iters, flops_per_s, (cudaStream_t)stream);
+}
+
+namespace {
+__global__ void convert_kernel(const double *in_d, float *out_f, const float *in_f, double *out_d, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out_f[i] = trixi::d2f_rn(in_d[i]);
+  out_d[i] = trixi::f2d_exact(in_f[i]);
+}
+}  // namespace
+
+extern "C" int trixi_probe_convert(const double *in_d, float *out_f, const float *in_f, double *out_d, int64_t n,
+                                   void *stream) {
+  if (n < 0 || (n > 0 && (!in_d || !out_f || !in_f || !out_d))) return TRIXI_ERR_INVALID_ARGUMENT;
+  if (n == 0) return TRIXI_OK;
+  convert_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(in_d, out_f, in_f, out_d, n);
+  return cudaGetLastError() == cudaSuccess ? TRIXI_OK : TRIXI_ERR_CUDA;
 }

@@ -114,6 +114,7 @@ SIGNATURES = {
     "trixi_lgl_basis": (C.c_int, [_I, _I, C.POINTER(C.c_double), _I64]),
     "trixi_synchronize": (C.c_int, [_VP, _VP]),
     "trixi_probe_fma_peak": (C.c_int, [_I, _I, C.POINTER(C.c_double), _VP]),
+    "trixi_probe_convert": (C.c_int, [_VP, _VP, _VP, _VP, _I64, _VP]),
 }
 
 _lib = None
