@@ -119,6 +119,10 @@ typedef struct trixi_problem_desc {
   const double *derivative_dhat;
   const double *inverse_vandermonde_legendre;
   const double *forward_upper, *forward_lower, *reverse_upper, *reverse_lower;
+  /* Optional node coordinates [ndims, N^ndims, nelements] (elements.node_coordinates,
+   * src/solvers/containers_2d.jl:7), needed by trixi_compute_coefficients and
+   * trixi_calc_error_norms with an analytic reference. */
+  const double *node_coordinates;
 } trixi_problem_desc;
 
 /* Library version string ("trixi_b200 <semver> sm_103a"). */
@@ -183,6 +187,54 @@ int trixi_container(trixi_handle *h, int which, void **dev_ptr, int64_t *count);
  * smoothed as configured.  Replaces the host round trip
  * `indicator(Array(u), ...)` of src/solvers/dg_3d.jl:187 (indicators.jl:7-42). */
 int trixi_indicator(trixi_handle *h, const double *u, double *alpha, void *stream);
+
+/* Initial conditions evaluated on the GPU (params may be NULL for defaults):
+ *   TRIXI_IC_CONSTANT          params = the nvars conservative values
+ *   TRIXI_IC_CONVERGENCE_TEST  params = (c, A, L); advection default (1, 0.5, 2),
+ *                              Euler default (2, 0.1, 2)
+ *   TRIXI_IC_WEAK_BLAST_WAVE   Euler; no params */
+typedef enum trixi_initial_condition_kind {
+  TRIXI_IC_CONSTANT = 0,
+  TRIXI_IC_CONVERGENCE_TEST = 1,
+  TRIXI_IC_WEAK_BLAST_WAVE = 2
+} trixi_initial_condition_kind;
+
+/* u = initial condition at the nodes (needs desc.node_coordinates); 1D
+ * moves element end points one ulp inwards like the reference.  Replaces
+ * compute_coefficients_gpu / compute_coefficients_kernel! (src/solvers/dg.jl:46-160,
+ * src/semidiscretization/semidiscretization.jl:4-20). */
+int trixi_compute_coefficients(trixi_handle *h, int ic_kind, const double *params, int64_t nparams, double t,
+                               double *u, void *stream);
+
+/* dt_dev[0] = 2 / (N * max_e J^{-1}_e sum_d max_nodes lambda_d(u)) on the GPU
+ * (device scalar; multiply by the CFL number).  Replaces max_dt of the
+ * StepsizeCallback (src/callbacks_step/stepsize_dg_{1,2,3}d.jl), which copies
+ * u to the host every step. */
+int trixi_max_dt(trixi_handle *h, const double *u, double *dt_dev, void *stream);
+
+/* Quadrature integrals sum_e J_e sum_nodes w q (not normalised by the volume):
+ *   TRIXI_INTEGRAL_STATE               q = u (nvars results)
+ *   TRIXI_INTEGRAL_ENTROPY             q = -rho s/(gamma-1) (Euler), u^2/2 (advection)
+ *   TRIXI_INTEGRAL_ENTROPY_PRODUCTION  q = w(u) . du with the entropy variables w
+ *   TRIXI_INTEGRAL_DU                  q = du (nvars results)
+ * Synchronous: results are written to host memory.  Replaces
+ * integrate_via_indices (src/callbacks_step/analysis_dg_2d.jl:1-40). */
+typedef enum trixi_integral_kind {
+  TRIXI_INTEGRAL_STATE = 0,
+  TRIXI_INTEGRAL_ENTROPY = 1,
+  TRIXI_INTEGRAL_ENTROPY_PRODUCTION = 2,
+  TRIXI_INTEGRAL_DU = 3
+} trixi_integral_kind;
+int trixi_integrate(trixi_handle *h, const double *u, const double *du, int which, double *out_host, int64_t count,
+                    void *stream);
+
+/* L2 and Linf errors per variable after interpolation to 2*polydeg+1 LGL
+ * analysis nodes, against an analytic initial condition at time t (u_ref
+ * NULL) or against a second state u_ref on the same mesh.  L2 is normalised
+ * by the total volume.  Synchronous.  Replaces calc_error_norms
+ * (src/callbacks_step/analysis_dg_2d.jl:44-89). */
+int trixi_calc_error_norms(trixi_handle *h, const double *u, const double *u_ref, int ic_kind, const double *params,
+                           int64_t nparams, double t, double *l2_host, double *linf_host, void *stream);
 
 /* Copies a basis operator to host memory: 0 nodes, 1 weights, 2 derivative_split,
  * 3 derivative_dhat, 4 inverse_vandermonde_legendre, 5 forward_upper,

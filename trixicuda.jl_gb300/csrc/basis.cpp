@@ -233,4 +233,24 @@ bool compute_basis(int polydeg, Basis &b) {
   return true;
 }
 
+bool analysis_operators(int polydeg, int na, std::vector<double> &vdm, std::vector<double> &wa,
+                        std::vector<double> &xa) {
+  const int n = polydeg + 1;
+  if (n < 2 || na < 2 || na > 16) return false;
+  const auto x = lobatto_nodes(n);
+  const auto lam = bary(x);
+  const auto xq = lobatto_nodes(na);
+  const auto wq = lobatto_weights(xq);
+  vdm.assign((size_t)na * n, 0.0);
+  wa.resize(na);
+  xa.resize(na);
+  for (int i = 0; i < na; ++i) {
+    const auto l = lagrange(x, lam, xq[i]);
+    for (int j = 0; j < n; ++j) vdm[(size_t)i * n + j] = (double)l[j];  // row-major [analysis node][node]
+    wa[i] = (double)wq[i];
+    xa[i] = (double)xq[i];
+  }
+  return true;
+}
+
 }  // namespace trixi

@@ -15,4 +15,10 @@ struct Basis {
 
 bool compute_basis(int polydeg, Basis &b);
 
+// Interpolation from the polydeg LGL nodes to `na` LGL analysis nodes
+// (row-major [na][polydeg+1]), with the analysis weights and nodes -- the
+// SolutionAnalyzer of the reference (src/solvers/basis_lobatto_legendre.jl:120-137).
+bool analysis_operators(int polydeg, int na, std::vector<double> &vdm, std::vector<double> &wa,
+                        std::vector<double> &xa);
+
 }  // namespace trixi

@@ -18,6 +18,7 @@
 
 #include "../../include/trixi_b200.h"
 #include "basis.h"
+#include "dg_analysis.h"
 #include "dg_host.h"
 
 using namespace trixi;
@@ -61,6 +62,13 @@ struct trixi_handle {
   // stage containers (allocated on first use)
   double *d_interfaces_u = nullptr, *d_sfv = nullptr, *d_mortar_u[4] = {nullptr, nullptr, nullptr, nullptr};
   int epb = 0;
+  // analysis / initial conditions (allocated on first use)
+  double *d_coords = nullptr;
+  unsigned long long *d_acc = nullptr;
+  double *d_partial = nullptr, *d_partial2 = nullptr, *d_red_out = nullptr;
+  double *d_vdm = nullptr, *d_wa = nullptr, *d_w = nullptr;
+  std::vector<double> xa;
+  double total_volume = 0.0;
   FusedHost fused;
   std::string last_error;
   int last_status = TRIXI_OK;
@@ -112,7 +120,8 @@ void free_all(trixi_handle *h) {
   void *ptrs[] = {h->d_face_table, h->d_slot_nbrs, h->d_inv_jac, h->d_if_nid, h->d_if_ori, h->d_mo_nid,
                   h->d_mo_ls, h->d_mo_ori, h->d_mortar_flux, h->d_alpha_raw, h->d_alpha, h->d_err,
                   h->d_scratch_u, h->d_interfaces_u, h->d_sfv, h->d_mortar_u[0], h->d_mortar_u[1],
-                  h->d_mortar_u[2], h->d_mortar_u[3]};
+                  h->d_mortar_u[2], h->d_mortar_u[3], h->d_coords, h->d_acc, h->d_partial, h->d_partial2,
+                  h->d_red_out, h->d_vdm, h->d_wa, h->d_w};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -282,6 +291,7 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
       return bad("element %lld face %lld has no interface or mortar (non-periodic meshes are not supported)",
                  (long long)(i / nfaces) + 1, (long long)(i % nfaces) + 1);
 
+  for (int64_t e = 0; e < h->E; ++e) h->total_volume += std::pow(2.0 / d->inverse_jacobian[e], h->dim);
   // all host-side validation is done; from here on the device is touched
   cudaGetDevice(&h->device);
   cudaError_t e = cudaSuccess;
@@ -302,6 +312,9 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
     ok(cudaMalloc(&h->d_alpha, sizeof(double) * (size_t)h->E));
     if (h->d_alpha) ok(cudaMemset(h->d_alpha, 0, sizeof(double) * (size_t)h->E));
   }
+  if (d->node_coordinates)
+    ok(upload(&h->d_coords, d->node_coordinates, (size_t)(h->dim * h->NN * h->E)));
+  ok(upload(&h->d_w, h->basis.weights.data(), (size_t)h->N));
   ok(cudaMalloc(&h->d_err, sizeof(int)));
   if (h->d_err) ok(cudaMemset(h->d_err, 0, sizeof(int)));
   if (e != cudaSuccess) {
@@ -679,6 +692,180 @@ int trixi_synchronize(trixi_handle *h, void *stream) {
   int flag = 0;
   TRIXI_CUDA(h, cudaMemcpy(&flag, h->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read error word");
   if (flag) return fail(h, TRIXI_ERR_DEVICE_FLAG, "device error word %d", flag);
+  return TRIXI_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+IcParams ic_params(const trixi_handle *h, int kind, const double *params, int64_t nparams) {
+  IcParams ip{};
+  for (int i = 0; i < 3; ++i) ip.a[i] = h->adv[i];
+  ip.gamma = h->gamma;
+  if (kind == IC_CONVERGENCE_TEST) {
+    if (h->eq == EQ_ADV) {
+      ip.p[0] = 1.0; ip.p[1] = 0.5; ip.p[2] = 2.0;
+    } else {
+      ip.p[0] = 2.0; ip.p[1] = 0.1; ip.p[2] = 2.0;
+    }
+  }
+  for (int64_t i = 0; params && i < nparams && i < 8; ++i) ip.p[i] = params[i];
+  for (size_t i = 0; i < h->xa.size() && i < 16; ++i) ip.xa[i] = h->xa[i];
+  return ip;
+}
+
+int check_ic(trixi_handle *h, int kind, int64_t nparams, const double *params) {
+  if (kind < IC_CONSTANT || kind > IC_WEAK_BLAST_WAVE) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "ic kind %d", kind);
+  if (kind == IC_WEAK_BLAST_WAVE && h->eq != EQ_EULER)
+    return fail(h, TRIXI_ERR_UNSUPPORTED, "weak blast wave needs the Euler equations");
+  if (kind == IC_CONSTANT && (!params || nparams < h->nv))
+    return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "constant state needs %d params", h->nv);
+  if (nparams < 0 || nparams > 8) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "nparams %lld", (long long)nparams);
+  return TRIXI_OK;
+}
+
+int ensure_reduction(trixi_handle *h, int nq) {
+  if (!h->d_acc) TRIXI_CUDA(h, cudaMalloc(&h->d_acc, sizeof(unsigned long long)), "alloc reduction");
+  if (!h->d_partial) {
+    TRIXI_CUDA(h, cudaMalloc(&h->d_partial, sizeof(double) * (size_t)(h->E * std::max(nq, 5))), "alloc partials");
+    TRIXI_CUDA(h, cudaMalloc(&h->d_partial2, sizeof(double) * (size_t)(h->E * std::max(nq, 5))), "alloc partials");
+    TRIXI_CUDA(h, cudaMalloc(&h->d_red_out, sizeof(double) * 16), "alloc reduction out");
+  }
+  return TRIXI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int trixi_compute_coefficients(trixi_handle *h, int ic_kind, const double *params, int64_t nparams, double t,
+                               double *u, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = check_ic(h, ic_kind, nparams, params)) return st;
+  if (!h->d_coords) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "desc.node_coordinates was not given");
+  IcHost ih;
+  ih.dim = h->dim;
+  ih.eq = h->eq;
+  ih.N = h->N;
+  ih.kind = ic_kind;
+  ih.E = h->E;
+  ih.coords = h->d_coords;
+  ih.ip = ic_params(h, ic_kind, params, nparams);
+  ih.t = t;
+  ih.u = u;
+  TRIXI_CUDA(h, launch_initial_condition(ih, (cudaStream_t)stream), "initial condition");
+  return TRIXI_OK;
+}
+
+int trixi_max_dt(trixi_handle *h, const double *u, double *dt_dev, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = check_u_args(h, dt_dev, "dt")) return st;
+  if (int st = ensure_reduction(h, 1)) return st;
+  MaxDtHost mh;
+  mh.dim = h->dim;
+  mh.eq = h->eq;
+  mh.N = h->N;
+  mh.E = h->E;
+  mh.u = u;
+  mh.inv_jac = h->d_inv_jac;
+  mh.gamma = h->gamma;
+  for (int i = 0; i < 3; ++i) mh.a[i] = h->adv[i];
+  mh.acc = h->d_acc;
+  mh.dt = dt_dev;
+  TRIXI_CUDA(h, launch_max_dt(mh, (cudaStream_t)stream), "max_dt");
+  return TRIXI_OK;
+}
+
+int trixi_integrate(trixi_handle *h, const double *u, const double *du, int which, double *out_host, int64_t count,
+                    void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (which < 0 || which > 3) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "integral kind %d", which);
+  if ((which == 2 || which == 3) && !aligned8(du)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "du is required");
+  const int nq = (which == 0 || which == 3) ? h->nv : 1;
+  if (!out_host || count < nq) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "output needs %d values", nq);
+  if (int st = ensure_reduction(h, nq)) return st;
+  IntegrateHost ih;
+  ih.dim = h->dim;
+  ih.eq = h->eq;
+  ih.N = h->N;
+  ih.which = which;
+  ih.nq = nq;
+  ih.E = h->E;
+  ih.u = u;
+  ih.du = du;
+  ih.inv_jac = h->d_inv_jac;
+  ih.w = h->d_w;
+  ih.gamma = h->gamma;
+  ih.partial = h->d_partial;
+  ih.out = h->d_red_out;
+  cudaStream_t s = (cudaStream_t)stream;
+  TRIXI_CUDA(h, launch_integrate(ih, s), "integrate");
+  TRIXI_CUDA(h, cudaMemcpyAsync(out_host, h->d_red_out, sizeof(double) * nq, cudaMemcpyDeviceToHost, s), "copy");
+  TRIXI_CUDA(h, cudaStreamSynchronize(s), "synchronize");
+  return TRIXI_OK;
+}
+
+int trixi_calc_error_norms(trixi_handle *h, const double *u, const double *u_ref, int ic_kind, const double *params,
+                           int64_t nparams, double t, double *l2_host, double *linf_host, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (!l2_host || !linf_host) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "null output");
+  if (!u_ref) {
+    if (int st = check_ic(h, ic_kind, nparams, params)) return st;
+  } else if (!aligned8(u_ref)) {
+    return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "u_ref misaligned");
+  }
+  if (!h->d_coords && !u_ref) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "desc.node_coordinates was not given");
+  if (int st = ensure_reduction(h, h->nv)) return st;
+  const int na = 2 * (h->N - 1) + 1;  // SolutionAnalyzer: analysis_polydeg = 2 polydeg
+  if (!h->d_vdm) {
+    std::vector<double> vdm, wa, xa;
+    if (!analysis_operators(h->N - 1, na, vdm, wa, xa)) return fail(h, TRIXI_ERR_UNSUPPORTED, "analysis nodes");
+    TRIXI_CUDA(h, upload(&h->d_vdm, vdm.data(), vdm.size()), "upload analysis operators");
+    TRIXI_CUDA(h, upload(&h->d_wa, wa.data(), wa.size()), "upload analysis weights");
+    h->xa = xa;
+  }
+  ErrorNormHost eh;
+  eh.dim = h->dim;
+  eh.eq = h->eq;
+  eh.N = h->N;
+  eh.NA = na;
+  eh.nv = h->nv;
+  eh.kind = ic_kind;
+  eh.E = h->E;
+  eh.u = u;
+  eh.uref = u_ref;
+  eh.coords = h->d_coords;
+  eh.ip = ic_params(h, ic_kind, params, nparams);
+  eh.t = t;
+  eh.vdm = h->d_vdm;
+  eh.wa = h->d_wa;
+  eh.inv_jac = h->d_inv_jac;
+  eh.l2p = h->d_partial;
+  eh.linfp = h->d_partial2;
+  eh.l2_out = h->d_red_out;
+  eh.linf_out = h->d_red_out + 8;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!h->d_coords) {
+    // coordinates are only read for the analytic reference; give a harmless pointer
+    eh.coords = h->d_inv_jac;
+  }
+  TRIXI_CUDA(h, launch_error_norms_all(eh, s), "error norms");
+  double buf[16];
+  TRIXI_CUDA(h, cudaMemcpyAsync(buf, h->d_red_out, sizeof(double) * 16, cudaMemcpyDeviceToHost, s), "copy");
+  TRIXI_CUDA(h, cudaStreamSynchronize(s), "synchronize");
+  // total volume = sum_e (2 / J^{-1}_e)^d: L2 is normalised by it
+  double vol = 0.0;
+  if (h->total_volume <= 0.0) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "total volume");
+  vol = h->total_volume;
+  for (int v = 0; v < h->nv; ++v) {
+    l2_host[v] = std::sqrt(buf[v] / vol);
+    linf_host[v] = buf[8 + v];
+  }
   return TRIXI_OK;
 }
 

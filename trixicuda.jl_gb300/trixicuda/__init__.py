@@ -30,6 +30,10 @@ from .mesh import TreeMesh
 from .semidiscretization import (
     ODEProblem,
     SemidiscretizationHyperbolicGPU,
+    calc_error_norms,
+    compute_coefficients_gpu,
+    integrate,
+    max_dt,
     cuda_boundary_flux,
     cuda_indicator,
     cuda_interface_flux,

@@ -29,6 +29,9 @@ VOLUME_WEAK_FORM, VOLUME_FLUX_DIFFERENCING, VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
 FLUX_LAX_FRIEDRICHS, FLUX_RANOCHA, FLUX_CENTRAL, FLUX_LAX_FRIEDRICHS_NAIVE = 0, 1, 2, 3
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
+IC_CONSTANT, IC_CONVERGENCE_TEST, IC_WEAK_BLAST_WAVE = 0, 1, 2
+INTEGRAL_STATE, INTEGRAL_ENTROPY, INTEGRAL_ENTROPY_PRODUCTION, INTEGRAL_DU = 0, 1, 2, 3
+
 CONTAINER_INTERFACES_U = 0
 CONTAINER_SURFACE_FLUX_VALUES = 1
 CONTAINER_MORTARS_U = 2
@@ -84,6 +87,7 @@ class ProblemDesc(C.Structure):
         ("forward_lower", C.POINTER(C.c_double)),
         ("reverse_upper", C.POINTER(C.c_double)),
         ("reverse_lower", C.POINTER(C.c_double)),
+        ("node_coordinates", C.POINTER(C.c_double)),
     ]
 
 
@@ -114,6 +118,11 @@ SIGNATURES = {
     "trixi_lgl_basis": (C.c_int, [_I, _I, C.POINTER(C.c_double), _I64]),
     "trixi_synchronize": (C.c_int, [_VP, _VP]),
     "trixi_probe_fma_peak": (C.c_int, [_I, _I, C.POINTER(C.c_double), _VP]),
+    "trixi_compute_coefficients": (C.c_int, [_VP, _I, C.POINTER(C.c_double), _I64, _D, _DP, _VP]),
+    "trixi_max_dt": (C.c_int, [_VP, _DP, _DP, _VP]),
+    "trixi_integrate": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _VP]),
+    "trixi_calc_error_norms": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _D,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double), _VP]),
     "trixi_probe_convert": (C.c_int, [_VP, _VP, _VP, _VP, _I64, _VP]),
 }
 

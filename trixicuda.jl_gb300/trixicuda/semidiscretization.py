@@ -91,6 +91,7 @@ def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver:
         mo_nid=np.ascontiguousarray(cont.mortar_neighbor_ids, dtype=np.int64),
         mo_ls=np.ascontiguousarray(cont.mortar_large_sides, dtype=np.int64),
         mo_ori=np.ascontiguousarray(cont.mortar_orientations, dtype=np.int64),
+        coords=np.ascontiguousarray(cont.node_coordinates, dtype=np.float64),
     )
     d.nelements = cont.nelements
     d.inverse_jacobian = _ptr_d(keep["inverse_jacobian"])
@@ -102,6 +103,7 @@ def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver:
     d.mortar_neighbor_ids = _ptr_i(keep["mo_nid"])
     d.mortar_large_sides = _ptr_i(keep["mo_ls"])
     d.mortar_orientations = _ptr_i(keep["mo_ori"])
+    d.node_coordinates = _ptr_d(keep["coords"])
     return d, keep, cont
 
 
@@ -319,6 +321,75 @@ def rk_steps(u, k, t, dt, nsteps, semi, stream=None):
     _check_state(semi, u, k)
     _call(semi, semi._lib.trixi_rk_steps, C.c_void_p(u.data_ptr()), C.c_void_p(k.data_ptr()), float(t),
           float(dt), int(nsteps), stream=stream)
+
+
+# -- analysis, time step and initial conditions on the GPU (reference callbacks) ----
+_IC_KINDS = {"constant": _lib.IC_CONSTANT, "convergence_test": _lib.IC_CONVERGENCE_TEST,
+             "weak_blast_wave": _lib.IC_WEAK_BLAST_WAVE}
+
+
+def _ic_args(kind, params):
+    code = _IC_KINDS[kind] if isinstance(kind, str) else int(kind)
+    if params is None:
+        return code, None, 0, None
+    arr = np.ascontiguousarray(params, dtype=np.float64)
+    return code, arr.ctypes.data_as(C.POINTER(C.c_double)), arr.size, arr
+
+
+def compute_coefficients_gpu(semi, kind, t=0.0, params=None, out=None, stream=None):
+    """u0 = initial condition evaluated on the GPU (reference compute_coefficients_gpu,
+    src/semidiscretization/semidiscretization.jl:4-20, dg.jl:46-160)."""
+    torch = _torch()
+    u = out if out is not None else torch.empty(semi.u_shape(), dtype=torch.float64, device=semi.device)
+    code, ptr, n, keep = _ic_args(kind, params)
+    _call(semi, semi._lib.trixi_compute_coefficients, code, ptr, n, float(t), C.c_void_p(u.data_ptr()),
+          stream=stream)
+    return u
+
+
+def max_dt(u, semi, stream=None) -> float:
+    """2 / (N max_e J^{-1} sum_d max lambda_d) on the GPU (reference max_dt,
+    src/callbacks_step/stepsize_dg_2d.jl:21-45); multiply by the CFL number."""
+    torch = _torch()
+    _check_state(semi, u)
+    dt = torch.empty(1, dtype=torch.float64, device=semi.device)
+    _call(semi, semi._lib.trixi_max_dt, C.c_void_p(u.data_ptr()), C.c_void_p(dt.data_ptr()), stream=stream)
+    return float(dt.item())
+
+
+def integrate(u, semi, which="state", du=None, stream=None) -> np.ndarray:
+    """sum_e J_e sum_nodes w q (reference integrate_via_indices,
+    src/callbacks_step/analysis_dg_2d.jl:1-40, without the volume normalisation)."""
+    codes = {"state": _lib.INTEGRAL_STATE, "entropy": _lib.INTEGRAL_ENTROPY,
+             "entropy_production": _lib.INTEGRAL_ENTROPY_PRODUCTION, "du": _lib.INTEGRAL_DU}
+    _check_state(semi, u)
+    if du is not None:
+        _check_state(semi, du)
+    out = np.zeros(8)
+    _lib.check(semi._lib.trixi_integrate(semi._handle, C.c_void_p(u.data_ptr()),
+                                         C.c_void_p(du.data_ptr()) if du is not None else None, codes[which],
+                                         out.ctypes.data_as(C.POINTER(C.c_double)), out.size,
+                                         _stream_handle(stream)), semi._handle)
+    n = semi.equations.nvariables if which in ("state", "du") else 1
+    return out[:n].copy()
+
+
+def calc_error_norms(u, semi, t=0.0, kind="convergence_test", params=None, u_ref=None, stream=None):
+    """(L2, Linf) per variable on 2*polydeg+1 analysis nodes (reference
+    calc_error_norms, src/callbacks_step/analysis_dg_2d.jl:44-89) against an
+    analytic initial condition or a second state `u_ref`."""
+    _check_state(semi, u)
+    if u_ref is not None:
+        _check_state(semi, u_ref)
+    code, ptr, n, keep = _ic_args(kind, params)
+    nv = semi.equations.nvariables
+    l2 = np.zeros(nv)
+    linf = np.zeros(nv)
+    _lib.check(semi._lib.trixi_calc_error_norms(
+        semi._handle, C.c_void_p(u.data_ptr()), C.c_void_p(u_ref.data_ptr()) if u_ref is not None else None, code,
+        ptr, n, float(t), l2.ctypes.data_as(C.POINTER(C.c_double)), linf.ctypes.data_as(C.POINTER(C.c_double)),
+        _stream_handle(stream)), semi._handle)
+    return l2, linf
 
 
 def synchronize(semi, stream=None):
