@@ -165,6 +165,46 @@ def time_gpu_path(precision, steps, warmup, device, flush):
     return step_ms, launch_ms, semi, bufs[cur], dt
 
 
+def batched_path(precision, steps, warmup, device, flush, n=512):
+    """The 512-instance ensemble: one CK2N54 step of every instance per
+    replay of the captured CUDA graph."""
+    import torch
+
+    from trixicuda.batch import BatchedSemidiscretizationGPU, make_ensemble
+
+    t0 = time.perf_counter()
+    problems = make_ensemble(n=n, device=device)
+    batch = BatchedSemidiscretizationGPU(problems, precision=precision, device=device)
+    u = batch.compute_coefficients()
+    dts = batch.stable_dt(u)
+    k = torch.zeros_like(u)
+    setup_s = time.perf_counter() - t0
+    for _ in range(warmup):
+        batch.rk_steps(u, k, dts, 1, use_graph=True)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        batch.rk_steps(u, k, dts, 1, use_graph=True)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    dofs = batch.ndofs()
+    nvals = batch.total_values
+    # per step: 5 stages x (read u, k; write u, k) - stage 1 reads no k - plus
+    # the copy back of the odd ping-pong (read + write)
+    step_bytes = nvals * 8 * (3 + 4 * 4) + nvals * 8 * 2
+    mean_ms = statistics.mean(ms)
+    return {"instances": n, "groups": batch.ngroups, "dofs": dofs, "values": nvals,
+            "state_mb_fp64": nvals * 8 / 1e6, "ms_per_step": mean_ms,
+            "dof_updates_per_s": 5 * dofs / (mean_ms * 1e-3),
+            "instance_steps_per_s": n / (mean_ms * 1e-3),
+            "achieved_gbs": step_bytes / (mean_ms * 1e-3) / 1e9, "setup_s": setup_s,
+            "graph": "one CUDA graph per step (all groups, all stages)"}
+
+
 def e2e_path(precision, steps, warmup, device):
     """The public API call with host buffers: H2D(u) -> rk_steps(1 step) -> D2H(u)."""
     import torch
@@ -265,7 +305,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "batched-mixed", "batched-fp64"], default=None,
                     help="run only the device-timed loop of one precision (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -299,6 +340,10 @@ def main():
     T._lib.check(lib.trixi_probe_fma_peak(0, 4096, C.byref(fp64_peak), None))
     T._lib.check(lib.trixi_probe_fma_peak(1, 16384, C.byref(fp32_peak), None))
 
+    if args.profile and args.profile.startswith("batched"):
+        r = batched_path(args.profile.split("-")[1], args.steps, args.warmup, device, flush)
+        print(json.dumps({"profile": args.profile, **r}))
+        return 0
     if args.profile:
         step_ms, launch_ms, semi, _, _ = time_gpu_path(args.profile, args.steps, args.warmup, device, flush)
         print(json.dumps({"profile": args.profile, "ms_per_step": statistics.mean(step_ms),
@@ -333,6 +378,11 @@ def main():
     # equal-L2 check: 100 steps of mixed vs FP64 from the same state
     l2 = l2_mixed_vs_fp64(semi, semi64, dt, nsteps=100)
     e2e_ms, nbytes, _ = e2e_path("mixed", max(3, args.steps // 2), 3, device)
+    batched = None
+    if not args.no_batched:
+        batched = {p: batched_path(p, max(3, args.steps // 4), 3, device, flush) for p in ("mixed", "fp64")}
+        for r in batched.values():
+            r["hbm_frac"] = r["achieved_gbs"] / hbm_peak
     cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline()
     traffic = None
     prof = ROOT / "profiles" / "traffic_fused_rk_stage_euler2d_l7.json"
@@ -355,6 +405,7 @@ def main():
         "equal_l2": l2,
         "e2e": {"value": per_step_updates / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes, "api": "trixicuda.rk_steps (C ABI trixi_rk_steps)"},
+        "batched": batched,
         "cpu_baseline": cpu,
         "gpu_launches": 5 * args.steps,
         "clocks": clocks,

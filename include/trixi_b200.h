@@ -257,6 +257,30 @@ int trixi_probe_fma_peak(int precision, int iters, double *flops_per_s, void *st
 int trixi_probe_convert(const double *in_d, float *out_f, const float *in_f, double *out_d, int64_t n,
                         void *stream);
 
+/* ---- Batched ensembles (no counterpart in the reference, which solves one
+ * problem at a time) --------------------------------------------------------
+ * Hundreds of independent instances (mixed ndims, polydeg, equations, meshes,
+ * mortars) advanced together.  Instances with the same kernel kind are merged
+ * into one group whose elements are concatenated (connectivity offset), so a
+ * group is served by one fused launch per RK stage; a full RK step of all
+ * groups is captured as a CUDA graph.  All instances share one precision.
+ * The batch state is one device buffer: instance i occupies
+ * [value_offsets[i], value_offsets[i] + nvalues[i]) in its own reference
+ * layout [nvars, N, .., nelements_i]; instances are ordered by group. */
+typedef struct trixi_batch trixi_batch;
+int trixi_batch_create(const trixi_problem_desc *const *descs, int64_t n, trixi_batch **out);
+int trixi_batch_destroy(trixi_batch *b);
+int trixi_batch_layout(const trixi_batch *b, int64_t *value_offsets, int64_t *nvalues, int64_t *total_values,
+                       int64_t *ngroups);
+int trixi_batch_rhs(trixi_batch *b, double *du, const double *u, void *stream);
+/* nsteps CarpenterKennedy2N54 steps; instance i uses dt_per_instance[i] (host
+ * array).  use_graph != 0 replays a captured CUDA graph of the whole step. */
+int trixi_batch_rk_steps(trixi_batch *b, double *u, double *k, const double *dt_per_instance, int64_t nsteps,
+                         int use_graph, void *stream);
+/* The merged handle of one group (for the stage API and analysis calls). */
+int trixi_batch_handle(trixi_batch *b, int64_t group, trixi_handle **h);
+int trixi_batch_last_error(const trixi_batch *b, char *buf, size_t len);
+
 /* Waits for the handle's stream work, then checks the device error word. */
 int trixi_synchronize(trixi_handle *h, void *stream);
 

@@ -39,6 +39,7 @@ struct FusedParams {
   const double *__restrict__ mortar_flux;   // [slot][NF][NV]
   const double *__restrict__ inv_jac;       // [E]
   const double *__restrict__ alpha;         // [E] (shock capturing)
+  const double *__restrict__ dt_elem;       // [E] per-element time step (batched ensembles) or null
   int *err;                                 // device error word
   int64_t nelements;
   int epb;                                  // elements per block
@@ -259,7 +260,8 @@ struct FusedKernel {
         s.alpha[el] = (fabs(a) <= p.atol) ? R(0) : from_double<R>(a);
       }
       // per-element factor of the node phase: -J^{-1} (rhs) or -J^{-1} dt (RK)
-      const double f = -p.inv_jac[e0 + el] * (mode == MODE_RK ? p.dt : 1.0);
+      const double dte = p.dt_elem ? p.dt_elem[e0 + el] : p.dt;
+      const double f = -p.inv_jac[e0 + el] * (mode == MODE_RK ? dte : 1.0);
       s.scale[el] = from_double<R>(f);
     }
     for (int q = threadIdx.x; q < N * N; q += BLOCK) {
@@ -407,13 +409,14 @@ struct FusedKernel {
         for (int v = 0; v < NV; ++v) p.out[g0 + v] = to_double(acc[v]);
       } else if constexpr (sizeof(R) == sizeof(double)) {
         const double sc = -p.inv_jac[e0 + el];
+        const double dte = p.dt_elem ? p.dt_elem[e0 + el] : p.dt;
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
           const double du = double(acc[v]) * sc;
           if (mode == MODE_RHS) {
             p.out[g0 + v] = du;
           } else {
-            const double kk = (use_k ? p.rk_a * p.k[g0 + v] : 0.0) + p.dt * du;
+            const double kk = (use_k ? p.rk_a * p.k[g0 + v] : 0.0) + dte * du;
             p.k[g0 + v] = kk;
             p.out[g0 + v] = p.u_in[g0 + v] + p.rk_b * kk;
           }

@@ -18,6 +18,7 @@ struct FusedHost {
   const double *mortar_flux = nullptr;
   const double *inv_jac = nullptr;
   const double *alpha = nullptr;
+  const double *dt_elem = nullptr;
   int *err = nullptr;
   int64_t nelements = 0;
   int mode = 1;

@@ -20,6 +20,7 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   p.mortar_flux = h.mortar_flux;
   p.inv_jac = h.inv_jac;
   p.alpha = h.alpha;
+  p.dt_elem = h.dt_elem;
   p.err = h.err;
   p.nelements = h.nelements;
   p.mode = h.mode;

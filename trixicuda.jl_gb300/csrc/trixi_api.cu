@@ -8,6 +8,7 @@
 // across the ABI.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstdarg>
@@ -865,6 +866,316 @@ int trixi_calc_error_norms(trixi_handle *h, const double *u, const double *u_ref
   for (int v = 0; v < h->nv; ++v) {
     l2_host[v] = std::sqrt(buf[v] / vol);
     linf_host[v] = buf[8 + v];
+  }
+  return TRIXI_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched ensembles: many independent instances advanced together.
+//
+// Instances with the same kernel kind (ndims, polydeg, equation, volume
+// integral and fluxes) are merged into one group: their elements are
+// concatenated and their connectivity offset, so that a group is one mesh
+// with disconnected components and is served by a single fused launch per
+// RK stage, whatever the number of instances in it.  Each element carries
+// the time step of its instance.  A whole CarpenterKennedy2N54 step (all
+// groups, all stages, mortar kernels included) is captured once as a CUDA
+// graph and replayed.
+// ===========================================================================
+
+struct trixi_batch {
+  struct Group {
+    trixi_handle *h = nullptr;
+    int64_t value_offset = 0;  // offset of the group's first value in the batch state
+    int64_t nvalues = 0;
+    std::vector<int64_t> instances;
+    double *d_dt = nullptr;    // [group elements]
+  };
+  std::vector<Group> groups;
+  std::vector<int64_t> inst_group, inst_offset, inst_nvalues, inst_nelem;
+  int64_t total_values = 0;
+  std::vector<double> last_dt;
+  double *d_scratch = nullptr;
+  // graphs of one full step: [0] from the caller's u, [1] from the scratch buffer
+  cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+  const double *graph_u = nullptr;
+  const double *graph_k = nullptr;
+  std::string last_error;
+};
+
+namespace {
+
+int batch_fail(trixi_batch *b, int status, const std::string &msg) {
+  g_last_error = msg;
+  g_last_status = status;
+  if (b) b->last_error = msg;
+  return status;
+}
+
+struct KindKey {
+  int32_t ndims, polydeg, eq, vol, vflux, sflux, fvflux, precision;
+  double gamma, a0, a1, a2, amax, amin;
+  int32_t smooth;
+  bool operator==(const KindKey &o) const {
+    return ndims == o.ndims && polydeg == o.polydeg && eq == o.eq && vol == o.vol && vflux == o.vflux &&
+           sflux == o.sflux && fvflux == o.fvflux && precision == o.precision && gamma == o.gamma && a0 == o.a0 &&
+           a1 == o.a1 && a2 == o.a2 && amax == o.amax && amin == o.amin && smooth == o.smooth;
+  }
+};
+
+KindKey key_of(const trixi_problem_desc *d) {
+  return KindKey{d->ndims, d->polydeg, d->equation, d->volume_integral, d->volume_flux, d->surface_flux,
+                 d->volume_flux_fv, d->precision, d->gamma, d->advection_velocity[0], d->advection_velocity[1],
+                 d->advection_velocity[2], d->alpha_max, d->alpha_min, d->alpha_smooth};
+}
+
+void destroy_graphs(trixi_batch *b) {
+  for (auto &g : b->step_graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  b->graph_u = b->graph_k = nullptr;
+}
+
+// one full CK2N54 step of every group from `from` to `to` (5 stages ping-pong)
+int batch_step(trixi_batch *b, double *from, double *to, double *k, cudaStream_t s) {
+  double *cur = from, *nxt = to;
+  for (int st = 0; st < 5; ++st) {
+    for (auto &g : b->groups) {
+      FusedHost save = g.h->fused;
+      g.h->fused.dt_elem = g.d_dt;
+      int r = run_rhs(g.h, MODE_RK, cur + g.value_offset, nxt + g.value_offset, k + g.value_offset, kCK_A[st],
+                      kCK_B[st], 0.0, s);
+      g.h->fused = save;
+      if (r) return batch_fail(b, r, g.h->last_error);
+    }
+    std::swap(cur, nxt);
+  }
+  return TRIXI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int trixi_batch_create(const trixi_problem_desc *const *descs, int64_t n, trixi_batch **out) {
+  if (!out || !descs || n <= 0) return batch_fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "batch: bad arguments");
+  *out = nullptr;
+  trixi_batch *b = new trixi_batch();
+  std::vector<KindKey> keys;
+  std::vector<std::vector<int64_t>> members;
+  for (int64_t i = 0; i < n; ++i) {
+    const trixi_problem_desc *d = descs[i];
+    if (!d || d->struct_size != (int32_t)sizeof(trixi_problem_desc)) {
+      delete b;
+      return batch_fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "batch: instance " + std::to_string(i) + " descriptor");
+    }
+    const KindKey k = key_of(d);
+    size_t gi = 0;
+    while (gi < keys.size() && !(keys[gi] == k)) ++gi;
+    if (gi == keys.size()) {
+      keys.push_back(k);
+      members.emplace_back();
+    }
+    members[gi].push_back(i);
+  }
+  if (keys.size() > 1)
+    for (size_t gi = 1; gi < keys.size(); ++gi)
+      if (keys[gi].precision != keys[0].precision) {
+        delete b;
+        return batch_fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "batch: mixed precisions in one batch");
+      }
+  b->inst_group.assign(n, 0);
+  b->inst_offset.assign(n, 0);
+  b->inst_nvalues.assign(n, 0);
+  b->inst_nelem.assign(n, 0);
+  int64_t offset = 0;
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    const trixi_problem_desc *d0 = descs[members[gi][0]];
+    const int nc = 1 << (d0->ndims - 1);
+    int64_t nn = 1;
+    for (int dd = 0; dd < d0->ndims; ++dd) nn *= d0->polydeg + 1;
+    std::vector<double> inv_jac, coords;
+    std::vector<int64_t> if_nid, if_ori, mo_nid, mo_ls, mo_ori;
+    int64_t E = 0;
+    bool have_coords = true;
+    for (int64_t i : members[gi]) {
+      const trixi_problem_desc *d = descs[i];
+      if (d->nboundaries != 0 || !d->inverse_jacobian) {
+        for (auto &g : b->groups) trixi_destroy(g.h);
+        delete b;
+        return batch_fail(nullptr, TRIXI_ERR_UNSUPPORTED, "batch: instance " + std::to_string(i));
+      }
+      b->inst_group[i] = (int64_t)gi;
+      b->inst_nelem[i] = d->nelements;
+      b->inst_nvalues[i] = d->nelements * nn * d->nvars;
+      b->inst_offset[i] = offset + E * nn * d->nvars;
+      inv_jac.insert(inv_jac.end(), d->inverse_jacobian, d->inverse_jacobian + d->nelements);
+      if (d->node_coordinates)
+        coords.insert(coords.end(), d->node_coordinates, d->node_coordinates + d->ndims * nn * d->nelements);
+      else
+        have_coords = false;
+      for (int64_t k = 0; k < 2 * d->ninterfaces; ++k) if_nid.push_back(d->interface_neighbor_ids[k] + E);
+      if_ori.insert(if_ori.end(), d->interface_orientations, d->interface_orientations + d->ninterfaces);
+      for (int64_t k = 0; k < (nc + 1) * d->nmortars; ++k) mo_nid.push_back(d->mortar_neighbor_ids[k] + E);
+      if (d->nmortars) {
+        mo_ls.insert(mo_ls.end(), d->mortar_large_sides, d->mortar_large_sides + d->nmortars);
+        mo_ori.insert(mo_ori.end(), d->mortar_orientations, d->mortar_orientations + d->nmortars);
+      }
+      E += d->nelements;
+    }
+    trixi_problem_desc md = *d0;
+    md.nelements = E;
+    md.inverse_jacobian = inv_jac.data();
+    md.ninterfaces = (int64_t)if_ori.size();
+    md.interface_neighbor_ids = if_nid.data();
+    md.interface_orientations = if_ori.data();
+    md.nmortars = (int64_t)mo_ori.size();
+    md.mortar_neighbor_ids = mo_nid.empty() ? nullptr : mo_nid.data();
+    md.mortar_large_sides = mo_ls.empty() ? nullptr : mo_ls.data();
+    md.mortar_orientations = mo_ori.empty() ? nullptr : mo_ori.data();
+    md.node_coordinates = have_coords ? coords.data() : nullptr;
+    md.weights = md.derivative_split = md.derivative_dhat = md.inverse_vandermonde_legendre = nullptr;
+    md.forward_upper = md.forward_lower = md.reverse_upper = md.reverse_lower = nullptr;
+    trixi_batch::Group g;
+    int st = trixi_create(&md, &g.h);
+    if (st) {
+      std::string msg = "batch group " + std::to_string(gi) + ": " + g_last_error;
+      for (auto &gg : b->groups) trixi_destroy(gg.h);
+      delete b;
+      return batch_fail(nullptr, st, msg);
+    }
+    g.value_offset = offset;
+    g.nvalues = E * nn * d0->nvars;
+    g.instances = members[gi];
+    if (cudaMalloc(&g.d_dt, sizeof(double) * (size_t)E) != cudaSuccess) {
+      trixi_destroy(g.h);
+      for (auto &gg : b->groups) trixi_destroy(gg.h);
+      delete b;
+      return batch_fail(nullptr, TRIXI_ERR_OUT_OF_MEMORY, "batch: dt buffer");
+    }
+    offset += g.nvalues;
+    b->groups.push_back(g);
+  }
+  b->total_values = offset;
+  *out = b;
+  return TRIXI_OK;
+}
+
+int trixi_batch_destroy(trixi_batch *b) {
+  if (!b) return TRIXI_OK;
+  destroy_graphs(b);
+  for (auto &g : b->groups) {
+    if (g.d_dt) cudaFree(g.d_dt);
+    trixi_destroy(g.h);
+  }
+  if (b->d_scratch) cudaFree(b->d_scratch);
+  delete b;
+  return TRIXI_OK;
+}
+
+int trixi_batch_layout(const trixi_batch *b, int64_t *value_offsets, int64_t *nvalues, int64_t *total_values,
+                       int64_t *ngroups) {
+  if (!b) return batch_fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "batch is null");
+  const size_t n = b->inst_offset.size();
+  for (size_t i = 0; i < n; ++i) {
+    if (value_offsets) value_offsets[i] = b->inst_offset[i];
+    if (nvalues) nvalues[i] = b->inst_nvalues[i];
+  }
+  if (total_values) *total_values = b->total_values;
+  if (ngroups) *ngroups = (int64_t)b->groups.size();
+  return TRIXI_OK;
+}
+
+int trixi_batch_rhs(trixi_batch *b, double *du, const double *u, void *stream) {
+  if (!b) return batch_fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "batch is null");
+  if (!aligned8(du) || !aligned8(u) || du == u) return batch_fail(b, TRIXI_ERR_INVALID_ARGUMENT, "batch rhs pointers");
+  for (auto &g : b->groups) {
+    int r = run_rhs(g.h, MODE_RHS, u + g.value_offset, du + g.value_offset, nullptr, 0, 0, 0, (cudaStream_t)stream);
+    if (r) return batch_fail(b, r, g.h->last_error);
+  }
+  return TRIXI_OK;
+}
+
+int trixi_batch_rk_steps(trixi_batch *b, double *u, double *k, const double *dt_per_instance, int64_t nsteps,
+                         int use_graph, void *stream) {
+  if (!b) return batch_fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "batch is null");
+  if (!aligned8(u) || !aligned8(k) || !dt_per_instance || nsteps < 0)
+    return batch_fail(b, TRIXI_ERR_INVALID_ARGUMENT, "batch rk arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t ninst = b->inst_offset.size();
+  if (b->last_dt.size() != ninst || !std::equal(b->last_dt.begin(), b->last_dt.end(), dt_per_instance)) {
+    for (size_t i = 0; i < ninst; ++i)
+      if (!std::isfinite(dt_per_instance[i])) return batch_fail(b, TRIXI_ERR_INVALID_ARGUMENT, "batch dt");
+    for (auto &g : b->groups) {
+      std::vector<double> dt;
+      for (int64_t i : g.instances) dt.insert(dt.end(), (size_t)b->inst_nelem[i], dt_per_instance[i]);
+      cudaError_t e = cudaMemcpy(g.d_dt, dt.data(), sizeof(double) * dt.size(), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    }
+    b->last_dt.assign(dt_per_instance, dt_per_instance + ninst);
+  }
+  if (nsteps == 0) return TRIXI_OK;
+  if (!b->d_scratch) {
+    cudaError_t e = cudaMalloc(&b->d_scratch, sizeof(double) * (size_t)b->total_values);
+    if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_OUT_OF_MEMORY, "batch scratch");
+  }
+  double *bufs[2] = {u, b->d_scratch};
+  if (use_graph && (b->graph_u != u || b->graph_k != k || !b->step_graph[0])) {
+    destroy_graphs(b);
+    for (int parity = 0; parity < 2; ++parity) {
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+      int r = batch_step(b, bufs[parity], bufs[1 - parity], k, s);
+      e = cudaStreamEndCapture(s, &graph);
+      if (r) {
+        if (graph) cudaGraphDestroy(graph);
+        return r;
+      }
+      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&b->step_graph[parity], graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    }
+    b->graph_u = u;
+    b->graph_k = k;
+  }
+  int cur = 0;
+  for (int64_t st = 0; st < nsteps; ++st) {
+    if (use_graph) {
+      cudaError_t e = cudaGraphLaunch(b->step_graph[cur], s);
+      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    } else {
+      int r = batch_step(b, bufs[cur], bufs[1 - cur], k, s);
+      if (r) return r;
+    }
+    cur = 1 - cur;
+  }
+  if (cur == 1) {
+    cudaError_t e = cudaMemcpyAsync(u, b->d_scratch, sizeof(double) * (size_t)b->total_values,
+                                    cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return TRIXI_OK;
+}
+
+int trixi_batch_handle(trixi_batch *b, int64_t group, trixi_handle **h) {
+  if (!b || !h || group < 0 || group >= (int64_t)b->groups.size())
+    return batch_fail(b, TRIXI_ERR_INVALID_ARGUMENT, "batch group");
+  *h = b->groups[(size_t)group].h;
+  return TRIXI_OK;
+}
+
+int trixi_batch_last_error(const trixi_batch *b, char *buf, size_t len) {
+  const std::string &msg = b ? b->last_error : g_last_error;
+  if (buf && len > 0) {
+    size_t m = std::min(len - 1, msg.size());
+    std::memcpy(buf, msg.data(), m);
+    buf[m] = '\0';
   }
   return TRIXI_OK;
 }

@@ -120,6 +120,14 @@ SIGNATURES = {
     "trixi_probe_fma_peak": (C.c_int, [_I, _I, C.POINTER(C.c_double), _VP]),
     "trixi_compute_coefficients": (C.c_int, [_VP, _I, C.POINTER(C.c_double), _I64, _D, _DP, _VP]),
     "trixi_max_dt": (C.c_int, [_VP, _DP, _DP, _VP]),
+    "trixi_batch_create": (C.c_int, [C.POINTER(C.POINTER(ProblemDesc)), _I64, C.POINTER(C.c_void_p)]),
+    "trixi_batch_destroy": (C.c_int, [_VP]),
+    "trixi_batch_layout": (C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                     C.POINTER(C.c_int64)]),
+    "trixi_batch_rhs": (C.c_int, [_VP, _DP, _DP, _VP]),
+    "trixi_batch_rk_steps": (C.c_int, [_VP, _DP, _DP, C.POINTER(C.c_double), _I64, _I, _VP]),
+    "trixi_batch_handle": (C.c_int, [_VP, _I64, C.POINTER(C.c_void_p)]),
+    "trixi_batch_last_error": (C.c_int, [_VP, C.c_char_p, C.c_size_t]),
     "trixi_integrate": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _VP]),
     "trixi_calc_error_norms": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _D,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double), _VP]),
