@@ -281,6 +281,30 @@ int trixi_batch_rk_steps(trixi_batch *b, double *u, double *k, const double *dt_
 int trixi_batch_handle(trixi_batch *b, int64_t group, trixi_handle **h);
 int trixi_batch_last_error(const trixi_batch *b, char *buf, size_t len);
 
+/* ---- Discrete adjoint (no counterpart in the reference) --------------------
+ * FP64; Euler flux differencing with flux_ranocha / flux_central and linear
+ * advection, on conforming periodic meshes. */
+
+/* ubar = J_rhs(u)^T lambda (device arrays in the state layout). */
+int trixi_rhs_vjp(trixi_handle *h, double *ubar, const double *u, const double *lambda, void *stream);
+
+/* J = 1/2 * sum_e J_e sum_nodes w (rho - rho_target)^2 (host scalar) and, if
+ * ubar != NULL, its gradient with respect to the state (device).  rho_target
+ * holds one value per node [N^ndims, nelements]. */
+int trixi_objective_density_l2(trixi_handle *h, const double *u, const double *rho_target, double *J_host,
+                               double *ubar, void *stream);
+
+/* Forward sweep of nsteps CarpenterKennedy2N54 steps of size dt from u0,
+ * storing up to nsnapshots checkpoints (binomial schedule); writes u(T).
+ * nsnapshots >= nsteps - 1 stores every step (no recomputation). */
+int trixi_adjoint_forward(trixi_handle *h, const double *u0, double dt, int64_t nsteps, int64_t nsnapshots,
+                          double *uT, void *stream);
+
+/* Backward sweep: given dJ/du(T) returns dJ/du0, recomputing states from the
+ * checkpoints.  *forward_steps = RK steps recomputed (0 when all were stored). */
+int trixi_adjoint_backward(trixi_handle *h, const double *uT_bar, double *u0_bar, int64_t *forward_steps,
+                           void *stream);
+
 /* Waits for the handle's stream work, then checks the device error word. */
 int trixi_synchronize(trixi_handle *h, void *stream);
 

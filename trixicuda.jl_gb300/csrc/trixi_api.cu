@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <map>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -19,6 +20,7 @@
 
 #include "../../include/trixi_b200.h"
 #include "basis.h"
+#include "dg_adjoint.h"
 #include "dg_analysis.h"
 #include "dg_host.h"
 
@@ -39,6 +41,19 @@ const double kCK_B[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13
                          2277821191437.0 / 14882151754819.0};
 
 }  // namespace
+
+struct AdjointState {
+  int64_t n = 0, snapshots = 0;
+  double dt = 0.0;
+  bool forward_done = false;
+  int64_t fwd_steps = 0;
+  double *u0 = nullptr, *ktmp = nullptr, *tmp = nullptr;
+  double *stage[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  double *lu[2] = {nullptr, nullptr}, *lk[2] = {nullptr, nullptr};
+  std::vector<double *> pool;           // free snapshot buffers
+  std::map<int64_t, double *> ckpt;     // step -> stored state
+  std::vector<double *> all;            // every allocation, for cleanup
+};
 
 struct trixi_handle {
   int device = 0;
@@ -70,6 +85,7 @@ struct trixi_handle {
   double *d_vdm = nullptr, *d_wa = nullptr, *d_w = nullptr;
   std::vector<double> xa;
   double total_volume = 0.0;
+  struct AdjointState *adj = nullptr;
   FusedHost fused;
   std::string last_error;
   int last_status = TRIXI_OK;
@@ -117,7 +133,15 @@ cudaError_t upload(T **dst, const T *src, size_t n) {
   return cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
 }
 
+void free_adjoint(trixi_handle *h) {
+  if (!h->adj) return;
+  for (double *p : h->adj->all) cudaFree(p);
+  delete h->adj;
+  h->adj = nullptr;
+}
+
 void free_all(trixi_handle *h) {
+  free_adjoint(h);
   void *ptrs[] = {h->d_face_table, h->d_slot_nbrs, h->d_inv_jac, h->d_if_nid, h->d_if_ori, h->d_mo_nid,
                   h->d_mo_ls, h->d_mo_ori, h->d_mortar_flux, h->d_alpha_raw, h->d_alpha, h->d_err,
                   h->d_scratch_u, h->d_interfaces_u, h->d_sfv, h->d_mortar_u[0], h->d_mortar_u[1],
@@ -900,6 +924,7 @@ struct trixi_batch {
   double *d_scratch = nullptr;
   // graphs of one full step: [0] from the caller's u, [1] from the scratch buffer
   cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+  cudaStream_t capture_stream = nullptr;  // graphs are recorded here (the caller's stream may be the legacy one)
   const double *graph_u = nullptr;
   const double *graph_k = nullptr;
   std::string last_error;
@@ -1073,6 +1098,7 @@ int trixi_batch_destroy(trixi_batch *b) {
     trixi_destroy(g.h);
   }
   if (b->d_scratch) cudaFree(b->d_scratch);
+  if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
   delete b;
   return TRIXI_OK;
 }
@@ -1126,12 +1152,33 @@ int trixi_batch_rk_steps(trixi_batch *b, double *u, double *k, const double *dt_
   double *bufs[2] = {u, b->d_scratch};
   if (use_graph && (b->graph_u != u || b->graph_k != k || !b->step_graph[0])) {
     destroy_graphs(b);
+    if (!b->capture_stream) {
+      cudaError_t e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    }
+    // one eager step outside capture makes every lazy initialisation (kernel
+    // attributes, mortar buffers) happen before recording; it writes only the
+    // scratch buffer and k, whose value at the start of a step is never read
+    // (the first stage has A_1 = 0), so the caller's state is untouched
+    {
+      cudaEvent_t ready;
+      cudaError_t e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(ready, s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->capture_stream, ready, 0);
+      cudaEventDestroy(ready);
+      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+      int r = batch_step(b, bufs[0], bufs[1], k, b->capture_stream);
+      if (r) return r;
+      e = cudaStreamSynchronize(b->capture_stream);
+      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    }
     for (int parity = 0; parity < 2; ++parity) {
       cudaGraph_t graph = nullptr;
-      cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+      cudaStream_t cs = b->capture_stream;
+      cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
       if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
-      int r = batch_step(b, bufs[parity], bufs[1 - parity], k, s);
-      e = cudaStreamEndCapture(s, &graph);
+      int r = batch_step(b, bufs[parity], bufs[1 - parity], k, cs);
+      e = cudaStreamEndCapture(cs, &graph);
       if (r) {
         if (graph) cudaGraphDestroy(graph);
         return r;
@@ -1177,6 +1224,258 @@ int trixi_batch_last_error(const trixi_batch *b, char *buf, size_t len) {
     std::memcpy(buf, msg.data(), m);
     buf[m] = '\0';
   }
+  return TRIXI_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Discrete adjoint: VJP of the rhs, and reverse-mode CarpenterKennedy2N54 with
+// binomial checkpointing (Griewank & Walther's "revolve" schedule: with s
+// snapshots and r forward repetitions, beta(s, r) = C(s + r, s) steps can be
+// reversed).  The forward sweep stores the snapshots of the schedule's
+// rightmost branch; the backward sweep recomputes the rest.
+// ===========================================================================
+namespace {
+
+AdjointHost adjoint_host(const trixi_handle *h) {
+  AdjointHost a;
+  a.dim = h->dim;
+  a.N = h->N;
+  a.eq = h->eq;
+  a.vol = h->vol;
+  a.face_table = h->d_face_table;
+  a.inv_jac = h->d_inv_jac;
+  a.nelements = h->E;
+  a.surface_flux = h->sflux;
+  a.volume_flux = h->vflux;
+  a.gamma = h->gamma;
+  for (int i = 0; i < 3; ++i) a.adv[i] = h->adv[i];
+  for (int i = 0; i < h->N * h->N; ++i) {
+    a.dsplit[i] = h->fused.dsplit[i];
+    a.dhat[i] = h->fused.dhat[i];
+  }
+  a.lhat_l = h->fused.lhat_l;
+  a.lhat_r = h->fused.lhat_r;
+  return a;
+}
+
+int check_adjoint_supported(trixi_handle *h) {
+  if (h->mixed) return fail(h, TRIXI_ERR_UNSUPPORTED, "the adjoint runs in FP64 (precision = FP64)");
+  if (!adjoint_supported(h->dim, h->N, h->eq, h->vol, h->vflux, h->sflux, h->M > 0))
+    return fail(h, TRIXI_ERR_UNSUPPORTED,
+                "adjoint: supported are Euler flux differencing with flux_ranocha/flux_central and linear "
+                "advection, on conforming periodic meshes");
+  return TRIXI_OK;
+}
+
+double beta(int64_t s, int64_t t) {  // C(s + t, s), saturating
+  double r = 1.0;
+  for (int64_t i = 1; i <= t; ++i) {
+    r = r * (double)(s + i) / (double)i;
+    if (r > 1e18) return 1e18;
+  }
+  return r;
+}
+
+// checkpoint position for reversing steps [a, b) with s free snapshots
+int64_t split_point(int64_t a, int64_t b, int64_t s) {
+  const int64_t n = b - a;
+  if (s <= 0 || n <= 1) return -1;
+  int64_t t = 1;
+  while (beta(s, t) < (double)n) ++t;
+  const double right = beta(s - 1, t);
+  int64_t m = b - (int64_t)std::min<double>(right, (double)(n - 1));
+  return std::max<int64_t>(a + 1, std::min<int64_t>(m, b - 1));
+}
+
+size_t state_bytes(const trixi_handle *h) { return sizeof(double) * (size_t)(h->E * h->NN * h->nv); }
+
+// dst = state after `steps` RK steps from src (dst may equal src)
+int advance(trixi_handle *h, const double *src, double *dst, int64_t steps, cudaStream_t s) {
+  AdjointState *A = h->adj;
+  if (src != dst) TRIXI_CUDA(h, cudaMemcpyAsync(dst, src, state_bytes(h), cudaMemcpyDeviceToDevice, s), "copy");
+  if (steps > 0) {
+    int r = trixi_rk_steps(h, dst, A->ktmp, 0.0, A->dt, steps, s);
+    if (r) return r;
+    A->fwd_steps += steps;
+  }
+  return TRIXI_OK;
+}
+
+int adjoint_step(trixi_handle *h, const double *state, int &cur, cudaStream_t s) {
+  AdjointState *A = h->adj;
+  TRIXI_CUDA(h, cudaMemcpyAsync(A->stage[0], state, state_bytes(h), cudaMemcpyDeviceToDevice, s), "copy");
+  for (int st = 0; st < 4; ++st) {
+    int r = run_rhs(h, MODE_RK, A->stage[st], A->stage[st + 1], A->ktmp, kCK_A[st], kCK_B[st], A->dt, s);
+    if (r) return r;
+  }
+  AdjointHost a = adjoint_host(h);
+  a.dt = A->dt;
+  for (int st = 4; st >= 0; --st) {
+    a.u = A->stage[st];
+    a.lu_in = A->lu[cur];
+    a.lk_in = A->lk[cur];
+    a.lu_out = A->lu[1 - cur];
+    a.lk_out = A->lk[1 - cur];
+    a.rk_a = kCK_A[st];
+    a.rk_b = kCK_B[st];
+    TRIXI_CUDA(h, launch_adjoint(a, s), "adjoint stage");
+    cur = 1 - cur;
+  }
+  return TRIXI_OK;
+}
+
+int reverse(trixi_handle *h, int64_t a, int64_t b, int64_t s_free, const double *state_a, int &cur, cudaStream_t st) {
+  AdjointState *A = h->adj;
+  if (b - a == 1) return adjoint_step(h, state_a, cur, st);
+  const int64_t m = split_point(a, b, s_free);
+  if (m < 0) {  // no snapshot left: recompute every step from a
+    for (int64_t j = b - 1; j >= a; --j) {
+      int r = advance(h, state_a, A->tmp, j - a, st);
+      if (r) return r;
+      r = adjoint_step(h, A->tmp, cur, st);
+      if (r) return r;
+    }
+    return TRIXI_OK;
+  }
+  double *buf = nullptr;
+  auto it = A->ckpt.find(m);
+  if (it != A->ckpt.end()) {
+    buf = it->second;
+  } else {
+    if (A->pool.empty()) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "adjoint: snapshot pool exhausted");
+    buf = A->pool.back();
+    A->pool.pop_back();
+    int r = advance(h, state_a, buf, m - a, st);
+    if (r) return r;
+    A->ckpt[m] = buf;
+  }
+  int r = reverse(h, m, b, s_free - 1, buf, cur, st);
+  if (r) return r;
+  A->ckpt.erase(m);
+  A->pool.push_back(buf);
+  return reverse(h, a, m, s_free, state_a, cur, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int trixi_rhs_vjp(trixi_handle *h, double *ubar, const double *u, const double *lambda, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, ubar, "ubar")) return st;
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = check_u_args(h, lambda, "lambda")) return st;
+  if (int st = check_adjoint_supported(h)) return st;
+  AdjointHost a = adjoint_host(h);
+  a.u = u;
+  a.lu_in = nullptr;
+  a.lk_in = lambda;
+  a.lu_out = ubar;
+  a.lk_out = nullptr;
+  a.rk_a = 0.0;
+  a.rk_b = 0.0;
+  a.dt = 1.0;
+  TRIXI_CUDA(h, launch_adjoint(a, (cudaStream_t)stream), "rhs vjp");
+  return TRIXI_OK;
+}
+
+int trixi_objective_density_l2(trixi_handle *h, const double *u, const double *rho_target, double *J_host,
+                               double *ubar, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = check_u_args(h, rho_target, "rho_target")) return st;
+  if (!J_host) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "J is null");
+  if (ubar && !aligned8(ubar)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "ubar misaligned");
+  if (int st = ensure_reduction(h, 1)) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  TRIXI_CUDA(h, launch_density_objective(h->dim, h->N, h->nv, h->E, u, rho_target, h->d_inv_jac, h->d_w, ubar,
+                                         h->d_partial, h->d_red_out, s), "objective");
+  TRIXI_CUDA(h, cudaMemcpyAsync(J_host, h->d_red_out, sizeof(double), cudaMemcpyDeviceToHost, s), "copy");
+  TRIXI_CUDA(h, cudaStreamSynchronize(s), "synchronize");
+  return TRIXI_OK;
+}
+
+int trixi_adjoint_forward(trixi_handle *h, const double *u0, double dt, int64_t nsteps, int64_t nsnapshots,
+                          double *uT, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (int st = check_u_args(h, u0, "u0")) return st;
+  if (int st = check_u_args(h, uT, "uT")) return st;
+  if (int st = check_adjoint_supported(h)) return st;
+  if (nsteps <= 0 || nsnapshots < 0 || !std::isfinite(dt))
+    return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "adjoint: nsteps %lld, snapshots %lld", (long long)nsteps,
+                (long long)nsnapshots);
+  cudaStream_t s = (cudaStream_t)stream;
+  free_adjoint(h);
+  h->adj = new AdjointState();
+  AdjointState *A = h->adj;
+  A->n = nsteps;
+  A->snapshots = std::min<int64_t>(nsnapshots, nsteps - 1);
+  A->dt = dt;
+  const size_t bytes = state_bytes(h);
+  auto alloc = [&](double **p) -> int {
+    TRIXI_CUDA(h, cudaMalloc(p, bytes), "alloc adjoint buffers");
+    A->all.push_back(*p);
+    return TRIXI_OK;
+  };
+  int r = alloc(&A->u0);
+  if (!r) r = alloc(&A->ktmp);
+  if (!r) r = alloc(&A->tmp);
+  for (int i = 0; i < 5 && !r; ++i) r = alloc(&A->stage[i]);
+  for (int i = 0; i < 2 && !r; ++i) r = alloc(&A->lu[i]);
+  for (int i = 0; i < 2 && !r; ++i) r = alloc(&A->lk[i]);
+  for (int64_t i = 0; i < A->snapshots && !r; ++i) {
+    double *p = nullptr;
+    r = alloc(&p);
+    if (!r) A->pool.push_back(p);
+  }
+  if (r) {
+    free_adjoint(h);
+    return r;
+  }
+  TRIXI_CUDA(h, cudaMemcpyAsync(A->u0, u0, bytes, cudaMemcpyDeviceToDevice, s), "copy u0");
+  // forward sweep to T, storing the snapshots of the schedule's rightmost branch
+  int64_t a = 0, s_free = A->snapshots;
+  const double *from = A->u0;
+  TRIXI_CUDA(h, cudaMemcpyAsync(uT, A->u0, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+  int64_t pos = 0;
+  while (true) {
+    const int64_t m = split_point(a, nsteps, s_free);
+    if (m < 0) break;
+    double *buf = A->pool.back();
+    A->pool.pop_back();
+    r = advance(h, from, buf, m - pos, s);
+    if (r) return r;
+    A->ckpt[m] = buf;
+    from = buf;
+    pos = m;
+    a = m;
+    --s_free;
+  }
+  r = advance(h, from, uT, nsteps - pos, s);
+  if (r) return r;
+  A->forward_done = true;
+  return TRIXI_OK;
+}
+
+int trixi_adjoint_backward(trixi_handle *h, const double *uT_bar, double *u0_bar, int64_t *forward_steps,
+                           void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (!h->adj || !h->adj->forward_done) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "adjoint: run the forward sweep first");
+  if (int st = check_u_args(h, uT_bar, "uT_bar")) return st;
+  if (int st = check_u_args(h, u0_bar, "u0_bar")) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  AdjointState *A = h->adj;
+  const size_t bytes = state_bytes(h);
+  int cur = 0;
+  TRIXI_CUDA(h, cudaMemcpyAsync(A->lu[0], uT_bar, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+  TRIXI_CUDA(h, cudaMemsetAsync(A->lk[0], 0, bytes, s), "zero");
+  int r = reverse(h, 0, A->n, A->snapshots, A->u0, cur, s);
+  if (r) return r;
+  TRIXI_CUDA(h, cudaMemcpyAsync(u0_bar, A->lu[cur], bytes, cudaMemcpyDeviceToDevice, s), "copy");
+  if (forward_steps) *forward_steps = A->fwd_steps;
+  A->forward_done = false;
   return TRIXI_OK;
 }
 

@@ -120,6 +120,10 @@ SIGNATURES = {
     "trixi_probe_fma_peak": (C.c_int, [_I, _I, C.POINTER(C.c_double), _VP]),
     "trixi_compute_coefficients": (C.c_int, [_VP, _I, C.POINTER(C.c_double), _I64, _D, _DP, _VP]),
     "trixi_max_dt": (C.c_int, [_VP, _DP, _DP, _VP]),
+    "trixi_rhs_vjp": (C.c_int, [_VP, _DP, _DP, _DP, _VP]),
+    "trixi_objective_density_l2": (C.c_int, [_VP, _DP, _DP, C.POINTER(C.c_double), _DP, _VP]),
+    "trixi_adjoint_forward": (C.c_int, [_VP, _DP, _D, _I64, _I64, _DP, _VP]),
+    "trixi_adjoint_backward": (C.c_int, [_VP, _DP, _DP, C.POINTER(C.c_int64), _VP]),
     "trixi_batch_create": (C.c_int, [C.POINTER(C.POINTER(ProblemDesc)), _I64, C.POINTER(C.c_void_p)]),
     "trixi_batch_destroy": (C.c_int, [_VP]),
     "trixi_batch_layout": (C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
