@@ -205,6 +205,71 @@ def batched_path(precision, steps, warmup, device, flush, n=512):
             "graph": "one CUDA graph per step (all groups, all stages)"}
 
 
+def adjoint_path(device, nsteps=200, snapshots=15, ndirs=4):
+    """2D Euler level 6, polydeg 4 (flux_ranocha volume + surface), J = 1/2 int
+    (rho(T) - rho_target)^2 over 200 CK2N54 steps: wall time of the gradient
+    (forward sweep + backward sweep with binomial checkpoints) over one plain
+    forward solve, and agreement with central finite differences (h = 1e-6)."""
+    import torch
+
+    import trixicuda as T
+    from trixicuda import adjoint as ADJ
+
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEMGPU(polydeg=4, surface_flux=T.flux_ranocha,
+                        volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((-2.0, -2.0), (2.0, 2.0), initial_refinement_level=6)
+    ic = T.initial_condition_fourier_euler(eq, seed=20261203, kmax=8)
+    semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver)
+    u0 = semi.compute_coefficients()
+    x = semi.containers.node_coordinates.reshape(-1, 2).T
+    rt = torch.from_numpy(1.0 + 0.05 * T.equations.FourierField(2, 4, 4242, -2.0, 2.0)(x)).to(device)
+    dt = 0.5 * T.max_dt(u0, semi)
+
+    def fwd():
+        u = u0.clone()
+        k = torch.zeros_like(u)
+        T.rk_steps(u, k, 0.0, dt, nsteps, semi)
+        return u
+
+    def timed(fn, reps=2):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            out = fn()
+            b.record()
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        return best, out
+
+    fwd()  # warm-up
+    f_ms, _ = timed(fwd)
+    res = {}
+    for label, s_ in (("binomial", snapshots), ("store_all", nsteps - 1)):
+        g_ms, (J, grad, nrec) = timed(lambda: ADJ.gradient_density_l2(semi, u0, rt, dt, nsteps, s_))
+        res[label] = {"snapshots": s_, "gradient_ms": g_ms, "ratio_to_forward": g_ms / f_ms,
+                      "forward_steps_recomputed": nrec}
+    rng = np.random.default_rng(20261203)
+    errs = []
+    for _ in range(ndirs):
+        dirn = torch.from_numpy(rng.standard_normal(u0.shape)).to(device)
+        vals = []
+        for sgn in (1, -1):
+            u = (u0 + sgn * 1e-6 * dirn).contiguous()
+            k = torch.zeros_like(u)
+            T.rk_steps(u, k, 0.0, dt, nsteps, semi)
+            vals.append(ADJ.objective_density_l2(u, rt, semi, grad=False)[0])
+        fd = (vals[0] - vals[1]) / 2e-6
+        ad = float((grad * dirn).sum())
+        errs.append(abs(fd - ad) / abs(ad))
+    return {"workload": "2D Euler level 6 (4096 elements), polydeg 4, flux_ranocha, 200 CK2N54 steps, FP64",
+            "forward_ms": f_ms, "J": J, **res, "fd_directions": ndirs, "fd_h": 1e-6,
+            "fd_max_rel_err": max(errs)}
+
+
 def e2e_path(precision, steps, warmup, device):
     """The public API call with host buffers: H2D(u) -> rk_steps(1 step) -> D2H(u)."""
     import torch
@@ -306,6 +371,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "fp64", "batched-mixed", "batched-fp64"], default=None,
                     help="run only the device-timed loop of one precision (for ncu captures)")
     args = ap.parse_args()
@@ -383,6 +449,7 @@ def main():
         batched = {p: batched_path(p, max(3, args.steps // 4), 3, device, flush) for p in ("mixed", "fp64")}
         for r in batched.values():
             r["hbm_frac"] = r["achieved_gbs"] / hbm_peak
+    adjoint = None if args.no_adjoint else adjoint_path(device)
     cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline()
     traffic = None
     prof = ROOT / "profiles" / "traffic_fused_rk_stage_euler2d_l7.json"
@@ -406,6 +473,7 @@ def main():
         "e2e": {"value": per_step_updates / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes, "api": "trixicuda.rk_steps (C ABI trixi_rk_steps)"},
         "batched": batched,
+        "adjoint": adjoint,
         "cpu_baseline": cpu,
         "gpu_launches": 5 * args.steps,
         "clocks": clocks,
