@@ -20,8 +20,8 @@
 namespace trixi {
 
 // ---- derivatives of the logarithmic means (same series / branches as forward)
-__device__ __forceinline__ void ln_mean_grad(double x, double y, double &L, double &dx, double &dy) {
-  const double s = x + y, d = x - y, r = 1.0 / s, f = d * r, u = f * f;
+__device__ __forceinline__ void ln_mean_grad(double x, double y, double r, double &L, double &dx, double &dy) {
+  const double s = x + y, d = x - y, f = d * r, u = f * f;
   if (u < LnMeanThreshold<double>::value) {
     const double h = 1.0 + u * (-1.0 / 3.0 + u * (-4.0 / 45.0 + u * (-44.0 / 945.0)));
     const double hp = -1.0 / 3.0 + u * (-8.0 / 45.0 + u * (-132.0 / 945.0));
@@ -36,8 +36,8 @@ __device__ __forceinline__ void ln_mean_grad(double x, double y, double &L, doub
   }
 }
 
-__device__ __forceinline__ void inv_ln_mean_grad(double x, double y, double &Q, double &dx, double &dy) {
-  const double s = x + y, d = x - y, r = 1.0 / s, f = d * r, u = f * f;
+__device__ __forceinline__ void inv_ln_mean_grad(double x, double y, double r, double &Q, double &dx, double &dy) {
+  const double d = x - y, f = d * r, u = f * f;
   if (u < LnMeanThreshold<double>::value) {
     const double g = 1.0 + u * (1.0 / 3.0 + u * (1.0 / 5.0 + u * (1.0 / 7.0)));
     const double gp = 1.0 / 3.0 + u * (2.0 / 5.0 + u * (3.0 / 7.0));
@@ -61,9 +61,9 @@ struct Adjoint<DIM, EQ_ADV> {
   static constexpr int NV = 1;
   // cotangents of a two-point flux f(u_l, u_r) with respect to u_l and u_r
   template <int O>
-  __device__ __forceinline__ static void two_point_vjp(int kind, const double *, const double *, const double *,
-                                                      const double *, const double *g, double *ul_bar,
-                                                      double *ur_bar, const PhysParams<double> &pp) {
+  __device__ __forceinline__ static void two_point_vjp(int kind, const double *, const double *, double,
+                                                      const double *, const double *, double, const double *g,
+                                                      double *ul_bar, double *ur_bar, const PhysParams<double> &pp) {
     const double a = pp.a[O];
     if (kind == FLUX_LLF || kind == FLUX_LLF_NAIVE) {
       ul_bar[0] = 0.5 * (a + fabs(a)) * g[0];
@@ -85,9 +85,8 @@ struct Adjoint<DIM, EQ_EULER> {
   static constexpr int NV = DIM + 2;
 
   // cotangent of the primitive state (rho, v, p) -> conservative state
-  __device__ __forceinline__ static void prim_vjp(const double *w, const double *wb, double *ub,
+  __device__ __forceinline__ static void prim_vjp(const double *w, double inv_rho, const double *wb, double *ub,
                                                   const PhysParams<double> &pp) {
-    const double rho = w[0], inv_rho = 1.0 / rho;
     double kin = 0.0, vbv = 0.0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
@@ -107,9 +106,10 @@ struct Adjoint<DIM, EQ_EULER> {
                                                      double *wrb, const PhysParams<double> &pp) {
     const double rl = wl[0], rr = wr[0], pl = wl[DIM + 1], pr = wr[DIM + 1];
     double L, dLl, dLr, Q, dQx, dQy;
-    ln_mean_grad(rl, rr, L, dLl, dLr);
     const double x2 = rl * pr, y2 = rr * pl;
-    inv_ln_mean_grad(x2, y2, Q, dQx, dQy);
+    const double s1 = rl + rr, s2 = x2 + y2, qq = 1.0 / (s1 * s2);  // one division for both means
+    ln_mean_grad(rl, rr, s2 * qq, L, dLl, dLr);
+    inv_ln_mean_grad(x2, y2, s1 * qq, Q, dQx, dQy);
     const double ipm = pl * pr * Q;
     double va[DIM], v2 = 0.0;
 #pragma unroll
@@ -187,15 +187,17 @@ struct Adjoint<DIM, EQ_EULER> {
     ub[DIM + 1] = ubE;
   }
 
+  // ul/ur: conservative, wl/wr: primitive states; irl/irr: 1/rho of each state
   template <int O>
-  __device__ __forceinline__ static void two_point_vjp(int kind, const double *ul, const double *wl, const double *ur,
-                                                      const double *wr, const double *g, double *ulb, double *urb,
+  __device__ __forceinline__ static void two_point_vjp(int kind, const double *ul, const double *wl, double irl,
+                                                      const double *ur, const double *wr, double irr,
+                                                      const double *g, double *ulb, double *urb,
                                                       const PhysParams<double> &pp) {
     if (kind == FLUX_RANOCHA) {
       double wlb[NV], wrb[NV];
       ranocha_vjp<O>(wl, wr, g, wlb, wrb, pp);
-      prim_vjp(wl, wlb, ulb, pp);
-      prim_vjp(wr, wrb, urb, pp);
+      prim_vjp(wl, irl, wlb, ulb, pp);
+      prim_vjp(wr, irr, wrb, urb, pp);
     } else {  // central: 1/2 (f(u_l) + f(u_r))
       double gh[NV];
 #pragma unroll
@@ -236,7 +238,8 @@ struct AdjointKernel {
   static constexpr int BLOCK = 256;
   static constexpr int ITEMS_PER_EL = DIM * VOL_PER_DIR + 2 * DIM * NF;
   static constexpr size_t smem_for(int epb) {
-    return sizeof(double) * ((size_t)epb * (3 * NV * NN + (DIM * VOL_PER_DIR * VOL_BAR + 2 * DIM * NF) * NV) + epb);
+    return sizeof(double) * ((size_t)epb * (3 * NV * NN + NN + (DIM * VOL_PER_DIR * VOL_BAR + 2 * DIM * NF) * NV) +
+                             epb);
   }
   static constexpr int epb_pick() {
     int e = (2 * BLOCK + ITEMS_PER_EL - 1) / ITEMS_PER_EL;
@@ -256,6 +259,7 @@ struct AdjointKernel {
     double *s_vb = s_l + epb * NV * NN;                        // [el][dir][slot][VOL_BAR][v]
     double *s_sb = s_vb + epb * DIM * VOL_PER_DIR * VOL_BAR * NV;  // [el][face][t][v]
     double *s_ij = s_sb + epb * 2 * DIM * NF * NV;
+    double *s_ir = s_ij + epb;                                 // 1/rho per node [el][n]
     const int64_t e0 = (int64_t)blockIdx.x * epb;
     if (e0 >= p.nelements) return;
     const int ne = (int)min((int64_t)epb, p.nelements - e0);
@@ -271,6 +275,7 @@ struct AdjointKernel {
 #pragma unroll
       for (int v = 0; v < NV; ++v) uu[v] = p.u[g0 + v];
       P::prim(uu, ww, p.pp);
+      s_ir[el * NN + n] = 1.0 / uu[0];
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         U(el, v, n) = uu[v];
@@ -291,9 +296,9 @@ struct AdjointKernel {
         const int r0 = w - dir * PER_VOL;
         const int el = r0 / VOL_PER_DIR, r = r0 - (r0 / VOL_PER_DIR) * VOL_PER_DIR;
         if (el >= ne) continue;
-        if (dir == 0) vol_item<0>(p, el, r, s_u, s_w, s_l, s_vb, s_ij);
-        if constexpr (DIM > 1) if (dir == 1) vol_item<1>(p, el, r, s_u, s_w, s_l, s_vb, s_ij);
-        if constexpr (DIM > 2) if (dir == 2) vol_item<2>(p, el, r, s_u, s_w, s_l, s_vb, s_ij);
+        if (dir == 0) vol_item<0>(p, el, r, s_u, s_w, s_l, s_vb, s_ij, s_ir);
+        if constexpr (DIM > 1) if (dir == 1) vol_item<1>(p, el, r, s_u, s_w, s_l, s_vb, s_ij, s_ir);
+        if constexpr (DIM > 2) if (dir == 2) vol_item<2>(p, el, r, s_u, s_w, s_l, s_vb, s_ij, s_ir);
       } else {
         const int w2 = w - N_VOL;
         const int dir = w2 / PER_SURF;
@@ -302,9 +307,9 @@ struct AdjointKernel {
         const int r1 = r0 - el * (2 * NF);
         const int side = r1 / NF, t = r1 - (r1 / NF) * NF;
         if (el >= ne) continue;
-        if (dir == 0) surf_item<0>(p, e0, el, side, t, s_u, s_w, s_l, s_sb, s_ij);
-        if constexpr (DIM > 1) if (dir == 1) surf_item<1>(p, e0, el, side, t, s_u, s_w, s_l, s_sb, s_ij);
-        if constexpr (DIM > 2) if (dir == 2) surf_item<2>(p, e0, el, side, t, s_u, s_w, s_l, s_sb, s_ij);
+        if (dir == 0) surf_item<0>(p, e0, el, side, t, s_u, s_w, s_l, s_sb, s_ij, s_ir);
+        if constexpr (DIM > 1) if (dir == 1) surf_item<1>(p, e0, el, side, t, s_u, s_w, s_l, s_sb, s_ij, s_ir);
+        if constexpr (DIM > 2) if (dir == 2) surf_item<2>(p, e0, el, side, t, s_u, s_w, s_l, s_sb, s_ij, s_ir);
       }
     }
     __syncthreads();
@@ -373,7 +378,7 @@ struct AdjointKernel {
 
   template <int O>
   __device__ __forceinline__ static void vol_item(const AdjointParams &p, int el, int r, double *s_u, double *s_w,
-                                                  double *s_l, double *s_vb, const double *s_ij) {
+                                                  double *s_l, double *s_vb, const double *s_ij, const double *s_ir) {
     const double scale = -s_ij[el];
     if constexpr (VOL == VOL_WEAK) {
       // du_i = -J^{-1} sum_m dhat[i,m] f(u_m): cotangent of f(u_r) gathers the column r of dhat
@@ -413,7 +418,8 @@ struct AdjointKernel {
         um[v] = s_u[(el * NV + v) * NN + nm];
         wm[v] = s_w[(el * NV + v) * NN + nm];
       }
-      A::template two_point_vjp<O>(p.volume_flux, ui, wi, um, wm, g, bi, bm, p.pp);
+      A::template two_point_vjp<O>(p.volume_flux, ui, wi, s_ir[el * NN + ni], um, wm, s_ir[el * NN + nm], g, bi, bm,
+                                   p.pp);
       double *dst = s_vb + ((el * DIM + O) * VOL_PER_DIR + r) * 2 * NV;
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
@@ -426,7 +432,7 @@ struct AdjointKernel {
   template <int O>
   __device__ __forceinline__ static void surf_item(const AdjointParams &p, int64_t e0, int el, int side, int t,
                                                    double *s_u, double *s_w, double *s_l, double *s_sb,
-                                                   const double *s_ij) {
+                                                   const double *s_ij, const double *s_ir) {
     const int64_t e = e0 + el;
     const int32_t nb = p.face_table[e * (2 * DIM) + 2 * O + side];
     const int own = line_node<DIM, N, O>(t, side == 0 ? 0 : N - 1);
@@ -448,13 +454,14 @@ struct AdjointKernel {
                          : (-ij_own * p.lhat_r * lown + ij_nb * p.lhat_l * lnb);
     }
     P::prim(un, wn, p.pp);
+    const double irn = 1.0 / un[0], iro = s_ir[el * NN + own];
     double *dst = s_sb + ((el * 2 * DIM + 2 * O + side) * NF + t) * NV;
     if (side == 0) {
-      A::template two_point_vjp<O>(p.surface_flux, un, wn, uo, wo, g, bl, br, p.pp);
+      A::template two_point_vjp<O>(p.surface_flux, un, wn, irn, uo, wo, iro, g, bl, br, p.pp);
 #pragma unroll
       for (int v = 0; v < NV; ++v) dst[v] = br[v];
     } else {
-      A::template two_point_vjp<O>(p.surface_flux, uo, wo, un, wn, g, bl, br, p.pp);
+      A::template two_point_vjp<O>(p.surface_flux, uo, wo, iro, un, wn, irn, g, bl, br, p.pp);
 #pragma unroll
       for (int v = 0; v < NV; ++v) dst[v] = bl[v];
     }

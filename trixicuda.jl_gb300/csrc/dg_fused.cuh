@@ -70,6 +70,18 @@ __device__ __forceinline__ int line_node(int t, int a) {
   }
 }
 
+template <int DIM, int N>
+__device__ __forceinline__ int line_node_rt(int o, int t, int a) {
+  if constexpr (DIM == 1) {
+    return a;
+  } else if constexpr (DIM == 2) {
+    return (o == 0) ? a + t * N : t + a * N;
+  } else {
+    const int t1 = t % N, t2 = t / N;
+    return (o == 0) ? a + t1 * N + t2 * N * N : (o == 1) ? t1 + a * N + t2 * N * N : t1 + t2 * N + a * N * N;
+  }
+}
+
 // index of the pair (a, b), a != b, among the N(N-1)/2 pairs of a line
 template <int N>
 __device__ __forceinline__ int pair_index(int a, int b) {
@@ -111,8 +123,10 @@ struct FusedKernel {
   static constexpr int ITEMS_PER_EL = DIM * VOL_PER_DIR + SURF_PER_EL + DIM * FV_PER_DIR;
   static constexpr int F_PER_EL = ITEMS_PER_EL * NV;
   static constexpr int BLOCK = 256;
+  static constexpr int TRACE_PER_EL = 2 * DIM * NF * NV;  // neighbour face nodes (or mortar fluxes)
   static constexpr size_t smem_for(int epb) {
-    return sizeof(R) * ((size_t)epb * (2 * NV * NN + F_PER_EL) + 2 * epb + 2 * N * N + N);
+    return sizeof(R) * ((size_t)epb * (2 * NV * NN + F_PER_EL + TRACE_PER_EL) + 2 * epb + 2 * N * N + N) +
+           sizeof(int) * (size_t)epb * 2 * DIM;
   }
   // elements per block: ~2 flux items per thread, <= 48 KB of shared memory
   static constexpr int epb_pick() {
@@ -120,13 +134,20 @@ struct FusedKernel {
     if (e < 1) e = 1;
     if (e > 32) e = 32;
     while (e > 1 && smem_for(e) > 48 * 1024) --e;
+    while (e > 1 && e * NN > BLOCK) --e;  // one node per thread in phases A and C
     return e;
   }
   static constexpr int EPB = epb_pick();
+  static_assert(EPB * NN <= BLOCK, "one node per thread");
   static size_t smem_bytes() { return smem_for(EPB); }
 
   struct Smem {
-    R *cons, *prim, *fvol, *fsurf, *ffv, *alpha, *scale, *dsplit, *dhat, *invw;
+    R *cons, *prim, *fvol, *fsurf, *ffv, *alpha, *scale, *dsplit, *dhat, *invw, *trace;
+    int *conforming;  // [el][face]: 1 = trace holds the neighbour's node, 0 = a mortar flux
+    // [el][face][t][v]
+    __device__ __forceinline__ R *tr(int el, int face, int t) const {
+      return trace + ((el * 2 * DIM + face) * NF + t) * NV;
+    }
     // [el][v][node]
     __device__ __forceinline__ R &c(int el, int v, int n) const { return cons[(el * NV + v) * NN + n]; }
     __device__ __forceinline__ R &w(int el, int v, int n) const { return prim[(el * NV + v) * NN + n]; }
@@ -174,20 +195,18 @@ struct FusedKernel {
     for (int v = 0; v < NV; ++v) dst[v] = f[v];
   }
 
-  // surface item: face 2*O + side, face node t
+  // surface item: face 2*O + side, face node t (neighbour data staged in phase A)
   template <int O>
-  __device__ __forceinline__ static void surface_item(const FusedParams<R> &p, const Smem &s, int64_t e0, int el,
-                                                      int side, int t) {
-    const int64_t e = e0 + el;
-    const int32_t nb = p.face_table[e * (2 * DIM) + 2 * O + side];
+  __device__ __forceinline__ static void surface_item(const FusedParams<R> &p, const Smem &s, int el, int side,
+                                                      int t) {
+    const int face = 2 * O + side;
+    const R *src = s.tr(el, face, t);
     R f[NV];
-    if (nb >= 0) {
+    if (s.conforming[el * 2 * DIM + face]) {
       const int own = line_node<DIM, N, O>(t, side == 0 ? 0 : N - 1);
-      const int other = line_node<DIM, N, O>(t, side == 0 ? N - 1 : 0);
-      const double *src = p.u_in + ((int64_t)nb * NN + other) * NV;
       R un[NV], wn[NV], uo[NV], wo[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) un[v] = from_double<R>(src[v]);
+      for (int v = 0; v < NV; ++v) un[v] = src[v];
       P::prim(un, wn, p.pp);
       load_node(s, el, own, uo, wo);
       if (side == 0)
@@ -195,11 +214,10 @@ struct FusedKernel {
       else
         two_point_flux<DIM, EQ, R, O>(p.surface_flux, uo, wo, un, wn, f, p.pp);
     } else {
-      const double *src = p.mortar_flux + ((int64_t)(-nb - 1) * NF + t) * NV;
 #pragma unroll
-      for (int v = 0; v < NV; ++v) f[v] = from_double<R>(src[v]);
+      for (int v = 0; v < NV; ++v) f[v] = src[v];
     }
-    R *dst = s.surf(el, 2 * O + side, t);
+    R *dst = s.surf(el, face, t);
 #pragma unroll
     for (int v = 0; v < NV; ++v) dst[v] = f[v];
   }
@@ -230,6 +248,8 @@ struct FusedKernel {
     s.dsplit = s.scale + epb;
     s.dhat = s.dsplit + N * N;
     s.invw = s.dhat + N * N;
+    s.trace = s.invw + N;
+    s.conforming = reinterpret_cast<int *>(s.trace + epb * TRACE_PER_EL);
 
     const int64_t e0 = (int64_t)blockIdx.x * epb;
     if (e0 >= p.nelements) return;
@@ -237,20 +257,54 @@ struct FusedKernel {
     const int mode = p.mode;
     const bool surface = (mode != MODE_VOLUME);
 
-    // phase A: one thread per (element, node): load the node's variables,
-    // convert, primitive variables; per-element factors; operators to smem
-    for (int q = threadIdx.x; q < epb * NN; q += BLOCK) {
-      const int el = q / NN, node = q - (q / NN) * NN;
-      if (el >= ne) continue;
-      const double *src = p.u_in + ((e0 + el) * NN + node) * NV;
+    // phase A: every global read of the tile is issued here.  Thread q < epb*NN
+    // owns node q for the whole kernel (its u and k stay in registers until
+    // the node phase); the other threads stage the neighbours' face nodes
+    // (or the mortar fluxes) of the tile's faces in shared memory.
+    const int tid = threadIdx.x;
+    const bool use_k = (mode == MODE_RK) && (p.rk_a != 0.0);
+    const int my_el = tid / NN, my_node = tid - (tid / NN) * NN;
+    const bool has_node = (tid < epb * NN) && (my_el < ne);
+    const int64_t g0 = ((e0 + my_el) * NN + my_node) * NV;
+    double ureg[NV], kreg[NV];
+    if (has_node) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) ureg[v] = p.u_in[g0 + v];
+      if (use_k) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) kreg[v] = p.k[g0 + v];
+      }
+    }
+    if (surface) {
+      constexpr int PER_EL = 2 * DIM * NF;
+      const int n_trace = ne * PER_EL;
+      for (int j = (tid - epb * NN + BLOCK) % BLOCK; j < n_trace; j += BLOCK) {
+        const int el = j / PER_EL, r = j - (j / PER_EL) * PER_EL;
+        const int face = r / NF, t = r - (r / NF) * NF;
+        const int32_t nb = p.face_table[(e0 + el) * (2 * DIM) + face];
+        const double *src;
+        if (nb >= 0) {
+          const int o = face >> 1;
+          const int other = line_node_rt<DIM, N>(o, t, (face & 1) ? 0 : N - 1);
+          src = p.u_in + ((int64_t)nb * NN + other) * NV;
+        } else {
+          src = p.mortar_flux + ((int64_t)(-nb - 1) * NF + t) * NV;
+        }
+        R *dst = s.tr(el, face, t);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) dst[v] = from_double<R>(src[v]);
+        if (t == 0) s.conforming[el * 2 * DIM + face] = (nb >= 0);
+      }
+    }
+    if (has_node) {
       R uu[NV], ww[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) uu[v] = from_double<R>(src[v]);
+      for (int v = 0; v < NV; ++v) uu[v] = from_double<R>(ureg[v]);
       P::prim(uu, ww, p.pp);
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        s.c(el, v, node) = uu[v];
-        s.w(el, v, node) = ww[v];
+        s.c(my_el, v, my_node) = uu[v];
+        s.w(my_el, v, my_node) = ww[v];
       }
     }
     if (threadIdx.x < epb && threadIdx.x < ne) {
@@ -296,9 +350,9 @@ struct FusedKernel {
         const int r1 = r0 - el * (2 * NF);
         const int side = r1 / NF, t = r1 - (r1 / NF) * NF;
         if (el >= ne) continue;
-        if (dir == 0) surface_item<0>(p, s, e0, el, side, t);
-        if constexpr (DIM > 1) if (dir == 1) surface_item<1>(p, s, e0, el, side, t);
-        if constexpr (DIM > 2) if (dir == 2) surface_item<2>(p, s, e0, el, side, t);
+        if (dir == 0) surface_item<0>(p, s, el, side, t);
+        if constexpr (DIM > 1) if (dir == 1) surface_item<1>(p, s, el, side, t);
+        if constexpr (DIM > 2) if (dir == 2) surface_item<2>(p, s, el, side, t);
       } else if constexpr (VOL == VOL_SC) {
         const int w2 = w - N_VOL - n_surf;
         const int dir = w2 / PER_FV;
@@ -314,11 +368,9 @@ struct FusedKernel {
     }
     __syncthreads();
 
-    // phase C: one thread per (element, node), all variables
-    const bool use_k = (mode == MODE_RK) && (p.rk_a != 0.0);
-    for (int q = threadIdx.x; q < epb * NN; q += BLOCK) {
-      const int el = q / NN, node = q - (q / NN) * NN;
-      if (el >= ne) continue;
+    // phase C: the thread that loaded node q finishes it
+    if (has_node) {
+      const int el = my_el, node = my_node;
       int coord[3] = {0, 0, 0}, tface[3] = {0, 0, 0};
       {
         int qq = node;
@@ -403,7 +455,6 @@ struct FusedKernel {
           }
         }
       }
-      const int64_t g0 = ((e0 + el) * NN + node) * NV;
       if (mode == MODE_VOLUME) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) p.out[g0 + v] = to_double(acc[v]);
@@ -416,9 +467,9 @@ struct FusedKernel {
           if (mode == MODE_RHS) {
             p.out[g0 + v] = du;
           } else {
-            const double kk = (use_k ? p.rk_a * p.k[g0 + v] : 0.0) + dte * du;
+            const double kk = (use_k ? p.rk_a * kreg[v] : 0.0) + dte * du;
             p.k[g0 + v] = kk;
-            p.out[g0 + v] = p.u_in[g0 + v] + p.rk_b * kk;
+            p.out[g0 + v] = ureg[v] + p.rk_b * kk;
           }
         }
       } else {
@@ -431,9 +482,9 @@ struct FusedKernel {
           if (mode == MODE_RHS) {
             p.out[g0 + v] = dd;
           } else {
-            const double kk = use_k ? fma(p.rk_a, p.k[g0 + v], dd) : dd;
+            const double kk = use_k ? fma(p.rk_a, kreg[v], dd) : dd;
             p.k[g0 + v] = kk;
-            p.out[g0 + v] = fma(p.rk_b, kk, p.u_in[g0 + v]);
+            p.out[g0 + v] = fma(p.rk_b, kk, ureg[v]);
           }
         }
       }

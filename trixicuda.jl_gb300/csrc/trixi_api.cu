@@ -52,6 +52,7 @@ struct AdjointState {
   double *lu[2] = {nullptr, nullptr}, *lk[2] = {nullptr, nullptr};
   std::vector<double *> pool;           // free snapshot buffers
   std::map<int64_t, double *> ckpt;     // step -> stored state
+  double *stages_all = nullptr;         // store-all mode: the 5 stage inputs of every step
   std::vector<double *> all;            // every allocation, for cleanup
 };
 
@@ -1156,20 +1157,13 @@ int trixi_batch_rk_steps(trixi_batch *b, double *u, double *k, const double *dt_
       cudaError_t e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
       if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
     }
-    // one eager step outside capture makes every lazy initialisation (kernel
-    // attributes, mortar buffers) happen before recording; it writes only the
-    // scratch buffer and k, whose value at the start of a step is never read
-    // (the first stage has A_1 = 0), so the caller's state is untouched
-    {
-      cudaEvent_t ready;
-      cudaError_t e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
-      if (e == cudaSuccess) e = cudaEventRecord(ready, s);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->capture_stream, ready, 0);
-      cudaEventDestroy(ready);
-      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
-      int r = batch_step(b, bufs[0], bufs[1], k, b->capture_stream);
-      if (r) return r;
-      e = cudaStreamSynchronize(b->capture_stream);
+    // lazy initialisation (per-kernel shared-memory attributes) must not
+    // happen during capture: a zero-element launch of every group's kernel
+    // performs it without touching any data
+    for (auto &g : b->groups) {
+      FusedHost f = g.h->fused;
+      f.nelements = 0;
+      cudaError_t e = launch_fused(g.h->dim, g.h->N, g.h->eq, g.h->vol, g.h->vflux, g.h->mixed, f, s);
       if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
     }
     for (int parity = 0; parity < 2; ++parity) {
@@ -1425,7 +1419,16 @@ int trixi_adjoint_forward(trixi_handle *h, const double *u0, double dt, int64_t 
   for (int i = 0; i < 5 && !r; ++i) r = alloc(&A->stage[i]);
   for (int i = 0; i < 2 && !r; ++i) r = alloc(&A->lu[i]);
   for (int i = 0; i < 2 && !r; ++i) r = alloc(&A->lk[i]);
-  for (int64_t i = 0; i < A->snapshots && !r; ++i) {
+  // store-all mode: when the snapshot budget covers every step and the stage
+  // states of the whole solve fit in half of the free memory, keep the input
+  // of every RK stage, so that the backward sweep recomputes nothing
+  if (!r && nsnapshots >= nsteps - 1) {
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t need = 5 * (size_t)nsteps * bytes;
+    if (need < free_b / 2 && cudaMalloc(&A->stages_all, need) == cudaSuccess) A->all.push_back(A->stages_all);
+  }
+  for (int64_t i = 0; i < A->snapshots && !r && !A->stages_all; ++i) {
     double *p = nullptr;
     r = alloc(&p);
     if (!r) A->pool.push_back(p);
@@ -1435,6 +1438,23 @@ int trixi_adjoint_forward(trixi_handle *h, const double *u0, double dt, int64_t 
     return r;
   }
   TRIXI_CUDA(h, cudaMemcpyAsync(A->u0, u0, bytes, cudaMemcpyDeviceToDevice, s), "copy u0");
+  if (A->stages_all) {
+    {
+      const size_t nval = bytes / sizeof(double);
+      TRIXI_CUDA(h, cudaMemcpyAsync(A->stages_all, A->u0, bytes, cudaMemcpyDeviceToDevice, s), "copy");
+      for (int64_t j = 0; j < nsteps; ++j) {
+        double *base = A->stages_all + (size_t)j * 5 * nval;
+        for (int st = 0; st < 5; ++st) {
+          double *out = (st < 4) ? base + (size_t)(st + 1) * nval : (j + 1 < nsteps ? base + 5 * nval : uT);
+          r = run_rhs(h, MODE_RK, base + (size_t)st * nval, out, A->ktmp, kCK_A[st], kCK_B[st], dt, s);
+          if (r) return r;
+        }
+      }
+      A->fwd_steps = 0;
+      A->forward_done = true;
+      return TRIXI_OK;
+    }
+  }
   // forward sweep to T, storing the snapshots of the schedule's rightmost branch
   int64_t a = 0, s_free = A->snapshots;
   const double *from = A->u0;
@@ -1455,6 +1475,7 @@ int trixi_adjoint_forward(trixi_handle *h, const double *u0, double dt, int64_t 
   }
   r = advance(h, from, uT, nsteps - pos, s);
   if (r) return r;
+  A->fwd_steps = 0;  // count only the recomputation of the backward sweep
   A->forward_done = true;
   return TRIXI_OK;
 }
@@ -1471,7 +1492,26 @@ int trixi_adjoint_backward(trixi_handle *h, const double *uT_bar, double *u0_bar
   int cur = 0;
   TRIXI_CUDA(h, cudaMemcpyAsync(A->lu[0], uT_bar, bytes, cudaMemcpyDeviceToDevice, s), "copy");
   TRIXI_CUDA(h, cudaMemsetAsync(A->lk[0], 0, bytes, s), "zero");
-  int r = reverse(h, 0, A->n, A->snapshots, A->u0, cur, s);
+  int r = TRIXI_OK;
+  if (A->stages_all) {
+    const size_t nval = bytes / sizeof(double);
+    AdjointHost adj = adjoint_host(h);
+    adj.dt = A->dt;
+    for (int64_t j = A->n - 1; j >= 0; --j)
+      for (int st = 4; st >= 0; --st) {
+        adj.u = A->stages_all + ((size_t)j * 5 + st) * nval;
+        adj.lu_in = A->lu[cur];
+        adj.lk_in = A->lk[cur];
+        adj.lu_out = A->lu[1 - cur];
+        adj.lk_out = A->lk[1 - cur];
+        adj.rk_a = kCK_A[st];
+        adj.rk_b = kCK_B[st];
+        TRIXI_CUDA(h, launch_adjoint(adj, s), "adjoint stage");
+        cur = 1 - cur;
+      }
+  } else {
+    r = reverse(h, 0, A->n, A->snapshots, A->u0, cur, s);
+  }
   if (r) return r;
   TRIXI_CUDA(h, cudaMemcpyAsync(u0_bar, A->lu[cur], bytes, cudaMemcpyDeviceToDevice, s), "copy");
   if (forward_steps) *forward_steps = A->fwd_steps;
