@@ -123,6 +123,10 @@ typedef struct trixi_problem_desc {
    * src/solvers/containers_2d.jl:7), needed by trixi_compute_coefficients and
    * trixi_calc_error_norms with an analytic reference. */
   const double *node_coordinates;
+  /* Partitioned meshes: the last nghost_elements elements are ghosts (copies
+   * of another rank's elements, refreshed by a halo exchange).  Their faces
+   * may be left unconnected and their rhs is not meaningful. */
+  int64_t nghost_elements;
 } trixi_problem_desc;
 
 /* Library version string ("trixi_b200 <semver> sm_103a"). */

@@ -312,10 +312,18 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
     if (f != INT32_MIN) return bad("mortar %lld: large face already connected (element %lld)", (long long)m + 1, (long long)large);
     f = (int32_t)(-(base + nc) - 1);
   }
+  if (d->nghost_elements < 0 || d->nghost_elements >= h->E) return bad("nghost_elements %lld of %lld", (long long)d->nghost_elements, (long long)h->E);
+  const int64_t first_ghost = h->E - d->nghost_elements;
   for (size_t i = 0; i < ft.size(); ++i)
-    if (ft[i] == INT32_MIN)
+    if (ft[i] == INT32_MIN) {
+      const int64_t e = (int64_t)(i / nfaces);
+      if (e >= first_ghost) {
+        ft[i] = (int32_t)e;  // open ghost face: read the ghost itself (its rhs is discarded)
+        continue;
+      }
       return bad("element %lld face %lld has no interface or mortar (non-periodic meshes are not supported)",
                  (long long)(i / nfaces) + 1, (long long)(i % nfaces) + 1);
+    }
 
   for (int64_t e = 0; e < h->E; ++e) h->total_volume += std::pow(2.0 / d->inverse_jacobian[e], h->dim);
   // all host-side validation is done; from here on the device is touched
@@ -1064,6 +1072,7 @@ int trixi_batch_create(const trixi_problem_desc *const *descs, int64_t n, trixi_
     md.mortar_large_sides = mo_ls.empty() ? nullptr : mo_ls.data();
     md.mortar_orientations = mo_ori.empty() ? nullptr : mo_ori.data();
     md.node_coordinates = have_coords ? coords.data() : nullptr;
+    md.nghost_elements = 0;
     md.weights = md.derivative_split = md.derivative_dhat = md.inverse_vandermonde_legendre = nullptr;
     md.forward_upper = md.forward_lower = md.reverse_upper = md.reverse_lower = nullptr;
     trixi_batch::Group g;

@@ -63,6 +63,7 @@ mutable struct ProblemDesc
     reverse_upper::Ptr{Float64}
     reverse_lower::Ptr{Float64}
     node_coordinates::Ptr{Float64}
+    nghost_elements::Int64
 end
 
 flux_code(::typeof(Trixi.flux_ranocha)) = FLUX_RANOCHA
@@ -110,7 +111,7 @@ function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
                        ninterfaces(interfaces), pointer(interfaces.neighbor_ids), pointer(interfaces.orientations),
                        0, Trixi.nmortars(mortars), pointer(mortars.neighbor_ids), pointer(mortars.large_sides),
                        pointer(mortars.orientations), pointer(weights), pointer(dsplit), pointer(dhat),
-                       C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, pointer(elements.node_coordinates))
+                       C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, pointer(elements.node_coordinates), 0)
     desc.struct_size = Int32(sizeof(ProblemDesc))
     handle = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve elements interfaces mortars dsplit dhat weights desc begin

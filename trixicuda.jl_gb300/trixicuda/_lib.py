@@ -88,6 +88,7 @@ class ProblemDesc(C.Structure):
         ("reverse_upper", C.POINTER(C.c_double)),
         ("reverse_lower", C.POINTER(C.c_double)),
         ("node_coordinates", C.POINTER(C.c_double)),
+        ("nghost_elements", C.c_int64),
     ]
 
 

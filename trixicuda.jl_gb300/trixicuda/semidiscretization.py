@@ -104,6 +104,7 @@ def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver:
     d.mortar_large_sides = _ptr_i(keep["mo_ls"])
     d.mortar_orientations = _ptr_i(keep["mo_ori"])
     d.node_coordinates = _ptr_d(keep["coords"])
+    d.nghost_elements = int(getattr(cont, "nghost_elements", 0))
     return d, keep, cont
 
 
@@ -113,7 +114,7 @@ class SemidiscretizationHyperbolicGPU:
 
     def __init__(self, mesh: TreeMesh, equations: AbstractEquations, initial_condition, solver: DGSEMGPU,
                  source_terms=None, boundary_conditions="periodic", RealT=np.float64, uEltype=np.float64,
-                 precision: str = "fp64", device=None):
+                 precision: str = "fp64", device=None, containers=None):
         if mesh.ndims != equations.ndims:
             raise ValueError("mesh and equations dimension differ")
         if source_terms is not None:
@@ -127,7 +128,8 @@ class SemidiscretizationHyperbolicGPU:
         self.source_terms = source_terms
         self.boundary_conditions = "periodic"
         self.precision = precision
-        desc, keep, cont = build_problem_desc(mesh, equations, solver, precision)
+        desc, keep, cont = build_problem_desc(containers if containers is not None else mesh, equations, solver,
+                                              precision)
         self.containers = cont
         self._desc, self._keep = desc, keep
         torch = _torch()
