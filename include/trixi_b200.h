@@ -232,6 +232,26 @@ typedef enum trixi_integral_kind {
 int trixi_integrate(trixi_handle *h, const double *u, const double *du, int which, double *out_host, int64_t count,
                     void *stream);
 
+/* The integrals of trixi_integrate for callers that cannot allocate device
+ * memory.  No counterpart in the reference: it exists for callers whose GPU
+ * memory belongs to another allocator (a CUDA.jl or PyTorch caching pool that
+ * has reserved the device) and for loops that must not pay the device-wide
+ * synchronisation of cudaMalloc / cudaFree.  It needs no handle and calls no
+ * allocating routine: u, du (node layout [nelements][N^ndims][nvars]),
+ * inverse_jacobian[nelements] and out_dev (nvars values for STATE and DU, one
+ * otherwise) are device pointers owned by the caller; the per-element partial
+ * sums go to a static device array of 2^20 doubles (8 MiB) that every GPU
+ * loading the library reserves until the process exits.  Calls with
+ * nelements * (number of results) > 2^20 return TRIXI_ERR_INVALID_ARGUMENT.
+ * The first call on a device looks up that array's address with the device
+ * current, so make it before any stream capture.  All calls share the array
+ * and it keeps the last call's contents (each call writes every slot it
+ * reads); calls whose kernels overlap on the GPU race on it.  Asynchronous on
+ * `stream`; errors are read with trixi_last_error(NULL, ...). */
+int trixi_integrate_noalloc(int ndims, int polydeg, int equation, double gamma, const double *u, const double *du,
+                            const double *inverse_jacobian, int64_t nelements, int which, double *out_dev,
+                            void *stream);
+
 /* L2 and Linf errors per variable after interpolation to 2*polydeg+1 LGL
  * analysis nodes, against an analytic initial condition at time t (u_ref
  * NULL) or against a second state u_ref on the same mesh.  L2 is normalised

@@ -233,6 +233,30 @@ bool compute_basis(int polydeg, Basis &b) {
   return true;
 }
 
+bool lgl_weights_fixed(int polydeg, double *w_out) {
+  const int n = polydeg + 1;
+  if (n < 2 || n > 16) return false;
+  const int p = polydeg;
+  real_t x[16];
+  x[0] = -1;
+  x[n - 1] = 1;
+  for (int j = 1; j < p; ++j) {
+    real_t z = -std::cos(kPi * j / p);
+    for (int it = 0; it < 200; ++it) {
+      const LegendreValue lv = legendre_value(p, z);
+      const real_t step = lv.dp / ((2 * z * lv.dp - p * (p + 1) * lv.p) / (1 - z * z));
+      z -= step;
+      if (std::fabs(step) <= 1e-32L) break;
+    }
+    x[j] = z;
+  }
+  for (int j = 0; j < n; ++j) {
+    const real_t lp = legendre_value(p, x[j]).p;
+    w_out[j] = (double)(2 / (p * (p + 1) * lp * lp));
+  }
+  return true;
+}
+
 bool analysis_operators(int polydeg, int na, std::vector<double> &vdm, std::vector<double> &wa,
                         std::vector<double> &xa) {
   const int n = polydeg + 1;

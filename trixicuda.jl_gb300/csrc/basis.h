@@ -15,6 +15,9 @@ struct Basis {
 
 bool compute_basis(int polydeg, Basis &b);
 
+// LGL quadrature weights into w_out[polydeg+1] using stack storage only.
+bool lgl_weights_fixed(int polydeg, double *w_out);
+
 // Interpolation from the polydeg LGL nodes to `na` LGL analysis nodes
 // (row-major [na][polydeg+1]), with the analysis weights and nodes -- the
 // SolutionAnalyzer of the reference (src/solvers/basis_lobatto_legendre.jl:120-137).

@@ -9,9 +9,14 @@
 // Reductions are deterministic: per-element partials, then one block that
 // sums them in a fixed order.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdio>
 
+#include "../../include/trixi_b200.h"
+#include "basis.h"
 #include "dg_analysis.h"
+#include "dg_host.h"
 #include "dg_physics.cuh"
 
 namespace trixi {
@@ -127,6 +132,42 @@ __global__ void integrate_kernel(int N, int64_t E, const double *__restrict__ u,
     double wt = 1.0;
     for (int d = 0; d < DIM; ++d) {
       wt *= w[r % N];
+      r /= N;
+    }
+    double q[NV];
+    quantity<DIM, EQ>(which, u + (e * NN + n) * NV, du ? du + (e * NN + n) * NV : nullptr, gamma, q);
+    for (int k = 0; k < nq; ++k) acc[k] += wt * q[k];
+  }
+  double J = 1.0;
+  for (int d = 0; d < DIM; ++d) J /= inv_jac[e];
+  for (int k = 0; k < nq; ++k) {
+    double v = acc[k];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) partial[e * nq + k] = v * J;
+  }
+}
+
+struct WeightsArg {
+  double w[16];
+};
+
+// integrate_kernel with the quadrature weights passed by value (no device copy of them needed)
+template <int DIM, int EQ>
+__global__ void integrate_w_kernel(int N, int64_t E, const double *__restrict__ u, const double *__restrict__ du,
+                                   const double *__restrict__ inv_jac, WeightsArg wa, int which, int nq, double gamma,
+                                   double *__restrict__ partial) {
+  constexpr int NV = NVarsOf<DIM, EQ>::value;
+  const int64_t e = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (e >= E) return;
+  const int NN = nodes_per_elem<DIM>(N);
+  double acc[NV];
+  for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+  for (int n = lane; n < NN; n += 32) {
+    int r = n;
+    double wt = 1.0;
+    for (int d = 0; d < DIM; ++d) {
+      wt *= wa.w[r % N];
       r /= N;
     }
     double q[NV];
@@ -440,3 +481,91 @@ cudaError_t launch_error_norms_all(const ErrorNormHost &h, cudaStream_t s) {
 }
 
 }  // namespace trixi
+
+// ===========================================================================
+// trixi_integrate_noalloc: the quadrature integrals of trixi_integrate for
+// callers that cannot allocate device memory -- for example an application
+// whose device memory is owned entirely by another allocator (a Julia
+// CUDA.jl or PyTorch caching pool that has reserved the GPU), or a
+// time-critical loop that must not pay for the device-wide synchronisation
+// that cudaMalloc / cudaFree imply.  Its per-element partial sums live in the
+// file-scope device array below instead of a handle-owned buffer, and it
+// needs no handle (trixi_create allocates).  Limits and sharing rules:
+//   * at most kNoallocMaxPartials = 2^20 partial sums per call, i.e.
+//     nelements * nq <= 1,048,576 (nq = nvars for STATE and DU, 1 otherwise);
+//     larger calls are rejected with TRIXI_ERR_INVALID_ARGUMENT;
+//   * the array (8 MiB) is reserved on every GPU that loads the library, until
+//     the process exits;
+//   * all calls share it and it keeps the last call's contents.  Every slot a
+//     call reads it has written itself first, so nothing needs clearing, but
+//     two calls whose kernels overlap on the GPU (different streams, or
+//     different host threads on the same device) race on it;
+//   * the first call on a device looks up the array's device address
+//     (cudaGetSymbolAddress) with that device current, and caches it per
+//     device.
+// ===========================================================================
+// file-scope scratch shared by every call on a device (see above)
+static constexpr int64_t kNoallocMaxPartials = int64_t(1) << 20;
+static __device__ __align__(256) double g_noalloc_partials[kNoallocMaxPartials];
+
+namespace {
+
+// device address of g_noalloc_partials per device ordinal; filled at the first
+// call on that device, with that device current
+constexpr int kMaxDevices = 64;
+std::atomic<double *> g_noalloc_ptr[kMaxDevices];
+
+int noalloc_scratch(double **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TRIXI_ERR_CUDA;
+  double *p = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_partials);
+    if (e != cudaSuccess || !p) return TRIXI_ERR_CUDA;
+    g_noalloc_ptr[dev].store(p, std::memory_order_release);
+  }
+  *out = p;
+  return TRIXI_OK;
+}
+
+}  // namespace
+extern "C" int trixi_integrate_noalloc(int ndims, int polydeg, int equation, double gamma, const double *u,
+                                       const double *du, const double *inverse_jacobian, int64_t nelements,
+                                       int which, double *out_dev, void *stream) {
+  using namespace trixi;
+  char msg[256];
+  auto reject = [&](int status, const char *text) {
+    set_last_error(status, text);
+    return status;
+  };
+  if (ndims < 1 || ndims > 3) return reject(TRIXI_ERR_INVALID_ARGUMENT, "integrate_noalloc: ndims");
+  if (polydeg < 1 || polydeg > 15) return reject(TRIXI_ERR_INVALID_ARGUMENT, "integrate_noalloc: polydeg");
+  if (equation != EQ_ADV && equation != EQ_EULER) return reject(TRIXI_ERR_INVALID_ARGUMENT, "integrate_noalloc: equation");
+  if (which < 0 || which > 3) return reject(TRIXI_ERR_INVALID_ARGUMENT, "integrate_noalloc: integral kind");
+  if (!u || !inverse_jacobian || !out_dev || nelements <= 0 || ((which == 2 || which == 3) && !du))
+    return reject(TRIXI_ERR_INVALID_ARGUMENT, "integrate_noalloc: null pointer or empty mesh");
+  const int nv = (equation == EQ_ADV) ? 1 : ndims + 2;
+  const int nq = (which == 0 || which == 3) ? nv : 1;
+  if (nelements > kNoallocMaxPartials / nq) {
+    snprintf(msg, sizeof(msg),
+             "integrate_noalloc: %lld elements x %d values exceed the %lld partial sums of its static scratch",
+             (long long)nelements, nq, (long long)kNoallocMaxPartials);
+    return reject(TRIXI_ERR_INVALID_ARGUMENT, msg);
+  }
+  double *partials = nullptr;
+  if (noalloc_scratch(&partials) != TRIXI_OK)
+    return reject(TRIXI_ERR_CUDA, "integrate_noalloc: cudaGetSymbolAddress of the scratch array failed");
+  WeightsArg wa{};
+  if (!lgl_weights_fixed(polydeg, wa.w)) return reject(TRIXI_ERR_INVALID_ARGUMENT, "integrate_noalloc: weights");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int per_block = 8;
+  const unsigned grid = (unsigned)((nelements + per_block - 1) / per_block);
+  const int N = polydeg + 1;
+  TRIXI_DISPATCH(ndims, equation,
+                 (integrate_w_kernel<D_, Q_><<<grid, 32 * per_block, 0, s>>>(N, nelements, u, du, inverse_jacobian, wa,
+                                                                             which, nq, gamma, partials)));
+  if (cudaGetLastError() != cudaSuccess) return reject(TRIXI_ERR_CUDA, "integrate_noalloc: kernel launch");
+  reduce_columns<<<1, 1024, 0, s>>>(nelements, nq, partials, 0, out_dev);
+  if (cudaGetLastError() != cudaSuccess) return reject(TRIXI_ERR_CUDA, "integrate_noalloc: reduction launch");
+  return TRIXI_OK;
+}

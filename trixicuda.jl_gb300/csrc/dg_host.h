@@ -9,6 +9,9 @@ namespace trixi {
 
 constexpr int HOST_NMAX = 6;  // largest N = polydeg + 1 with compiled kernels
 
+// records the message returned by trixi_last_error(NULL, ...) (trixi_api.cu)
+void set_last_error(int status, const char *msg);
+
 // Launch arguments of the fused kernel, precision independent.
 struct FusedHost {
   const double *u_in = nullptr;

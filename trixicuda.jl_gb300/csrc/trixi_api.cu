@@ -31,6 +31,15 @@ namespace {
 thread_local std::string g_last_error;
 thread_local int g_last_status = TRIXI_OK;
 
+}  // namespace
+
+void trixi::set_last_error(int status, const char *msg) {
+  g_last_error = msg ? msg : "";
+  g_last_status = status;
+}
+
+namespace {
+
 // CarpenterKennedy2N54 coefficients (Carpenter & Kennedy 1994, NASA TM-109112).  The
 // stage times t + c_s dt are not needed: the semidiscretization is autonomous
 // (periodic boundaries, no source terms).

@@ -134,6 +134,7 @@ SIGNATURES = {
     "trixi_batch_handle": (C.c_int, [_VP, _I64, C.POINTER(C.c_void_p)]),
     "trixi_batch_last_error": (C.c_int, [_VP, C.c_char_p, C.c_size_t]),
     "trixi_integrate": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _VP]),
+    "trixi_integrate_noalloc": (C.c_int, [_I, _I, _I, C.c_double, _VP, _VP, _VP, _I64, _I, _VP, _VP]),
     "trixi_calc_error_norms": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _D,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double), _VP]),
     "trixi_probe_convert": (C.c_int, [_VP, _VP, _VP, _VP, _I64, _VP]),
