@@ -298,9 +298,16 @@ int trixi_batch_layout(const trixi_batch *b, int64_t *value_offsets, int64_t *nv
                        int64_t *ngroups);
 int trixi_batch_rhs(trixi_batch *b, double *du, const double *u, void *stream);
 /* nsteps CarpenterKennedy2N54 steps; instance i uses dt_per_instance[i] (host
- * array).  use_graph != 0 replays a captured CUDA graph of the whole step. */
+ * array).  use_graph != 0 replays a captured CUDA graph of the whole step, in
+ * which the groups run as parallel branches; the first graph build tunes the
+ * branch count by timing candidate graphs on copies of u and k. */
 int trixi_batch_rk_steps(trixi_batch *b, double *u, double *k, const double *dt_per_instance, int64_t nsteps,
                          int use_graph, void *stream);
+/* The tuner's choice and its timings: *branches (0 before the first graph
+ * build), up to `max` candidate branch counts with their ms per step, and the
+ * number of candidates in *count. */
+int trixi_batch_tuning(const trixi_batch *b, int *branches, int *candidates, double *ms_per_step, int64_t max,
+                       int64_t *count);
 /* The merged handle of one group (for the stage API and analysis calls). */
 int trixi_batch_handle(trixi_batch *b, int64_t group, trixi_handle **h);
 int trixi_batch_last_error(const trixi_batch *b, char *buf, size_t len);

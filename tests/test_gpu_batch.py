@@ -56,6 +56,10 @@ def test_batch_matches_single_problems(precision, cuda):
     batch.rk_steps(un, kn, dts, 3, use_graph=False)
     cuda.cuda.synchronize()
     assert cuda.equal(ug, un) and cuda.equal(kg, kn)  # graph replay == direct launches
+    # the branch tuner ran at the graph build, on copies of the state
+    branches, timings = batch.tuning()
+    assert branches in timings and all(ms > 0 for ms in timings.values())
+    assert 1 in timings and max(timings) <= batch.ngroups
     for i, pb in enumerate(probs):
         semi = T.SemidiscretizationHyperbolicGPU(pb.mesh, pb.equations, pb.initial_condition, pb.solver,
                                                  precision=precision)

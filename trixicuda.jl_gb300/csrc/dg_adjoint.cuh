@@ -23,8 +23,8 @@ namespace trixi {
 __device__ __forceinline__ void ln_mean_grad(double x, double y, double r, double &L, double &dx, double &dy) {
   const double s = x + y, d = x - y, f = d * r, u = f * f;
   if (u < LnMeanThreshold<double>::value) {
-    const double h = 1.0 + u * (-1.0 / 3.0 + u * (-4.0 / 45.0 + u * (-44.0 / 945.0)));
-    const double hp = -1.0 / 3.0 + u * (-8.0 / 45.0 + u * (-132.0 / 945.0));
+    const double h = series_h(u);
+    const double hp = series_h_du(u);
     L = 0.5 * s * h;
     dx = 0.5 * h + 2.0 * f * y * hp * r;
     dy = 0.5 * h - 2.0 * f * x * hp * r;
@@ -39,8 +39,8 @@ __device__ __forceinline__ void ln_mean_grad(double x, double y, double r, doubl
 __device__ __forceinline__ void inv_ln_mean_grad(double x, double y, double r, double &Q, double &dx, double &dy) {
   const double d = x - y, f = d * r, u = f * f;
   if (u < LnMeanThreshold<double>::value) {
-    const double g = 1.0 + u * (1.0 / 3.0 + u * (1.0 / 5.0 + u * (1.0 / 7.0)));
-    const double gp = 1.0 / 3.0 + u * (2.0 / 5.0 + u * (3.0 / 7.0));
+    const double g = series_g(u);
+    const double gp = series_g_du(u);
     Q = 2.0 * r * g;
     dx = -2.0 * r * r * g + 8.0 * f * y * r * r * r * gp;
     dy = -2.0 * r * r * g - 8.0 * f * x * r * r * r * gp;

@@ -9,19 +9,23 @@
 //   and optionally the 2N low-storage RK stage update (OrdinaryDiffEq's
 //   CarpenterKennedy2N54 broadcast, outside the reference).
 //
-// Work decomposition: one thread per two-point flux.  Phase A stages the
-// tile's states in shared memory (conservative and primitive variables, in
-// the compute precision).  Phase B evaluates every flux the tile needs, each
-// exactly once per element: the symmetric volume fluxes f#(u_i, u_m), i < m,
-// on every line (N(N-1)/2 per line instead of the reference's N^2), the
-// surface fluxes on the element's 2*ndims faces (the neighbour's adjacent
-// node is read straight from u -- "owner computes", no interfaces.u or
-// surface_flux_values round trip through HBM; mortar faces read the flux
-// prepared by the mortar kernel), and for shock capturing the LGL subcell
-// FV fluxes.  Phase C gives one thread per (node, variable): it sums
-// D_split / D_hat times the staged fluxes along each dimension, adds the
-// surface terms, scales by -J^{-1}, and stores du or performs the RK update,
-// with coalesced global accesses in the reference layout.
+// Work decomposition.  A block holds GPB independent groups; a group of WPG
+// warps owns EPG consecutive elements (chosen at compile time so that each
+// warp's flux items fall in one direction/section) and synchronises only
+// among itself.  Phase A: one owner thread per node loads its u (and k) into
+// registers and stores the node's conservative and primitive variables, in
+// the compute precision, as a record in shared memory; all threads of the
+// group stage the neighbours' face nodes.  Phase B: one thread per two-point
+// flux evaluates every flux the group needs, each exactly once per element:
+// the symmetric volume fluxes f#(u_i, u_m), i < m, on every line (N(N-1)/2
+// per line instead of the reference's N^2), the surface fluxes on the
+// element's 2*ndims faces (the neighbour's adjacent node is read straight
+// from u -- "owner computes", no interfaces.u or surface_flux_values round
+// trip through HBM; mortar faces read the flux prepared by the mortar
+// kernel), and for shock capturing the LGL subcell FV fluxes.  Phase C: the
+// owner thread sums D_split / D_hat times the staged fluxes along each
+// dimension, adds the surface terms, scales by -J^{-1}, and stores du or
+// performs the RK update, in the reference layout.
 #pragma once
 #include "dg_convert.cuh"
 #include "dg_physics.cuh"
@@ -46,6 +50,8 @@ struct FusedParams {
   int mode;
   int surface_flux, fv_flux;
   double rk_a, rk_b, dt;
+  int use_k;                                // RK: read k (rk_a != 0)
+  int vec16;                                // u_in, out, k, mortar_flux 16-byte aligned
   double atol;                              // dg-only test for alpha
   PhysParams<R> pp;
   R dsplit[NMAXT * NMAXT];                  // row-major [i][m], diagonal zeroed
@@ -109,6 +115,72 @@ __device__ __forceinline__ void pair_nodes(int p, int &i, int &m) {
   m = (int)((PairBits<N>::M >> (4 * p)) & 0xfull);
 }
 
+// Node records of NV values in shared memory: one 16-byte (float) or two
+// 16-byte (double) accesses when NV == 4, scalar accesses otherwise.
+template <int NV, typename R>
+__device__ __forceinline__ void lds_rec(const R *src, R *dst) {
+  if constexpr (NV == 4 && sizeof(R) == 4) {
+    const float4 t = *reinterpret_cast<const float4 *>(src);
+    dst[0] = t.x;
+    dst[1] = t.y;
+    dst[2] = t.z;
+    dst[3] = t.w;
+  } else if constexpr (NV == 4 && sizeof(R) == 8) {
+    const double2 a = reinterpret_cast<const double2 *>(src)[0], b = reinterpret_cast<const double2 *>(src)[1];
+    dst[0] = a.x;
+    dst[1] = a.y;
+    dst[2] = b.x;
+    dst[3] = b.y;
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dst[v] = src[v];
+  }
+}
+template <int NV, typename R>
+__device__ __forceinline__ void sts_rec(R *dst, const R *src) {
+  if constexpr (NV == 4 && sizeof(R) == 4) {
+    *reinterpret_cast<float4 *>(dst) = make_float4(src[0], src[1], src[2], src[3]);
+  } else if constexpr (NV == 4 && sizeof(R) == 8) {
+    reinterpret_cast<double2 *>(dst)[0] = make_double2(src[0], src[1]);
+    reinterpret_cast<double2 *>(dst)[1] = make_double2(src[2], src[3]);
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dst[v] = src[v];
+  }
+}
+// The NV doubles of one node in global memory: two 16-byte accesses when
+// NV == 4 and the arrays are 16-byte aligned (vec), scalar accesses otherwise.
+template <int NV>
+__device__ __forceinline__ void ldg_node(const double *src, double *dst, bool vec) {
+  if constexpr (NV == 4) {
+    if (vec) {
+      const double2 a = __ldg(reinterpret_cast<const double2 *>(src));
+      const double2 b = __ldg(reinterpret_cast<const double2 *>(src) + 1);
+      dst[0] = a.x;
+      dst[1] = a.y;
+      dst[2] = b.x;
+      dst[3] = b.y;
+      return;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) dst[v] = src[v];
+}
+template <int NV>
+__device__ __forceinline__ void stg_node(double *dst, const double *src, bool vec) {
+  if constexpr (NV == 4) {
+    if (vec) {
+      reinterpret_cast<double2 *>(dst)[0] = make_double2(src[0], src[1]);
+      reinterpret_cast<double2 *>(dst)[1] = make_double2(src[2], src[3]);
+      return;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) dst[v] = src[v];
+}
+
+constexpr int round_up4(int x) { return (x + 3) & ~3; }
+
 template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX>
 struct FusedKernel {
   using P = Physics<DIM, EQ, R>;
@@ -121,36 +193,107 @@ struct FusedKernel {
   static constexpr int SURF_PER_EL = 2 * DIM * NF;
   static constexpr int FV_PER_DIR = (VOL == VOL_SC) ? NF * (N - 1) : 0;
   static constexpr int ITEMS_PER_EL = DIM * VOL_PER_DIR + SURF_PER_EL + DIM * FV_PER_DIR;
-  static constexpr int F_PER_EL = ITEMS_PER_EL * NV;
-  static constexpr int BLOCK = 256;
   static constexpr int TRACE_PER_EL = 2 * DIM * NF * NV;  // neighbour face nodes (or mortar fluxes)
-  static constexpr size_t smem_for(int epb) {
-    return sizeof(R) * ((size_t)epb * (2 * NV * NN + F_PER_EL + TRACE_PER_EL) + 2 * epb + 2 * N * N + N) +
-           sizeof(int) * (size_t)epb * 2 * DIM;
+  // Thread mapping: one owner thread per node.  A group of WPG warps owns EPG
+  // elements and synchronises only among itself (__syncwarp or a named
+  // barrier), never block-wide, so groups of a block drift apart and hide
+  // each other's latency.
+  static constexpr int TPE = NN;  // owner threads per element
+  // shared memory of one group of `epg` elements (every array 16-byte aligned)
+  static constexpr int n_cons(int epg) { return round_up4(epg * NN * NV); }
+  static constexpr int n_vol(int epg) { return round_up4(epg * DIM * VOL_PER_DIR * NV); }
+  static constexpr int n_surf(int epg) { return round_up4(epg * SURF_PER_EL * NV); }
+  static constexpr int n_fv(int epg) { return round_up4(epg * DIM * FV_PER_DIR * NV); }
+  static constexpr int n_trace(int epg) { return round_up4(epg * TRACE_PER_EL); }
+  static constexpr int n_el(int epg) { return round_up4(epg); }
+  static constexpr int N_OPS = round_up4(2 * N * N + N);  // D_split, D_hat, 1/w
+  static constexpr size_t group_smem(int epg) {
+    return sizeof(R) * (size_t)(2 * n_cons(epg) + n_vol(epg) + n_surf(epg) + n_fv(epg) + n_trace(epg) +
+                                2 * n_el(epg) + N_OPS) +
+           sizeof(int) * (size_t)round_up4(epg * 2 * DIM);
   }
-  // elements per block: ~2 flux items per thread, <= 48 KB of shared memory
-  static constexpr int epb_pick() {
-    int e = (2 * BLOCK + ITEMS_PER_EL - 1) / ITEMS_PER_EL;
-    if (e < 1) e = 1;
-    if (e > 32) e = 32;
-    while (e > 1 && smem_for(e) > 48 * 1024) --e;
-    while (e > 1 && e * NN > BLOCK) --e;  // one node per thread in phases A and C
-    return e;
+  static constexpr int warps_for(int epg) { return (epg * TPE + 31) / 32; }
+  // Warp passes of phase B for a group of `epg` elements: items are ordered
+  // [volume dir 0 | dir 1 | ... | surface dir 0 | ... | FV dir 0 | ...] and a
+  // warp executes one pass per section that its 32 items touch.
+  static constexpr int phase_b_passes(int epg) {
+    int bounds[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int nb = 0, acc = 0;
+    for (int d = 0; d < DIM; ++d) bounds[nb++] = (acc += epg * VOL_PER_DIR);
+    for (int d = 0; d < DIM; ++d) bounds[nb++] = (acc += epg * 2 * NF);
+    if (FV_PER_DIR > 0)
+      for (int d = 0; d < DIM; ++d) bounds[nb++] = (acc += epg * FV_PER_DIR);
+    int passes = 0;
+    for (int w0 = 0; w0 < acc; w0 += 32) {
+      const int w1 = (w0 + 32 < acc) ? w0 + 32 : acc;
+      int lo = 0;
+      for (int b = 0; b < nb; ++b) {
+        if (bounds[b] > lo && lo < w1 && bounds[b] > w0) ++passes;  // section [lo, bounds[b]) meets [w0, w1)
+        lo = bounds[b];
+      }
+    }
+    return passes;
   }
-  static constexpr int EPB = epb_pick();
-  static_assert(EPB * NN <= BLOCK, "one node per thread");
+  // elements per group: fewest phase-B passes per element, then fewest idle
+  // owner lanes, within 8 warps and (beyond one element) 48 KB per group
+  static constexpr int epg_pick() {
+    int best = 1;
+    long best_cost = -1;
+    for (int e = 1; e <= 32; e *= 2) {
+      if (warps_for(e) > 8) break;
+      if (e > 1 && group_smem(e) > 48 * 1024) break;
+      // cost per element in 1/1000 units: passes plus idle-lane waste of phases A/C
+      const long cost = 1000L * phase_b_passes(e) / e + 1000L * (warps_for(e) * 32 - e * TPE) / (32 * e);
+      if (best_cost < 0 || cost < best_cost) {
+        best = e;
+        best_cost = cost;
+      }
+    }
+    return best;
+  }
+  static constexpr int EPG = epg_pick();  // elements per group
+  // warps per group: the owners of EPG elements, and at least one warp per
+  // 6 KB of the group's shared memory (so that shared-memory-limited
+  // occupancy still leaves ~38 warps per SM for phase B), at most 8
+  static constexpr int wpg_pick() {
+    int w = warps_for(EPG);
+    const int by_smem = (int)((group_smem(EPG) + 6 * 1024 - 1) / (6 * 1024));
+    if (by_smem > w) w = by_smem;
+    return w < 8 ? w : (warps_for(EPG) > 8 ? warps_for(EPG) : 8);
+  }
+  static constexpr int WPG = wpg_pick();  // warps per group
+  static constexpr int GT = 32 * WPG;                  // threads per group
+  static constexpr int N_CONS = n_cons(EPG);
+  static constexpr int N_VOL = n_vol(EPG);
+  static constexpr int N_SURF = n_surf(EPG);
+  static constexpr int N_FV = n_fv(EPG);
+  static constexpr int N_TRACE = n_trace(EPG);
+  static constexpr int N_EL = n_el(EPG);
+  static constexpr size_t GROUP_SMEM = group_smem(EPG);
+  // groups per block: up to 256 threads and 48 KB of shared memory
+  static constexpr int gpb_pick() {
+    int g = 256 / GT;
+    if (g < 1) g = 1;
+    while (g > 1 && g * GROUP_SMEM > 48 * 1024) --g;
+    return g;
+  }
+  static constexpr int GPB = gpb_pick();
+  static constexpr int BLOCK = GPB * GT;
+  static constexpr int EPB = GPB * EPG;  // elements per block
+  static_assert(GPB <= 15, "named barrier ids");
+  static constexpr size_t smem_for(int) { return GPB * GROUP_SMEM; }
   static size_t smem_bytes() { return smem_for(EPB); }
 
   struct Smem {
-    R *cons, *prim, *fvol, *fsurf, *ffv, *alpha, *scale, *dsplit, *dhat, *invw, *trace;
+    R *cons, *prim, *fvol, *fsurf, *ffv, *trace, *alpha, *scale, *dsplit, *dhat, *invw;
     int *conforming;  // [el][face]: 1 = trace holds the neighbour's node, 0 = a mortar flux
+    // node records [el][node][v]
+    __device__ __forceinline__ R *c(int el, int n) const { return cons + (el * NN + n) * NV; }
+    __device__ __forceinline__ R *w(int el, int n) const { return prim + (el * NN + n) * NV; }
     // [el][face][t][v]
     __device__ __forceinline__ R *tr(int el, int face, int t) const {
       return trace + ((el * 2 * DIM + face) * NF + t) * NV;
     }
-    // [el][v][node]
-    __device__ __forceinline__ R &c(int el, int v, int n) const { return cons[(el * NV + v) * NN + n]; }
-    __device__ __forceinline__ R &w(int el, int v, int n) const { return prim[(el * NV + v) * NN + n]; }
     // [el][dir][slot][v]
     __device__ __forceinline__ R *vol(int el, int d, int slot) const {
       return fvol + ((el * DIM + d) * VOL_PER_DIR + slot) * NV;
@@ -165,11 +308,11 @@ struct FusedKernel {
     }
   };
 
-  __device__ __forceinline__ static void load_node(const Smem &s, int el, int n, R *u, R *w) {
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      u[v] = s.c(el, v, n);
-      w[v] = s.w(el, v, n);
+  __device__ __forceinline__ static void group_sync(int gid) {
+    if constexpr (WPG == 1) {
+      __syncwarp();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "r"(GT) : "memory");
     }
   }
 
@@ -179,20 +322,22 @@ struct FusedKernel {
     R f[NV];
     if constexpr (VOL == VOL_WEAK) {
       R u[NV], w[NV];
-      load_node(s, el, r, u, w);
+      lds_rec<NV>(s.c(el, r), u);
+      lds_rec<NV>(s.w(el, r), w);
       P::template flux<O>(u, w, f, p.pp);
     } else {
       const int t = r / NP, pp_ = r - (r / NP) * NP;
       int i, m;
       pair_nodes<N>(pp_, i, m);
+      const int ni = line_node<DIM, N, O>(t, i), nm = line_node<DIM, N, O>(t, m);
       R ui[NV], wi[NV], um[NV], wm[NV];
-      load_node(s, el, line_node<DIM, N, O>(t, i), ui, wi);
-      load_node(s, el, line_node<DIM, N, O>(t, m), um, wm);
+      lds_rec<NV>(s.c(el, ni), ui);
+      lds_rec<NV>(s.w(el, ni), wi);
+      lds_rec<NV>(s.c(el, nm), um);
+      lds_rec<NV>(s.w(el, nm), wm);
       two_point_flux_t<DIM, EQ, R, O, VFLUX>(ui, wi, um, wm, f, p.pp);
     }
-    R *dst = s.vol(el, O, r);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) dst[v] = f[v];
+    sts_rec<NV>(s.vol(el, O, r), f);
   }
 
   // surface item: face 2*O + side, face node t (neighbour data staged in phase A)
@@ -200,85 +345,80 @@ struct FusedKernel {
   __device__ __forceinline__ static void surface_item(const FusedParams<R> &p, const Smem &s, int el, int side,
                                                       int t) {
     const int face = 2 * O + side;
-    const R *src = s.tr(el, face, t);
     R f[NV];
+    lds_rec<NV>(s.tr(el, face, t), f);
     if (s.conforming[el * 2 * DIM + face]) {
       const int own = line_node<DIM, N, O>(t, side == 0 ? 0 : N - 1);
       R un[NV], wn[NV], uo[NV], wo[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) un[v] = src[v];
+      for (int v = 0; v < NV; ++v) un[v] = f[v];
       P::prim(un, wn, p.pp);
-      load_node(s, el, own, uo, wo);
+      lds_rec<NV>(s.c(el, own), uo);
+      lds_rec<NV>(s.w(el, own), wo);
       if (side == 0)
         two_point_flux<DIM, EQ, R, O>(p.surface_flux, un, wn, uo, wo, f, p.pp);
       else
         two_point_flux<DIM, EQ, R, O>(p.surface_flux, uo, wo, un, wn, f, p.pp);
-    } else {
-#pragma unroll
-      for (int v = 0; v < NV; ++v) f[v] = src[v];
     }
-    R *dst = s.surf(el, face, t);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) dst[v] = f[v];
+    sts_rec<NV>(s.surf(el, face, t), f);
   }
 
   // FV subcell item (shock capturing): flux between nodes a and a+1 of line t
   template <int O>
   __device__ __forceinline__ static void fv_item(const FusedParams<R> &p, const Smem &s, int el, int t, int a) {
     R ul[NV], wl[NV], ur[NV], wr[NV], f[NV];
-    load_node(s, el, line_node<DIM, N, O>(t, a), ul, wl);
-    load_node(s, el, line_node<DIM, N, O>(t, a + 1), ur, wr);
+    const int nl = line_node<DIM, N, O>(t, a), nr = line_node<DIM, N, O>(t, a + 1);
+    lds_rec<NV>(s.c(el, nl), ul);
+    lds_rec<NV>(s.w(el, nl), wl);
+    lds_rec<NV>(s.c(el, nr), ur);
+    lds_rec<NV>(s.w(el, nr), wr);
     two_point_flux<DIM, EQ, R, O>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
-    R *dst = s.fv(el, O, t, a);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) dst[v] = f[v];
+    sts_rec<NV>(s.fv(el, O, t, a), f);
   }
 
   __device__ __forceinline__ static void run(const FusedParams<R> &p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int epb = EPB;
+    const int gid = threadIdx.x / GT;  // group within the block
+    const int gt = threadIdx.x - gid * GT;
+    const int64_t e0 = ((int64_t)blockIdx.x * GPB + gid) * EPG;  // first element of the group
+    if (e0 >= p.nelements) return;  // whole groups leave together
+    const int ne = (int)min((int64_t)EPG, p.nelements - e0);
+
     Smem s;
-    s.cons = reinterpret_cast<R *>(smem_raw);
-    s.prim = s.cons + epb * NV * NN;
-    s.fvol = s.prim + epb * NV * NN;
-    s.fsurf = s.fvol + epb * DIM * VOL_PER_DIR * NV;
-    s.ffv = s.fsurf + epb * SURF_PER_EL * NV;
-    s.alpha = s.ffv + epb * DIM * FV_PER_DIR * NV;
-    s.scale = s.alpha + epb;
-    s.dsplit = s.scale + epb;
+    s.cons = reinterpret_cast<R *>(smem_raw + gid * GROUP_SMEM);
+    s.prim = s.cons + N_CONS;
+    s.fvol = s.prim + N_CONS;
+    s.fsurf = s.fvol + N_VOL;
+    s.ffv = s.fsurf + N_SURF;
+    s.trace = s.ffv + N_FV;
+    s.alpha = s.trace + N_TRACE;
+    s.scale = s.alpha + N_EL;
+    s.dsplit = s.scale + N_EL;
     s.dhat = s.dsplit + N * N;
     s.invw = s.dhat + N * N;
-    s.trace = s.invw + N;
-    s.conforming = reinterpret_cast<int *>(s.trace + epb * TRACE_PER_EL);
+    s.conforming = reinterpret_cast<int *>(s.dsplit + N_OPS);
 
-    const int64_t e0 = (int64_t)blockIdx.x * epb;
-    if (e0 >= p.nelements) return;
-    const int ne = (int)min((int64_t)epb, p.nelements - e0);
     const int mode = p.mode;
     const bool surface = (mode != MODE_VOLUME);
+    const bool vec = p.vec16 != 0;
+    const bool use_k = (mode == MODE_RK) && p.use_k;
 
-    // phase A: every global read of the tile is issued here.  Thread q < epb*NN
-    // owns node q for the whole kernel (its u and k stay in registers until
-    // the node phase); the other threads stage the neighbours' face nodes
-    // (or the mortar fluxes) of the tile's faces in shared memory.
-    const int tid = threadIdx.x;
-    const bool use_k = (mode == MODE_RK) && (p.rk_a != 0.0);
-    const int my_el = tid / NN, my_node = tid - (tid / NN) * NN;
-    const bool has_node = (tid < epb * NN) && (my_el < ne);
+    // phase A: every global read of the group is issued here.  Owner thread
+    // (el, node) keeps its node's u and k in registers until phase C; all
+    // threads stage the neighbours' face nodes (or the mortar fluxes) of the
+    // group's faces in shared memory.
+    const int my_el = gt / NN, my_node = gt - (gt / NN) * NN;
+    const bool has_node = (gt < EPG * NN) && (my_el < ne);
     const int64_t g0 = ((e0 + my_el) * NN + my_node) * NV;
     double ureg[NV], kreg[NV];
     if (has_node) {
-#pragma unroll
-      for (int v = 0; v < NV; ++v) ureg[v] = p.u_in[g0 + v];
-      if (use_k) {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) kreg[v] = p.k[g0 + v];
-      }
+      ldg_node<NV>(p.u_in + g0, ureg, vec);
+      if (use_k) ldg_node<NV>(p.k + g0, kreg, vec);
     }
     if (surface) {
       constexpr int PER_EL = 2 * DIM * NF;
       const int n_trace = ne * PER_EL;
-      for (int j = (tid - epb * NN + BLOCK) % BLOCK; j < n_trace; j += BLOCK) {
+      for (int j = gt; j < n_trace; j += GT) {
         const int el = j / PER_EL, r = j - (j / PER_EL) * PER_EL;
         const int face = r / NF, t = r - (r / NF) * NF;
         const int32_t nb = p.face_table[(e0 + el) * (2 * DIM) + face];
@@ -290,9 +430,12 @@ struct FusedKernel {
         } else {
           src = p.mortar_flux + ((int64_t)(-nb - 1) * NF + t) * NV;
         }
-        R *dst = s.tr(el, face, t);
+        double tv[NV];
+        ldg_node<NV>(src, tv, vec);
+        R tr[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) dst[v] = from_double<R>(src[v]);
+        for (int v = 0; v < NV; ++v) tr[v] = from_double<R>(tv[v]);
+        sts_rec<NV>(s.tr(el, face, t), tr);
         if (t == 0) s.conforming[el * 2 * DIM + face] = (nb >= 0);
       }
     }
@@ -301,40 +444,36 @@ struct FusedKernel {
 #pragma unroll
       for (int v = 0; v < NV; ++v) uu[v] = from_double<R>(ureg[v]);
       P::prim(uu, ww, p.pp);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        s.c(my_el, v, my_node) = uu[v];
-        s.w(my_el, v, my_node) = ww[v];
+      sts_rec<NV>(s.c(my_el, my_node), uu);
+      sts_rec<NV>(s.w(my_el, my_node), ww);
+      if (my_node == 0) {
+        if constexpr (VOL == VOL_SC) {
+          const double a = p.alpha[e0 + my_el];
+          s.alpha[my_el] = (fabs(a) <= p.atol) ? R(0) : from_double<R>(a);
+        }
+        // per-element factor of the node phase: -J^{-1} (rhs) or -J^{-1} dt (RK)
+        const double dte = p.dt_elem ? p.dt_elem[e0 + my_el] : p.dt;
+        const double f = -p.inv_jac[e0 + my_el] * (mode == MODE_RK ? dte : 1.0);
+        s.scale[my_el] = from_double<R>(f);
       }
     }
-    if (threadIdx.x < epb && threadIdx.x < ne) {
-      const int el = threadIdx.x;
-      if constexpr (VOL == VOL_SC) {
-        const double a = p.alpha[e0 + el];
-        s.alpha[el] = (fabs(a) <= p.atol) ? R(0) : from_double<R>(a);
-      }
-      // per-element factor of the node phase: -J^{-1} (rhs) or -J^{-1} dt (RK)
-      const double dte = p.dt_elem ? p.dt_elem[e0 + el] : p.dt;
-      const double f = -p.inv_jac[e0 + el] * (mode == MODE_RK ? dte : 1.0);
-      s.scale[el] = from_double<R>(f);
-    }
-    for (int q = threadIdx.x; q < N * N; q += BLOCK) {
+    for (int q = gt; q < N * N; q += GT) {
       s.dsplit[q] = p.dsplit[q];
       s.dhat[q] = p.dhat[q];
     }
-    if (threadIdx.x < N) s.invw[threadIdx.x] = p.invw[threadIdx.x];
-    __syncthreads();
+    if (gt < N) s.invw[gt] = p.invw[gt];
+    group_sync(gid);
 
-    // phase B: every flux of the tile, sections [volume | surface | FV],
+    // phase B: every flux of the group, sections [volume | surface | FV],
     // each ordered [direction][element][item] so warps stay on one direction
-    constexpr int PER_VOL = epb * VOL_PER_DIR;
-    constexpr int PER_SURF = epb * 2 * NF;
-    constexpr int PER_FV = epb * FV_PER_DIR;
-    constexpr int N_VOL = DIM * PER_VOL;
+    constexpr int PER_VOL = EPG * VOL_PER_DIR;
+    constexpr int PER_SURF = EPG * 2 * NF;
+    constexpr int PER_FV = EPG * FV_PER_DIR;
+    constexpr int NVOL_ITEMS = DIM * PER_VOL;
     const int n_surf = surface ? DIM * PER_SURF : 0;
-    const int n_all = N_VOL + n_surf + DIM * PER_FV;
-    for (int w = threadIdx.x; w < n_all; w += BLOCK) {
-      if (w < N_VOL) {
+    const int n_all = NVOL_ITEMS + n_surf + DIM * PER_FV;
+    for (int w = gt; w < n_all; w += GT) {
+      if (w < NVOL_ITEMS) {
         const int dir = w / PER_VOL;
         const int r0 = w - dir * PER_VOL;
         const int el = r0 / VOL_PER_DIR, r = r0 - (r0 / VOL_PER_DIR) * VOL_PER_DIR;
@@ -342,8 +481,8 @@ struct FusedKernel {
         if (dir == 0) volume_item<0>(p, s, el, r);
         if constexpr (DIM > 1) if (dir == 1) volume_item<1>(p, s, el, r);
         if constexpr (DIM > 2) if (dir == 2) volume_item<2>(p, s, el, r);
-      } else if (w < N_VOL + n_surf) {
-        const int w2 = w - N_VOL;
+      } else if (w < NVOL_ITEMS + n_surf) {
+        const int w2 = w - NVOL_ITEMS;
         const int dir = w2 / PER_SURF;
         const int r0 = w2 - dir * PER_SURF;
         const int el = r0 / (2 * NF);
@@ -354,7 +493,7 @@ struct FusedKernel {
         if constexpr (DIM > 1) if (dir == 1) surface_item<1>(p, s, el, side, t);
         if constexpr (DIM > 2) if (dir == 2) surface_item<2>(p, s, el, side, t);
       } else if constexpr (VOL == VOL_SC) {
-        const int w2 = w - N_VOL - n_surf;
+        const int w2 = w - NVOL_ITEMS - n_surf;
         const int dir = w2 / PER_FV;
         const int r0 = w2 - dir * PER_FV;
         const int el = r0 / FV_PER_DIR;
@@ -366,134 +505,144 @@ struct FusedKernel {
         if constexpr (DIM > 2) if (dir == 2) fv_item<2>(p, s, el, t, a);
       }
     }
-    __syncthreads();
+    group_sync(gid);
 
     // phase C: the thread that loaded node q finishes it
-    if (has_node) {
-      const int el = my_el, node = my_node;
-      int coord[3] = {0, 0, 0}, tface[3] = {0, 0, 0};
-      {
-        int qq = node;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          coord[d] = qq % N;
-          qq /= N;
-        }
-        if constexpr (DIM == 2) {
-          tface[0] = coord[1];
-          tface[1] = coord[0];
-        } else if constexpr (DIM == 3) {
-          tface[0] = coord[1] + N * coord[2];
-          tface[1] = coord[0] + N * coord[2];
-          tface[2] = coord[0] + N * coord[1];
-        }
-      }
-      R acc[NV];
-#pragma unroll
-      for (int v = 0; v < NV; ++v) acc[v] = R(0);
+    if (!has_node) return;
+    const int el = my_el, node = my_node;
+    int coord[3] = {0, 0, 0}, tface[3] = {0, 0, 0};
+    {
+      int qq = node;
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
-        const int ci = coord[d];
-        if constexpr (VOL == VOL_WEAK) {
-          constexpr int strides[3] = {1, N, N * N};
-          const int n0 = node - ci * strides[d];
-#pragma unroll
-          for (int m = 0; m < N; ++m) {
-            const R dm = s.dhat[ci * N + m];
-            const R *F = s.vol(el, d, n0 + m * strides[d]);
-#pragma unroll
-            for (int v = 0; v < NV; ++v) acc[v] += dm * F[v];
-          }
-        } else {
-#pragma unroll
-          for (int m = 0; m < N; ++m) {
-            if (m == ci) continue;
-            const R dm = s.dsplit[ci * N + m];
-            const R *F = s.vol(el, d, tface[d] * NP + pair_index<N>(ci, m));
-#pragma unroll
-            for (int v = 0; v < NV; ++v) acc[v] += dm * F[v];
-          }
-        }
+        coord[d] = qq % N;
+        qq /= N;
       }
-      if constexpr (VOL == VOL_SC) {
-        const R alpha = s.alpha[el];
-        if (alpha != R(0)) {
-          R fv[NV];
-#pragma unroll
-          for (int v = 0; v < NV; ++v) fv[v] = R(0);
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) {
-            const int ci = coord[d];
-            const R iw = s.invw[ci];
-            if (ci + 1 < N) {
-              const R *F = s.fv(el, d, tface[d], ci);
-#pragma unroll
-              for (int v = 0; v < NV; ++v) fv[v] += iw * F[v];
-            }
-            if (ci > 0) {
-              const R *F = s.fv(el, d, tface[d], ci - 1);
-#pragma unroll
-              for (int v = 0; v < NV; ++v) fv[v] -= iw * F[v];
-            }
-          }
-#pragma unroll
-          for (int v = 0; v < NV; ++v) acc[v] = (R(1) - alpha) * acc[v] + alpha * fv[v];
-        }
+      if constexpr (DIM == 2) {
+        tface[0] = coord[1];
+        tface[1] = coord[0];
+      } else if constexpr (DIM == 3) {
+        tface[0] = coord[1] + N * coord[2];
+        tface[1] = coord[0] + N * coord[2];
+        tface[2] = coord[0] + N * coord[1];
       }
-      if (surface) {
+    }
+    R acc[NV];
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          if (coord[d] == 0) {
-            const R *F = s.surf(el, 2 * d, tface[d]);
+    for (int v = 0; v < NV; ++v) acc[v] = R(0);
 #pragma unroll
-            for (int v = 0; v < NV; ++v) acc[v] -= p.lhat_l * F[v];
-          }
-          if (coord[d] == N - 1) {
-            const R *F = s.surf(el, 2 * d + 1, tface[d]);
+    for (int d = 0; d < DIM; ++d) {
+      const int ci = coord[d];
+      if constexpr (VOL == VOL_WEAK) {
+        constexpr int strides[3] = {1, N, N * N};
+        const int n0 = node - ci * strides[d];
 #pragma unroll
-            for (int v = 0; v < NV; ++v) acc[v] += p.lhat_r * F[v];
-          }
-        }
-      }
-      if (mode == MODE_VOLUME) {
+        for (int m = 0; m < N; ++m) {
+          const R dm = s.dhat[ci * N + m];
+          R F[NV];
+          lds_rec<NV>(s.vol(el, d, n0 + m * strides[d]), F);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) p.out[g0 + v] = to_double(acc[v]);
-      } else if constexpr (sizeof(R) == sizeof(double)) {
-        const double sc = -p.inv_jac[e0 + el];
-        const double dte = p.dt_elem ? p.dt_elem[e0 + el] : p.dt;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          const double du = double(acc[v]) * sc;
-          if (mode == MODE_RHS) {
-            p.out[g0 + v] = du;
-          } else {
-            const double kk = (use_k ? p.rk_a * kreg[v] : 0.0) + dte * du;
-            p.k[g0 + v] = kk;
-            p.out[g0 + v] = ureg[v] + p.rk_b * kk;
-          }
+          for (int v = 0; v < NV; ++v) acc[v] += dm * F[v];
         }
       } else {
-        // mixed precision: scale in FP32, widen exactly, accumulate the RK
-        // register and the state in FP64 (two FMAs on the FP64 pipe)
-        const R sc = s.scale[el];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          const double dd = to_double(acc[v] * sc);
-          if (mode == MODE_RHS) {
-            p.out[g0 + v] = dd;
-          } else {
-            const double kk = use_k ? fma(p.rk_a, kreg[v], dd) : dd;
-            p.k[g0 + v] = kk;
-            p.out[g0 + v] = fma(p.rk_b, kk, ureg[v]);
-          }
+        for (int m = 0; m < N; ++m) {
+          if (m == ci) continue;
+          const R dm = s.dsplit[ci * N + m];
+          R F[NV];
+          lds_rec<NV>(s.vol(el, d, tface[d] * NP + pair_index<N>(ci, m)), F);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) acc[v] += dm * F[v];
         }
       }
+    }
+    if constexpr (VOL == VOL_SC) {
+      const R alpha = s.alpha[el];
+      if (alpha != R(0)) {
+        R fv[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) fv[v] = R(0);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const int ci = coord[d];
+          const R iw = s.invw[ci];
+          if (ci + 1 < N) {
+            R F[NV];
+            lds_rec<NV>(s.fv(el, d, tface[d], ci), F);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) fv[v] += iw * F[v];
+          }
+          if (ci > 0) {
+            R F[NV];
+            lds_rec<NV>(s.fv(el, d, tface[d], ci - 1), F);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) fv[v] -= iw * F[v];
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[v] = (R(1) - alpha) * acc[v] + alpha * fv[v];
+      }
+    }
+    if (surface) {
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        if (coord[d] == 0) {
+          R F[NV];
+          lds_rec<NV>(s.surf(el, 2 * d, tface[d]), F);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) acc[v] -= p.lhat_l * F[v];
+        }
+        if (coord[d] == N - 1) {
+          R F[NV];
+          lds_rec<NV>(s.surf(el, 2 * d + 1, tface[d]), F);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) acc[v] += p.lhat_r * F[v];
+        }
+      }
+    }
+    double o[NV], kk[NV];
+    if (mode == MODE_VOLUME) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) o[v] = to_double(acc[v]);
+      stg_node<NV>(p.out + g0, o, vec);
+    } else if constexpr (sizeof(R) == sizeof(double)) {
+      const double sc = -p.inv_jac[e0 + el];
+      const double dte = p.dt_elem ? p.dt_elem[e0 + el] : p.dt;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const double du = double(acc[v]) * sc;
+        if (mode == MODE_RHS) {
+          o[v] = du;
+        } else {
+          kk[v] = (use_k ? p.rk_a * kreg[v] : 0.0) + dte * du;
+          o[v] = ureg[v] + p.rk_b * kk[v];
+        }
+      }
+      if (mode == MODE_RK) stg_node<NV>(p.k + g0, kk, vec);
+      stg_node<NV>(p.out + g0, o, vec);
+    } else {
+      // mixed precision: scale in FP32, widen exactly, accumulate the RK
+      // register and the state in FP64 (two FMAs on the FP64 pipe)
+      const R sc = s.scale[el];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const double dd = to_double(acc[v] * sc);
+        if (mode == MODE_RHS) {
+          o[v] = dd;
+        } else {
+          kk[v] = use_k ? fma(p.rk_a, kreg[v], dd) : dd;
+          o[v] = fma(p.rk_b, kk[v], ureg[v]);
+        }
+      }
+      if (mode == MODE_RK) stg_node<NV>(p.k + g0, kk, vec);
+      stg_node<NV>(p.out + g0, o, vec);
     }
   }
 };
 
 template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX>
-__global__ void __launch_bounds__(256) dg_fused_kernel(const FusedParams<R> p) {
+__global__ void __launch_bounds__(FusedKernel<DIM, N, EQ, R, VOL, VFLUX>::BLOCK)
+    dg_fused_kernel(const FusedParams<R> p) {
   FusedKernel<DIM, N, EQ, R, VOL, VFLUX>::run(p);
 }
 

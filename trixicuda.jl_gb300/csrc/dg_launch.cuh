@@ -29,6 +29,9 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   p.rk_a = h.rk_a;
   p.rk_b = h.rk_b;
   p.dt = h.dt;
+  p.use_k = (h.rk_a != 0.0);
+  const uintptr_t addr_bits = (uintptr_t)h.u_in | (uintptr_t)h.out | (uintptr_t)h.k | (uintptr_t)h.mortar_flux;
+  p.vec16 = (addr_bits & 15u) == 0;
   p.atol = h.atol;
   p.pp.gamma = R(h.gamma);
   p.pp.gm1 = R(h.gamma - 1.0);
@@ -45,7 +48,7 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   for (int i = 0; i < NMAXT; ++i) p.invw[i] = R(i < N ? h.invw[i] : 0.0);
   p.lhat_l = R(h.lhat_l);
   p.lhat_r = R(h.lhat_r);
-  const int epb = K::EPB;  // compile-time tile size (see FusedKernel::epb_pick)
+  const int epb = K::EPB;  // compile-time tile size (see FusedKernel::gpb_pick)
   p.epb = epb;
   const int block = K::BLOCK;
   const size_t smem = K::smem_bytes();

@@ -50,14 +50,14 @@ __device__ __forceinline__ double dev_fmax(double x, double y) { return fmax(x, 
 __device__ __forceinline__ float dev_fmax(float x, float y) { return fmaxf(x, y); }
 
 // Ismail-Roe logarithmic mean (x - y)/(log x - log y) and its inverse.
-// With s = x + y and u = ((x - y)/s)^2, ln_mean = (s/2) / g(u) where
-// g(u) = artanh(f)/f = 1 + u/3 + u^2/5 + u^3/7 + ... (Ismail & Roe 2009).
-// Below the threshold the series is used: 1/g(u) = 1 - u/3 - 4u^2/45 -
-// 44u^3/945 + O(u^4) for the mean and g(u) itself for the inverse, so each
+// With s = x + y, f = (x - y)/s and u = f^2, ln_mean = (s/2) / g(u) where
+// g(u) = artanh(f)/f = sum_k u^k/(2k+1) (Ismail & Roe 2009).  Below the
+// threshold the series are used: h(u) = 1/g(u) = 1 - u/3 - 4u^2/45 - 44u^3/945
+// + O(u^4) (the reversion of g) for the mean and g(u) for the inverse, so each
 // mean costs one reciprocal of s; above it, log(x/y) is evaluated.  The
-// threshold is 1e-4 in FP64 (truncation ~1e-18) and 1e-2 in FP32
-// (truncation ~1e-10, and log(x/y) is only formed for ratios above ~1.2,
-// where FP32 cancellation is harmless).
+// threshold is 1e-4 in FP64 (truncation ~3e-18) and 1e-2 in FP32 (truncation
+// ~3e-10, and log(x/y) is only formed for ratios above ~1.2, where FP32
+// cancellation is harmless).  The adjoint differentiates the same branches.
 template <typename R>
 struct LnMeanThreshold;
 template <>
@@ -69,13 +69,27 @@ struct LnMeanThreshold<float> {
   static constexpr float value = 1.0e-2f;
 };
 
+// h(u) = 1/g(u) and g(u) through u^3 (Horner), and their derivatives in u
+template <typename R>
+__device__ __forceinline__ R series_h(R u) {
+  return R(1) + u * (R(-1.0 / 3.0) + u * (R(-4.0 / 45.0) + u * R(-44.0 / 945.0)));
+}
+template <typename R>
+__device__ __forceinline__ R series_g(R u) {
+  return R(1) + u * (R(1.0 / 3.0) + u * (R(1.0 / 5.0) + u * R(1.0 / 7.0)));
+}
+__device__ __forceinline__ double series_h_du(double u) {
+  return -1.0 / 3.0 + u * (-8.0 / 45.0 + u * (-132.0 / 945.0));
+}
+__device__ __forceinline__ double series_g_du(double u) { return 1.0 / 3.0 + u * (2.0 / 5.0 + u * (3.0 / 7.0)); }
+
 template <typename R>
 __device__ __forceinline__ R ln_mean_series(R s, R u) {
-  return R(0.5) * s * (R(1) + u * (R(-1.0 / 3.0) + u * (R(-4.0 / 45.0) + u * R(-44.0 / 945.0))));
+  return R(0.5) * s * series_h(u);
 }
 template <typename R>
 __device__ __forceinline__ R inv_ln_mean_series(R r, R u) {
-  return R(2) * r * (R(1) + u * (R(1.0 / 3.0) + u * (R(1.0 / 5.0) + u * R(1.0 / 7.0))));
+  return R(2) * r * series_g(u);
 }
 
 template <typename R>

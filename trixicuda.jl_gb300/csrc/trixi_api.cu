@@ -945,6 +945,15 @@ struct trixi_batch {
   cudaStream_t capture_stream = nullptr;  // graphs are recorded here (the caller's stream may be the legacy one)
   const double *graph_u = nullptr;
   const double *graph_k = nullptr;
+  // The groups of a step are independent chains of 5 stage launches, so the
+  // step graph runs them as parallel branches (fork/join through events on
+  // internal streams).  The branch count is picked by timing candidate graphs
+  // once, on copies of the state, at the first graph build.
+  int branches = 0;                        // 0: not tuned yet
+  std::vector<int> tune_candidates;        // branch counts timed by the tuner
+  std::vector<double> tune_ms;             // their ms per step
+  std::vector<cudaStream_t> branch_streams;
+  std::vector<cudaEvent_t> branch_events;  // [0] fork, [1 + j] join of branch j
   std::string last_error;
 };
 
@@ -997,6 +1006,156 @@ int batch_step(trixi_batch *b, double *from, double *to, double *k, cudaStream_t
     }
     std::swap(cur, nxt);
   }
+  return TRIXI_OK;
+}
+
+// groups of each branch: longest-processing-time assignment by state size
+std::vector<std::vector<int>> branch_groups(const trixi_batch *b, int nbranch) {
+  std::vector<int> order(b->groups.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return b->groups[x].nvalues > b->groups[y].nvalues; });
+  std::vector<std::vector<int>> out((size_t)nbranch);
+  std::vector<int64_t> load((size_t)nbranch, 0);
+  for (int gi : order) {
+    const size_t j = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+    out[j].push_back(gi);
+    load[j] += b->groups[(size_t)gi].nvalues;
+  }
+  return out;
+}
+
+int ensure_branch_resources(trixi_batch *b, int nbranch) {
+  while ((int)b->branch_streams.size() < nbranch) {
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    b->branch_streams.push_back(st);
+  }
+  while ((int)b->branch_events.size() < nbranch + 1) {
+    cudaEvent_t ev = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    b->branch_events.push_back(ev);
+  }
+  return TRIXI_OK;
+}
+
+// One full step as `nbranch` parallel chains forked from and joined back into
+// stream s (inside a capture on s this records a graph with parallel branches).
+int batch_step_branched(trixi_batch *b, double *from, double *to, double *k, cudaStream_t s, int nbranch) {
+  if (nbranch <= 1) return batch_step(b, from, to, k, s);
+  if (int r = ensure_branch_resources(b, nbranch)) return r;
+  const auto assign = branch_groups(b, nbranch);
+  cudaError_t e = cudaEventRecord(b->branch_events[0], s);
+  if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+  for (int j = 0; j < nbranch; ++j) {
+    cudaStream_t bs = b->branch_streams[(size_t)j];
+    e = cudaStreamWaitEvent(bs, b->branch_events[0], 0);
+    if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    for (int gi : assign[(size_t)j]) {
+      auto &g = b->groups[(size_t)gi];
+      double *cur = from, *nxt = to;
+      for (int st = 0; st < 5; ++st) {
+        FusedHost save = g.h->fused;
+        g.h->fused.dt_elem = g.d_dt;
+        int r = run_rhs(g.h, MODE_RK, cur + g.value_offset, nxt + g.value_offset, k + g.value_offset, kCK_A[st],
+                        kCK_B[st], 0.0, bs);
+        g.h->fused = save;
+        if (r) return batch_fail(b, r, g.h->last_error);
+        std::swap(cur, nxt);
+      }
+    }
+    e = cudaEventRecord(b->branch_events[(size_t)j + 1], bs);
+    if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+    e = cudaStreamWaitEvent(s, b->branch_events[(size_t)j + 1], 0);
+    if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return TRIXI_OK;
+}
+
+// Captures one step from `from` to `to` with `nbranch` branches and instantiates it.
+int capture_step(trixi_batch *b, double *from, double *to, double *k, int nbranch, cudaGraphExec_t *out) {
+  cudaGraph_t graph = nullptr;
+  cudaStream_t cs = b->capture_stream;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+  int r = batch_step_branched(b, from, to, k, cs, nbranch);
+  e = cudaStreamEndCapture(cs, &graph);
+  if (r) {
+    if (graph) cudaGraphDestroy(graph);
+    return r;
+  }
+  if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+  return TRIXI_OK;
+}
+
+// Branch-count tuner: times one step graph per candidate on copies of u and k
+// (the caller's data is not modified) and keeps the fastest.
+int tune_branches(trixi_batch *b, const double *u, const double *k, cudaStream_t s) {
+  const int G = (int)b->groups.size();
+  std::vector<int> cand;
+  for (int c : {1, 2, 4, 8, 16})
+    if (c <= G) cand.push_back(c);
+  if (G > 1 && std::find(cand.begin(), cand.end(), G) == cand.end() && G <= 32) cand.push_back(G);
+  b->tune_candidates = cand;
+  b->tune_ms.assign(cand.size(), 0.0);
+  if (cand.size() == 1) {
+    b->branches = 1;
+    return TRIXI_OK;
+  }
+  const size_t bytes = sizeof(double) * (size_t)b->total_values;
+  double *tu = nullptr, *tk = nullptr;
+  if (cudaMalloc(&tu, bytes) != cudaSuccess || cudaMalloc(&tk, bytes) != cudaSuccess) {
+    if (tu) cudaFree(tu);
+    cudaGetLastError();
+    b->branches = std::min(G, 4);  // no room for the copies: a fixed choice
+    return TRIXI_OK;
+  }
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  int best = 1;
+  double best_ms = 0.0;
+  int status = TRIXI_OK;
+  for (size_t ci = 0; ci < cand.size() && status == TRIXI_OK; ++ci) {
+    cudaMemcpyAsync(tu, u, bytes, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(tk, k, bytes, cudaMemcpyDeviceToDevice, s);
+    cudaGraphExec_t ge[2] = {nullptr, nullptr};
+    status = capture_step(b, tu, b->d_scratch, tk, cand[ci], &ge[0]);
+    if (status == TRIXI_OK) status = capture_step(b, b->d_scratch, tu, tk, cand[ci], &ge[1]);
+    if (status == TRIXI_OK) {
+      const int reps = 4;
+      cudaGraphLaunch(ge[0], s);
+      cudaGraphLaunch(ge[1], s);
+      cudaEventRecord(t0, s);
+      for (int r = 0; r < reps; ++r) {
+        cudaGraphLaunch(ge[0], s);
+        cudaGraphLaunch(ge[1], s);
+      }
+      cudaEventRecord(t1, s);
+      cudaError_t e = cudaEventSynchronize(t1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t0, t1);
+      if (e != cudaSuccess) status = batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
+      b->tune_ms[ci] = ms / (2.0 * reps);
+      if (ci == 0 || b->tune_ms[ci] < best_ms) {
+        best = cand[ci];
+        best_ms = b->tune_ms[ci];
+      }
+    }
+    for (auto g : ge)
+      if (g) cudaGraphExecDestroy(g);
+  }
+  cudaStreamSynchronize(s);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(tu);
+  cudaFree(tk);
+  if (status != TRIXI_OK) return status;
+  b->branches = best;
   return TRIXI_OK;
 }
 
@@ -1118,7 +1277,22 @@ int trixi_batch_destroy(trixi_batch *b) {
   }
   if (b->d_scratch) cudaFree(b->d_scratch);
   if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+  for (auto st : b->branch_streams) cudaStreamDestroy(st);
+  for (auto ev : b->branch_events) cudaEventDestroy(ev);
   delete b;
+  return TRIXI_OK;
+}
+
+int trixi_batch_tuning(const trixi_batch *b, int *branches, int *candidates, double *ms_per_step, int64_t max,
+                       int64_t *count) {
+  if (!b) return batch_fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "batch is null");
+  if (branches) *branches = b->branches;
+  const int64_t n = (int64_t)b->tune_candidates.size();
+  if (count) *count = n;
+  for (int64_t i = 0; i < n && i < max; ++i) {
+    if (candidates) candidates[i] = b->tune_candidates[(size_t)i];
+    if (ms_per_step) ms_per_step[i] = b->tune_ms[(size_t)i];
+  }
   return TRIXI_OK;
 }
 
@@ -1184,22 +1358,10 @@ int trixi_batch_rk_steps(trixi_batch *b, double *u, double *k, const double *dt_
       cudaError_t e = launch_fused(g.h->dim, g.h->N, g.h->eq, g.h->vol, g.h->vflux, g.h->mixed, f, s);
       if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
     }
-    for (int parity = 0; parity < 2; ++parity) {
-      cudaGraph_t graph = nullptr;
-      cudaStream_t cs = b->capture_stream;
-      cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
-      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
-      int r = batch_step(b, bufs[parity], bufs[1 - parity], k, cs);
-      e = cudaStreamEndCapture(cs, &graph);
-      if (r) {
-        if (graph) cudaGraphDestroy(graph);
-        return r;
-      }
-      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
-      e = cudaGraphInstantiate(&b->step_graph[parity], graph, 0);
-      cudaGraphDestroy(graph);
-      if (e != cudaSuccess) return batch_fail(b, TRIXI_ERR_CUDA, cudaGetErrorString(e));
-    }
+    if (b->branches == 0)
+      if (int r = tune_branches(b, u, k, s)) return r;
+    for (int parity = 0; parity < 2; ++parity)
+      if (int r = capture_step(b, bufs[parity], bufs[1 - parity], k, b->branches, &b->step_graph[parity])) return r;
     b->graph_u = u;
     b->graph_k = k;
   }

@@ -133,6 +133,8 @@ SIGNATURES = {
     "trixi_batch_rk_steps": (C.c_int, [_VP, _DP, _DP, C.POINTER(C.c_double), _I64, _I, _VP]),
     "trixi_batch_handle": (C.c_int, [_VP, _I64, C.POINTER(C.c_void_p)]),
     "trixi_batch_last_error": (C.c_int, [_VP, C.c_char_p, C.c_size_t]),
+    "trixi_batch_tuning": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double), _I64,
+                                     C.POINTER(C.c_int64)]),
     "trixi_integrate": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _VP]),
     "trixi_integrate_noalloc": (C.c_int, [_I, _I, _I, C.c_double, _VP, _VP, _VP, _I64, _I, _VP, _VP]),
     "trixi_calc_error_norms": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _D,

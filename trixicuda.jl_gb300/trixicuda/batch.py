@@ -133,6 +133,17 @@ class BatchedSemidiscretizationGPU:
                                                     dt.ctypes.data_as(C.POINTER(C.c_double)), int(nsteps),
                                                     int(bool(use_graph)), _stream_handle(stream)), self._h)
 
+    def tuning(self):
+        """(chosen branch count, {candidate branch count: ms per step}) of the
+        step-graph tuner; (0, {}) before the first graph build."""
+        br = C.c_int()
+        cand = (C.c_int * 16)()
+        ms = (C.c_double * 16)()
+        cnt = C.c_int64()
+        _batch_check(self._lib.trixi_batch_tuning(self._h, C.byref(br), cand, ms, 16, C.byref(cnt)), self._h)
+        n = min(int(cnt.value), 16)
+        return int(br.value), {int(cand[i]): float(ms[i]) for i in range(n)}
+
     def stable_dt(self, u, cfl=0.5):
         """Per-instance CFL time step cfl * 2 / (N * max J^{-1} sum_d lambda_d)."""
         torch = _torch()
