@@ -120,6 +120,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _tile_report(semi):
+    """The fused kernel's tile chosen by the tuner, with the tuner's table."""
+    import trixicuda as T
+
+    (epg, wpg, gpb), table = T.tile(semi)
+    return {"elements_per_group": epg, "warps_per_group": wpg, "groups_per_block": gpb,
+            "tuner_us_per_launch": {f"{w}x{g}": round(ms * 1e3, 2) for (w, g), ms in sorted(table.items())}}
+
+
 def time_gpu_path(precision, steps, warmup, device, flush):
     """Device-timed CK2N54 steps through trixi_rk_stage (ping-pong buffers).
     Returns per-step ms, per-launch ms of the fused kernel, the semi, final u."""
@@ -132,6 +141,7 @@ def time_gpu_path(precision, steps, warmup, device, flush):
     semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, precision=precision)
     dt = stable_dt(semi)
     u0 = semi.compute_coefficients()
+    T.autotune(u0, semi)  # tile tuner (setup, outside the timed region)
     bufs = [u0.clone(), torch.empty_like(u0)]
     k = torch.zeros_like(u0)
     stream = torch.cuda.current_stream()
@@ -199,13 +209,22 @@ def batched_path(precision, steps, warmup, device, flush, n=512):
     step_bytes = nvals * 8 * (3 + 4 * 4)
     mean_ms = statistics.mean(ms)
     branches, tune_ms = batch.tuning()
+    kinds = {}
+    for i, pb in enumerate(problems):
+        kinds.setdefault(batch.group_of(i), pb.label.split("-")[0] + f"-p{pb.solver.polydeg}")
+    group_tiles = []
+    for gi, ((epg, wpg, gpb), table) in enumerate(batch.group_tiles()):
+        group_tiles.append({"kind": kinds.get(gi, "?"), "tile": f"{wpg}x{gpb}", "elements_per_group": epg,
+                            "best_us": round(min(table.values()) * 1e3, 2) if table else None,
+                            "worst_us": round(max(table.values()) * 1e3, 2) if table else None})
     return {"instances": n, "groups": batch.ngroups, "dofs": dofs, "values": nvals,
             "state_mb_fp64": nvals * 8 / 1e6, "ms_per_step": mean_ms,
             "dof_updates_per_s": 5 * dofs / (mean_ms * 1e-3),
             "instance_steps_per_s": n / (mean_ms * 1e-3),
             "achieved_gbs": step_bytes / (mean_ms * 1e-3) / 1e9, "setup_s": setup_s,
             "graph": "one CUDA graph per step: groups as parallel branches, 5 stage launches each",
-            "tuned_branches": branches, "tuner_ms_per_step": {str(b): v for b, v in tune_ms.items()}}
+            "tuned_branches": branches, "tuner_ms_per_step": {str(b): v for b, v in tune_ms.items()},
+            "group_tiles": group_tiles}
 
 
 def adjoint_path(device, nsteps=200, snapshots=15, ndirs=4):
@@ -282,6 +301,7 @@ def e2e_path(precision, steps, warmup, device):
     mesh, eq, ic, solver = build_problem(precision)
     semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, precision=precision)
     dt = stable_dt(semi)
+    T.autotune(semi.compute_coefficients(), semi)  # setup, outside the timed region
     host = torch.from_numpy(semi.compute_coefficients_host()).pin_memory()
     u = torch.empty(host.shape, dtype=torch.float64, device=device)
     k = torch.zeros_like(u)
@@ -469,6 +489,7 @@ def main():
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "kernel": "dg_fused_kernel (RK stage)", "algorithmic_bytes_per_launch": mean_bytes,
                      "mean_launch_ms": mean_launch_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        "tiles": {"mixed": _tile_report(semi), "fp64": _tile_report(semi64)},
         "fp64": {"value": value64, "unit": METRIC, "ms_per_step": statistics.mean(step64),
                  "mean_launch_ms": statistics.mean(launch64),
                  "fp64_fma_peak_tflops": fp64_peak.value / 1e12, "fp32_fma_peak_tflops": fp32_peak.value / 1e12},

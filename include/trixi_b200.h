@@ -162,6 +162,21 @@ int trixi_rk_stage(trixi_handle *h, double *u_out, const double *u_in, double *k
 int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt,
                    int64_t nsteps, void *stream);
 
+/* Tile tuner (no counterpart in the reference).  The fused kernel's tile --
+ * warps per element group and groups per block, i.e. threads per node and
+ * elements per block -- is a launch parameter.  trixi_autotune times the RK
+ * stage launch for every valid tile on the state u (read only; outputs go to
+ * temporary buffers) and keeps the fastest for this handle; results do not
+ * depend on the tile.  Synchronous.  trixi_tile reports the elements per
+ * group (compile time), the tile in use, and the tuner's candidates with
+ * their ms per launch (up to `max`; *count = number measured). */
+int trixi_autotune(trixi_handle *h, const double *u, void *stream);
+/* Sets the tile by hand (wpg warps per group, gpb groups per block, at most 16
+ * warps per block); wpg = gpb = 0 restores the compile-time default. */
+int trixi_set_tile(trixi_handle *h, int wpg, int gpb);
+int trixi_tile(trixi_handle *h, int *epg, int *wpg, int *gpb, int *cand_wpg, int *cand_gpb, double *cand_ms,
+               int64_t max, int64_t *count);
+
 /* Stage entry points with the reference's stage split (the de-facto API used
  * by the reference tests, src/solvers/dg.jl:181-301, docs/src/reference.md:14-30).
  * They compute in FP64 and fill the library-owned containers below. */
@@ -299,8 +314,9 @@ int trixi_batch_layout(const trixi_batch *b, int64_t *value_offsets, int64_t *nv
 int trixi_batch_rhs(trixi_batch *b, double *du, const double *u, void *stream);
 /* nsteps CarpenterKennedy2N54 steps; instance i uses dt_per_instance[i] (host
  * array).  use_graph != 0 replays a captured CUDA graph of the whole step, in
- * which the groups run as parallel branches; the first graph build tunes the
- * branch count by timing candidate graphs on copies of u and k. */
+ * which the groups run as parallel branches; the first graph build tunes, on
+ * copies of u and k, the tile of every group's kernel (as trixi_autotune) and
+ * then the branch count. */
 int trixi_batch_rk_steps(trixi_batch *b, double *u, double *k, const double *dt_per_instance, int64_t nsteps,
                          int use_graph, void *stream);
 /* The tuner's choice and its timings: *branches (0 before the first graph

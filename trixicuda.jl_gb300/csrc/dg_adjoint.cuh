@@ -239,7 +239,7 @@ struct AdjointKernel {
   static constexpr int ITEMS_PER_EL = DIM * VOL_PER_DIR + 2 * DIM * NF;
   static constexpr size_t smem_for(int epb) {
     return sizeof(double) * ((size_t)epb * (3 * NV * NN + NN + (DIM * VOL_PER_DIR * VOL_BAR + 2 * DIM * NF) * NV) +
-                             epb);
+                             epb + N * N);
   }
   static constexpr int epb_pick() {
     int e = (2 * BLOCK + ITEMS_PER_EL - 1) / ITEMS_PER_EL;
@@ -260,6 +260,10 @@ struct AdjointKernel {
     double *s_sb = s_vb + epb * DIM * VOL_PER_DIR * VOL_BAR * NV;  // [el][face][t][v]
     double *s_ij = s_sb + epb * 2 * DIM * NF * NV;
     double *s_ir = s_ij + epb;                                 // 1/rho per node [el][n]
+    double *s_D = s_ir + epb * NN;                             // D_hat (weak form) or D_split, row-major
+    // the operator is read with a different (i, m) per lane: shared memory, not
+    // the parameter (constant) bank, which serialises divergent reads
+    for (int q = threadIdx.x; q < N * N; q += BLOCK) s_D[q] = (VOL == VOL_WEAK) ? p.dhat[q] : p.dsplit[q];
     const int64_t e0 = (int64_t)blockIdx.x * epb;
     if (e0 >= p.nelements) return;
     const int ne = (int)min((int64_t)epb, p.nelements - e0);
@@ -380,6 +384,7 @@ struct AdjointKernel {
   __device__ __forceinline__ static void vol_item(const AdjointParams &p, int el, int r, double *s_u, double *s_w,
                                                   double *s_l, double *s_vb, const double *s_ij, const double *s_ir) {
     const double scale = -s_ij[el];
+    const double *s_D = s_ir + EPB * NN;
     if constexpr (VOL == VOL_WEAK) {
       // du_i = -J^{-1} sum_m dhat[i,m] f(u_m): cotangent of f(u_r) gathers the column r of dhat
       const int ci = (r / ipow(N, O)) % N;
@@ -390,7 +395,7 @@ struct AdjointKernel {
       for (int v = 0; v < NV; ++v) {
         double a = 0.0;
 #pragma unroll
-        for (int i = 0; i < N; ++i) a += p.dhat[i * N + ci] * s_l[(el * NV + v) * NN + n0 + i * stride];
+        for (int i = 0; i < N; ++i) a += s_D[i * N + ci] * s_l[(el * NV + v) * NN + n0 + i * stride];
         g[v] = scale * a;
       }
       double u[NV], w[NV], ub[NV];
@@ -408,7 +413,7 @@ struct AdjointKernel {
       int i, m;
       pair_nodes<N>(pp_, i, m);
       const int ni = line_node<DIM, N, O>(t, i), nm = line_node<DIM, N, O>(t, m);
-      const double dim_ = p.dsplit[i * N + m], dmi = p.dsplit[m * N + i];
+      const double dim_ = s_D[i * N + m], dmi = s_D[m * N + i];
       double g[NV], ui[NV], wi[NV], um[NV], wm[NV], bi[NV], bm[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) {

@@ -51,6 +51,7 @@ struct FusedParams {
   int surface_flux, fv_flux;
   double rk_a, rk_b, dt;
   int use_k;                                // RK: read k (rk_a != 0)
+  int wpg, gpb;                             // tile: warps per group, groups per block
   int vec16;                                // u_in, out, k, mortar_flux 16-byte aligned
   double atol;                              // dg-only test for alpha
   PhysParams<R> pp;
@@ -261,7 +262,7 @@ struct FusedKernel {
     if (by_smem > w) w = by_smem;
     return w < 8 ? w : (warps_for(EPG) > 8 ? warps_for(EPG) : 8);
   }
-  static constexpr int WPG = wpg_pick();  // warps per group
+  static constexpr int WPG = wpg_pick();  // default warps per group (the tile tuner may pick others)
   static constexpr int GT = 32 * WPG;                  // threads per group
   static constexpr int N_CONS = n_cons(EPG);
   static constexpr int N_VOL = n_vol(EPG);
@@ -270,7 +271,7 @@ struct FusedKernel {
   static constexpr int N_TRACE = n_trace(EPG);
   static constexpr int N_EL = n_el(EPG);
   static constexpr size_t GROUP_SMEM = group_smem(EPG);
-  // groups per block: up to 256 threads and 48 KB of shared memory
+  // default groups per block: up to 256 threads and 48 KB of shared memory
   static constexpr int gpb_pick() {
     int g = 256 / GT;
     if (g < 1) g = 1;
@@ -308,11 +309,12 @@ struct FusedKernel {
     }
   };
 
-  __device__ __forceinline__ static void group_sync(int gid) {
-    if constexpr (WPG == 1) {
+  // groups of one warp use __syncwarp; larger groups a named barrier (id 1 + gid)
+  __device__ __forceinline__ static void group_sync(int gid, int wpg, int gthreads) {
+    if (wpg == 1) {
       __syncwarp();
     } else {
-      asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "r"(GT) : "memory");
+      asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "r"(gthreads) : "memory");
     }
   }
 
@@ -378,12 +380,12 @@ struct FusedKernel {
 
   __device__ __forceinline__ static void run(const FusedParams<R> &p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int gid = threadIdx.x / GT;  // group within the block
-    const int gt = threadIdx.x - gid * GT;
-    const int64_t e0 = ((int64_t)blockIdx.x * GPB + gid) * EPG;  // first element of the group
-    if (e0 >= p.nelements) return;  // whole groups leave together
-    const int ne = (int)min((int64_t)EPG, p.nelements - e0);
-
+    // runtime tile: p.wpg warps per group (>= the owners of EPG elements),
+    // p.gpb groups per block (launch_one validates both)
+    const int GTr = 32 * p.wpg;
+    const int gid = threadIdx.x / GTr;  // group within the block
+    const int gt = threadIdx.x - gid * GTr;
+    if (gid >= p.gpb) return;
     Smem s;
     s.cons = reinterpret_cast<R *>(smem_raw + gid * GROUP_SMEM);
     s.prim = s.cons + N_CONS;
@@ -397,6 +399,15 @@ struct FusedKernel {
     s.dhat = s.dsplit + N * N;
     s.invw = s.dhat + N * N;
     s.conforming = reinterpret_cast<int *>(s.dsplit + N_OPS);
+    // the operators, staged once per group (first read after phase A's sync)
+    for (int q = gt; q < N * N; q += GTr) {
+      s.dsplit[q] = p.dsplit[q];
+      s.dhat[q] = p.dhat[q];
+    }
+    if (gt < N) s.invw[gt] = p.invw[gt];
+    const int64_t e0 = ((int64_t)blockIdx.x * p.gpb + gid) * EPG;  // first element of the group
+    if (e0 >= p.nelements) return;  // whole groups leave together
+    const int ne = (int)min((int64_t)EPG, p.nelements - e0);
 
     const int mode = p.mode;
     const bool surface = (mode != MODE_VOLUME);
@@ -418,7 +429,7 @@ struct FusedKernel {
     if (surface) {
       constexpr int PER_EL = 2 * DIM * NF;
       const int n_trace = ne * PER_EL;
-      for (int j = gt; j < n_trace; j += GT) {
+      for (int j = gt; j < n_trace; j += GTr) {
         const int el = j / PER_EL, r = j - (j / PER_EL) * PER_EL;
         const int face = r / NF, t = r - (r / NF) * NF;
         const int32_t nb = p.face_table[(e0 + el) * (2 * DIM) + face];
@@ -457,12 +468,7 @@ struct FusedKernel {
         s.scale[my_el] = from_double<R>(f);
       }
     }
-    for (int q = gt; q < N * N; q += GT) {
-      s.dsplit[q] = p.dsplit[q];
-      s.dhat[q] = p.dhat[q];
-    }
-    if (gt < N) s.invw[gt] = p.invw[gt];
-    group_sync(gid);
+    group_sync(gid, p.wpg, GTr);
 
     // phase B: every flux of the group, sections [volume | surface | FV],
     // each ordered [direction][element][item] so warps stay on one direction
@@ -472,7 +478,7 @@ struct FusedKernel {
     constexpr int NVOL_ITEMS = DIM * PER_VOL;
     const int n_surf = surface ? DIM * PER_SURF : 0;
     const int n_all = NVOL_ITEMS + n_surf + DIM * PER_FV;
-    for (int w = gt; w < n_all; w += GT) {
+    for (int w = gt; w < n_all; w += GTr) {
       if (w < NVOL_ITEMS) {
         const int dir = w / PER_VOL;
         const int r0 = w - dir * PER_VOL;
@@ -505,7 +511,7 @@ struct FusedKernel {
         if constexpr (DIM > 2) if (dir == 2) fv_item<2>(p, s, el, t, a);
       }
     }
-    group_sync(gid);
+    group_sync(gid, p.wpg, GTr);
 
     // phase C: the thread that loaded node q finishes it
     if (!has_node) return;
@@ -641,8 +647,7 @@ struct FusedKernel {
 };
 
 template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX>
-__global__ void __launch_bounds__(FusedKernel<DIM, N, EQ, R, VOL, VFLUX>::BLOCK)
-    dg_fused_kernel(const FusedParams<R> p) {
+__global__ void __launch_bounds__(512) dg_fused_kernel(const FusedParams<R> p) {
   FusedKernel<DIM, N, EQ, R, VOL, VFLUX>::run(p);
 }
 

@@ -35,6 +35,19 @@ struct FusedHost {
   double invw[HOST_NMAX] = {};
   double lhat_l = 0, lhat_r = 0;
   int epb = 0;  // elements per block, 0 = default
+  // tile of the fused kernel: warps per group and groups per block (0 = the
+  // compile-time defaults); a non-null tile_out makes launch_fused report the
+  // kernel's tile limits instead of launching
+  int wpg = 0, gpb = 0;
+  struct FusedTile *tile_out = nullptr;
+};
+
+// Tile limits of one fused-kernel instantiation.
+struct FusedTile {
+  int epg = 0;            // elements per group (compile time)
+  int min_wpg = 0;        // warps owning the group's nodes
+  int def_wpg = 0, def_gpb = 0;
+  size_t group_smem = 0;  // bytes of shared memory per group
 };
 
 // Returns cudaErrorNotSupported when the combination is not compiled.

@@ -48,10 +48,27 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   for (int i = 0; i < NMAXT; ++i) p.invw[i] = R(i < N ? h.invw[i] : 0.0);
   p.lhat_l = R(h.lhat_l);
   p.lhat_r = R(h.lhat_r);
-  const int epb = K::EPB;  // compile-time tile size (see FusedKernel::gpb_pick)
+  if (h.tile_out) {
+    h.tile_out->epg = K::EPG;
+    h.tile_out->min_wpg = K::warps_for(K::EPG);
+    h.tile_out->def_wpg = K::WPG;
+    h.tile_out->def_gpb = K::GPB;
+    h.tile_out->group_smem = K::GROUP_SMEM;
+    return cudaSuccess;
+  }
+  // tile: the requested one when valid, else the compile-time defaults
+  int wpg = K::WPG, gpb = K::GPB;
+  if (h.wpg >= K::warps_for(K::EPG) && h.wpg <= 8 && h.gpb >= 1 && h.gpb <= 15 && h.gpb * h.wpg <= 16 &&
+      (size_t)h.gpb * K::GROUP_SMEM <= 200 * 1024) {
+    wpg = h.wpg;
+    gpb = h.gpb;
+  }
+  p.wpg = wpg;
+  p.gpb = gpb;
+  const int epb = gpb * K::EPG;  // elements per block
   p.epb = epb;
-  const int block = K::BLOCK;
-  const size_t smem = K::smem_bytes();
+  const int block = 32 * wpg * gpb;
+  const size_t smem = (size_t)gpb * K::GROUP_SMEM;
   // opt in once per instantiation to the large dynamic shared-memory carve-out
   static const cudaError_t attr = cudaFuncSetAttribute(dg_fused_kernel<DIM, N, EQ, R, VOL, VF>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

@@ -97,6 +97,9 @@ struct trixi_handle {
   double total_volume = 0.0;
   struct AdjointState *adj = nullptr;
   FusedHost fused;
+  // tile tuner record: candidate (wpg, gpb) and ms per RK-stage launch
+  std::vector<int> tune_wpg, tune_gpb;
+  std::vector<double> tune_ms;
   std::string last_error;
   int last_status = TRIXI_OK;
 };
@@ -477,6 +480,83 @@ int run_rhs(trixi_handle *h, int mode, const double *u_in, double *out, double *
   return TRIXI_OK;
 }
 
+int fused_tile(trixi_handle *h, FusedTile &t) {
+  FusedHost f = h->fused;
+  f.tile_out = &t;
+  f.nelements = 0;
+  TRIXI_CUDA(h, launch_fused(h->dim, h->N, h->eq, h->vol, h->vflux, h->mixed, f, nullptr), "fused tile query");
+  return TRIXI_OK;
+}
+
+// Tile tuner: times the fused RK-stage launch for every valid (warps per
+// group, groups per block) on the state u (read only; the outputs go to
+// temporary buffers) and keeps the fastest.  Results do not depend on the
+// tile: every node and flux is computed by the same arithmetic.
+int tune_tiles(trixi_handle *h, const double *u, cudaStream_t s) {
+  FusedTile t;
+  if (int st = fused_tile(h, t)) return st;
+  struct Cand {
+    int w, g;
+  };
+  std::vector<Cand> cand;
+  for (int w = t.min_wpg; w <= 8; ++w)
+    for (int g : {1, 2, 4, 8})
+      if (g * w <= 16 && (size_t)g * t.group_smem <= 200 * 1024) cand.push_back({w, g});
+  const size_t bytes = sizeof(double) * (size_t)(h->E * h->NN * h->nv);
+  double *out = nullptr, *k = nullptr;
+  TRIXI_CUDA(h, cudaMalloc(&out, bytes), "tuner buffers");
+  if (cudaMalloc(&k, bytes) != cudaSuccess) {
+    cudaFree(out);
+    return fail(h, TRIXI_ERR_OUT_OF_MEMORY, "tuner buffers");
+  }
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  int status = TRIXI_OK;
+  h->tune_wpg.clear();
+  h->tune_gpb.clear();
+  h->tune_ms.clear();
+  const FusedHost saved = h->fused;
+  int best_w = 0, best_g = 0;
+  double best_ms = 0.0;
+  if (cudaMemsetAsync(k, 0, bytes, s) != cudaSuccess) status = fail(h, TRIXI_ERR_CUDA, "tuner k");
+  for (size_t ci = 0; ci < cand.size() && status == TRIXI_OK; ++ci) {
+    h->fused.wpg = cand[ci].w;
+    h->fused.gpb = cand[ci].g;
+    const int reps = 5;
+    status = run_rhs(h, MODE_RK, u, out, k, 0.5, 0.1, 1e-9, s);  // warm-up
+    cudaEventRecord(t0, s);
+    for (int r = 0; r < reps && status == TRIXI_OK; ++r) status = run_rhs(h, MODE_RK, u, out, k, 0.5, 0.1, 1e-9, s);
+    cudaEventRecord(t1, s);
+    if (status != TRIXI_OK) break;
+    float ms = 0.f;
+    cudaError_t e = cudaEventSynchronize(t1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t0, t1);
+    if (e != cudaSuccess) {
+      status = fail(h, TRIXI_ERR_CUDA, "tuner timing: %s", cudaGetErrorString(e));
+      break;
+    }
+    h->tune_wpg.push_back(cand[ci].w);
+    h->tune_gpb.push_back(cand[ci].g);
+    h->tune_ms.push_back(ms / reps);
+    if (best_w == 0 || ms / reps < best_ms) {
+      best_w = cand[ci].w;
+      best_g = cand[ci].g;
+      best_ms = ms / reps;
+    }
+  }
+  cudaStreamSynchronize(s);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(out);
+  cudaFree(k);
+  h->fused = saved;
+  if (status != TRIXI_OK) return status;
+  h->fused.wpg = best_w;
+  h->fused.gpb = best_g;
+  return TRIXI_OK;
+}
+
 StageHost stage_of(trixi_handle *h) {
   StageHost sh;
   sh.dim = h->dim;
@@ -727,6 +807,49 @@ int trixi_lgl_basis(int polydeg, int which, double *host_out, int64_t count) {
   if (polydeg < 1 || polydeg > 15 || !compute_basis(polydeg, b))
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "polydeg %d", polydeg);
   return copy_basis_item(b, which, host_out, count);
+}
+
+int trixi_autotune(trixi_handle *h, const double *u, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (!aligned8(u)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "u must be an 8-byte aligned device pointer");
+  if (h->E == 0) return TRIXI_OK;
+  return tune_tiles(h, u, (cudaStream_t)stream);
+}
+
+int trixi_set_tile(trixi_handle *h, int wpg, int gpb) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (wpg == 0 && gpb == 0) {
+    h->fused.wpg = h->fused.gpb = 0;
+    return TRIXI_OK;
+  }
+  FusedTile t;
+  if (int st = fused_tile(h, t)) return st;
+  if (wpg < t.min_wpg || wpg > 8 || gpb < 1 || gpb > 15 || gpb * wpg > 16 || (size_t)gpb * t.group_smem > 200 * 1024)
+    return fail(h, TRIXI_ERR_INVALID_ARGUMENT,
+                "tile (%d warps per group, %d groups per block) outside [%d..8] warps, <= 16 warps per block", wpg,
+                gpb, t.min_wpg);
+  h->fused.wpg = wpg;
+  h->fused.gpb = gpb;
+  return TRIXI_OK;
+}
+
+int trixi_tile(trixi_handle *h, int *epg, int *wpg, int *gpb, int *cand_wpg, int *cand_gpb, double *cand_ms,
+               int64_t max, int64_t *count) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  FusedTile t;
+  if (int st = fused_tile(h, t)) return st;
+  const bool custom = h->fused.wpg > 0 && h->fused.gpb > 0;
+  if (epg) *epg = t.epg;
+  if (wpg) *wpg = custom ? h->fused.wpg : t.def_wpg;
+  if (gpb) *gpb = custom ? h->fused.gpb : t.def_gpb;
+  const int64_t n = (int64_t)h->tune_ms.size();
+  if (count) *count = n;
+  for (int64_t i = 0; i < n && i < max; ++i) {
+    if (cand_wpg) cand_wpg[i] = h->tune_wpg[(size_t)i];
+    if (cand_gpb) cand_gpb[i] = h->tune_gpb[(size_t)i];
+    if (cand_ms) cand_ms[i] = h->tune_ms[(size_t)i];
+  }
+  return TRIXI_OK;
 }
 
 int trixi_synchronize(trixi_handle *h, void *stream) {
@@ -1102,10 +1225,6 @@ int tune_branches(trixi_batch *b, const double *u, const double *k, cudaStream_t
   if (G > 1 && std::find(cand.begin(), cand.end(), G) == cand.end() && G <= 32) cand.push_back(G);
   b->tune_candidates = cand;
   b->tune_ms.assign(cand.size(), 0.0);
-  if (cand.size() == 1) {
-    b->branches = 1;
-    return TRIXI_OK;
-  }
   const size_t bytes = sizeof(double) * (size_t)b->total_values;
   double *tu = nullptr, *tk = nullptr;
   if (cudaMalloc(&tu, bytes) != cudaSuccess || cudaMalloc(&tk, bytes) != cudaSuccess) {
@@ -1120,6 +1239,19 @@ int tune_branches(trixi_batch *b, const double *u, const double *k, cudaStream_t
   int best = 1;
   double best_ms = 0.0;
   int status = TRIXI_OK;
+  // first the tile of every group's kernel, on the copy of its state
+  cudaMemcpyAsync(tu, u, bytes, cudaMemcpyDeviceToDevice, s);
+  for (auto &g : b->groups) {
+    if (status != TRIXI_OK) break;
+    FusedHost save = g.h->fused;
+    g.h->fused.dt_elem = g.d_dt;
+    status = tune_tiles(g.h, tu + g.value_offset, s);
+    const int w = g.h->fused.wpg, gg = g.h->fused.gpb;
+    g.h->fused = save;
+    g.h->fused.wpg = w;
+    g.h->fused.gpb = gg;
+    if (status != TRIXI_OK) status = batch_fail(b, status, g.h->last_error);
+  }
   for (size_t ci = 0; ci < cand.size() && status == TRIXI_OK; ++ci) {
     cudaMemcpyAsync(tu, u, bytes, cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(tk, k, bytes, cudaMemcpyDeviceToDevice, s);

@@ -30,6 +30,8 @@ from .mesh import TreeMesh
 from .semidiscretization import (
     ODEProblem,
     SemidiscretizationHyperbolicGPU,
+    autotune,
+    set_tile,
     calc_error_norms,
     compute_coefficients_gpu,
     integrate,
@@ -50,6 +52,7 @@ from .semidiscretization import (
     rk_steps,
     semidiscretizeGPU,
     synchronize,
+    tile,
     wrap_array,
 )
 from .solver import (

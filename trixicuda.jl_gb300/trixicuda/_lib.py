@@ -136,6 +136,10 @@ SIGNATURES = {
     "trixi_batch_tuning": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double), _I64,
                                      C.POINTER(C.c_int64)]),
     "trixi_integrate": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _VP]),
+    "trixi_autotune": (C.c_int, [_VP, _VP, _VP]),
+    "trixi_set_tile": (C.c_int, [_VP, _I, _I]),
+    "trixi_tile": (C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                             C.POINTER(C.c_int), C.POINTER(C.c_double), _I64, C.POINTER(C.c_int64)]),
     "trixi_integrate_noalloc": (C.c_int, [_I, _I, _I, C.c_double, _VP, _VP, _VP, _I64, _I, _VP, _VP]),
     "trixi_calc_error_norms": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _D,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double), _VP]),

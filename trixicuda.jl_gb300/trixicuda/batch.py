@@ -144,6 +144,31 @@ class BatchedSemidiscretizationGPU:
         n = min(int(cnt.value), 16)
         return int(br.value), {int(cand[i]): float(ms[i]) for i in range(n)}
 
+    def group_of(self, i):
+        """Group index of instance i: kinds are numbered in order of first
+        appearance, as the library numbers them."""
+        if not hasattr(self, "_group_index"):
+            order, idx = {}, []
+            for pb in self.problems:
+                vi = pb.solver.volume_integral
+                key = (pb.mesh.ndims, pb.solver.polydeg, type(pb.equations).__name__, type(vi).__name__,
+                       repr(getattr(vi, "volume_flux", None)), repr(pb.solver.surface_flux))
+                idx.append(order.setdefault(key, len(order)))
+            self._group_index = idx
+        return self._group_index[i]
+
+    def group_tiles(self):
+        """Per group: ((elements per group, warps per group, groups per block),
+        the tile tuner's {(wpg, gpb): ms}) after the first graph build."""
+        from .semidiscretization import _read_tile
+
+        out = []
+        for g in range(self.ngroups):
+            h = C.c_void_p()
+            _batch_check(self._lib.trixi_batch_handle(self._h, g, C.byref(h)), self._h)
+            out.append(_read_tile(self._lib, h))
+        return out
+
     def stable_dt(self, u, cfl=0.5):
         """Per-instance CFL time step cfl * 2 / (N * max J^{-1} sum_d lambda_d)."""
         torch = _torch()

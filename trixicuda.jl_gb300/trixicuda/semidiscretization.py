@@ -325,6 +325,33 @@ def rk_steps(u, k, t, dt, nsteps, semi, stream=None):
           float(dt), int(nsteps), stream=stream)
 
 
+def autotune(u, semi, stream=None):
+    """Picks the fused kernel's tile (warps per element group, groups per
+    block) for this problem by timing every valid tile on u (read only)."""
+    _check_state(semi, u)
+    _call(semi, semi._lib.trixi_autotune, C.c_void_p(u.data_ptr()), stream=stream)
+
+
+def set_tile(semi, wpg, gpb):
+    """Fixes the tile by hand; wpg = gpb = 0 restores the compile-time default."""
+    _lib.check(semi._lib.trixi_set_tile(semi._handle, int(wpg), int(gpb)), semi._handle)
+
+
+def _read_tile(lib, handle):
+    epg, wpg, gpb, cnt = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+    cw, cg, cm = (C.c_int * 64)(), (C.c_int * 64)(), (C.c_double * 64)()
+    _lib.check(lib.trixi_tile(handle, C.byref(epg), C.byref(wpg), C.byref(gpb), cw, cg, cm, 64, C.byref(cnt)),
+               handle)
+    n = min(int(cnt.value), 64)
+    return (int(epg.value), int(wpg.value), int(gpb.value)), {(int(cw[i]), int(cg[i])): float(cm[i]) for i in range(n)}
+
+
+def tile(semi):
+    """((elements per group, warps per group, groups per block), the tuner's
+    {(wpg, gpb): ms per launch}) -- the table is empty before autotune."""
+    return _read_tile(semi._lib, semi._handle)
+
+
 # -- analysis, time step and initial conditions on the GPU (reference callbacks) ----
 _IC_KINDS = {"constant": _lib.IC_CONSTANT, "convergence_test": _lib.IC_CONVERGENCE_TEST,
              "weak_blast_wave": _lib.IC_WEAK_BLAST_WAVE}
