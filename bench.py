@@ -129,7 +129,7 @@ def _tile_report(semi):
             "tuner_us_per_launch": {f"{w}x{g}": round(ms * 1e3, 2) for (w, g), ms in sorted(table.items())}}
 
 
-def time_gpu_path(precision, steps, warmup, device, flush):
+def time_gpu_path(precision, steps, warmup, device, flush, tile=None):
     """Device-timed CK2N54 steps through trixi_rk_stage (ping-pong buffers).
     Returns per-step ms, per-launch ms of the fused kernel, the semi, final u."""
     import torch
@@ -141,7 +141,10 @@ def time_gpu_path(precision, steps, warmup, device, flush):
     semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, precision=precision)
     dt = stable_dt(semi)
     u0 = semi.compute_coefficients()
-    T.autotune(u0, semi)  # tile tuner (setup, outside the timed region)
+    if tile:  # a fixed tile (profiling: a tuner run under a profiler would time other things)
+        T.set_tile(semi, *tile)
+    else:
+        T.autotune(u0, semi)  # tile tuner (setup, outside the timed region)
     bufs = [u0.clone(), torch.empty_like(u0)]
     k = torch.zeros_like(u0)
     stream = torch.cuda.current_stream()
@@ -227,7 +230,7 @@ def batched_path(precision, steps, warmup, device, flush, n=512):
             "group_tiles": group_tiles}
 
 
-def adjoint_path(device, nsteps=200, snapshots=15, ndirs=4):
+def adjoint_path(device, nsteps=200, snapshots=15, ndirs=16):
     """2D Euler level 6, polydeg 4 (flux_ranocha volume + surface), J = 1/2 int
     (rho(T) - rho_target)^2 over 200 CK2N54 steps: wall time of the gradient
     (forward sweep + backward sweep with binomial checkpoints) over one plain
@@ -397,6 +400,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "fp64", "batched-mixed", "batched-fp64"], default=None,
                     help="run only the device-timed loop of one precision (for ncu captures)")
+    ap.add_argument("--tile", default=None,
+                    help="with --profile mixed/fp64: fixed tile WPGxGPB (e.g. 2x4) instead of the tuner")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -434,7 +439,8 @@ def main():
         print(json.dumps({"profile": args.profile, **r}))
         return 0
     if args.profile:
-        step_ms, launch_ms, semi, _, _ = time_gpu_path(args.profile, args.steps, args.warmup, device, flush)
+        tile = tuple(int(x) for x in args.tile.split("x")) if args.tile else None
+        step_ms, launch_ms, semi, _, _ = time_gpu_path(args.profile, args.steps, args.warmup, device, flush, tile)
         print(json.dumps({"profile": args.profile, "ms_per_step": statistics.mean(step_ms),
                           "mean_launch_ms": statistics.mean(launch_ms), "fp64_fma_peak_tflops": fp64_peak.value / 1e12,
                           "fp32_fma_peak_tflops": fp32_peak.value / 1e12}))

@@ -98,3 +98,35 @@ def test_autograd_function(cuda):
     uT.backward(g)
     _, g_ref, _ = ADJ.gradient_density_l2(semi, u0.detach(), rt, dt, 6, 2)
     assert cuda.allclose(u0.grad, g_ref, rtol=0, atol=0)
+
+
+def test_full_size_c4_gradient_matches_fd(cuda):
+    """The adjoint configuration at full size: 2D Euler level 6, polydeg 4,
+    flux_ranocha, J = 1/2 int (rho(T) - rho_target)^2 after 200 CK2N54 steps,
+    binomial checkpointing with 15 snapshots; the gradient must match central
+    finite differences (h = 1e-6) to 1e-6 along 16 seeded random directions."""
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEMGPU(polydeg=4, surface_flux=T.flux_ranocha,
+                        volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((-2.0, -2.0), (2.0, 2.0), initial_refinement_level=6)
+    ic = T.initial_condition_fourier_euler(eq, seed=20261203, kmax=8)
+    semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver)
+    u0 = semi.compute_coefficients()
+    x = semi.containers.node_coordinates.reshape(-1, 2).T
+    rt = cuda.from_numpy(1.0 + 0.05 * T.equations.FourierField(2, 4, 4242, -2.0, 2.0)(x)).to(u0.device)
+    dt = 0.5 * T.max_dt(u0, semi)
+    nsteps = 200
+    J, grad, nrec = ADJ.gradient_density_l2(semi, u0, rt, dt, nsteps, 15)
+    assert nrec > 0
+    rng = np.random.default_rng(20261203)
+    for _ in range(16):
+        dirn = cuda.from_numpy(rng.standard_normal(u0.shape)).to(u0.device)
+        vals = []
+        for sgn in (1, -1):
+            u = (u0 + sgn * 1e-6 * dirn).contiguous()
+            k = cuda.zeros_like(u)
+            T.rk_steps(u, k, 0.0, dt, nsteps, semi)
+            vals.append(ADJ.objective_density_l2(u, rt, semi, grad=False)[0])
+        fd = (vals[0] - vals[1]) / 2e-6
+        ad = float((grad * dirn).sum())
+        assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)

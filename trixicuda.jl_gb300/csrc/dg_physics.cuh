@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include "dg_consts.h"
+#include "dg_convert.cuh"
 
 namespace trixi {
 
@@ -32,15 +33,30 @@ struct PhysParams {
   R a[3];                 // advection velocity
 };
 
-// Precision-specific elementary operations.  FP64 keeps IEEE division and
-// log; the FP32 path of the mixed-precision kernels uses the fast hardware
-// approximations (__fdividef: 2 ulp; __logf: absolute error ~2^-21 near 1),
-// well inside its error budget (the rhs in FP32 is accurate to ~1e-6 relative).
+// Precision-specific elementary operations.  FP64 keeps the library log and
+// sqrt and divides through rcp_newton (below); the FP32 path of the
+// mixed-precision kernels uses the fast hardware approximations (__fdividef:
+// 2 ulp; __logf: absolute error ~2^-21 near 1), well inside its error budget
+// (the rhs in FP32 is accurate to ~1e-6 relative).
 __device__ __forceinline__ double dev_log(double x) { return log(x); }
 __device__ __forceinline__ float dev_log(float x) { return __logf(x); }
-__device__ __forceinline__ double dev_div(double a, double b) { return a / b; }
+// FP64 reciprocal by Newton-Raphson refinement r <- r + r (1 - x r) of the
+// FP32 hardware approximation (relative error 2^-22 -> 2^-44 -> ~1 ulp of
+// FP64 after the second step); the conversions run on the integer pipe, so
+// the FP64 pipe -- the bound of the FP64 kernels -- sees 4 FMAs instead of an
+// IEEE division.  Divisors are nonzero and within the float range (densities,
+// pressures, their sums and differences, logarithms of their ratios).
+__device__ __forceinline__ double rcp_newton(double x) {
+  const float rf = __fdividef(1.0f, d2f_rn(x));
+  double r = f2d_exact(rf);
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+__device__ __forceinline__ double dev_div(double a, double b) { return a * rcp_newton(b); }
 __device__ __forceinline__ float dev_div(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ double dev_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ double dev_rcp(double x) { return rcp_newton(x); }
 __device__ __forceinline__ float dev_rcp(float x) { return __fdividef(1.0f, x); }
 __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float dev_sqrt(float x) { return sqrtf(x); }
