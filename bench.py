@@ -290,6 +290,8 @@ def adjoint_path(device, nsteps=200, snapshots=15, ndirs=16):
         fd = (vals[0] - vals[1]) / 2e-6
         ad = float((grad * dirn).sum())
         errs.append(abs(fd - ad) / abs(ad))
+    if not errs:
+        errs = [float("nan")]
     return {"workload": "2D Euler level 6 (4096 elements), polydeg 4, flux_ranocha, 200 CK2N54 steps, FP64",
             "forward_ms": f_ms, "J": J, **res, "fd_directions": ndirs, "fd_h": 1e-6,
             "fd_max_rel_err": max(errs)}
@@ -398,7 +400,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "batched-mixed", "batched-fp64"], default=None,
+    ap.add_argument("--profile", choices=["mixed", "fp64", "batched-mixed", "batched-fp64", "adjoint"], default=None,
                     help="run only the device-timed loop of one precision (for ncu captures)")
     ap.add_argument("--tile", default=None,
                     help="with --profile mixed/fp64: fixed tile WPGxGPB (e.g. 2x4) instead of the tuner")
@@ -434,6 +436,11 @@ def main():
     T._lib.check(lib.trixi_probe_fma_peak(0, 4096, C.byref(fp64_peak), None))
     T._lib.check(lib.trixi_probe_fma_peak(1, 16384, C.byref(fp32_peak), None))
 
+    if args.profile == "adjoint":
+        # the adjoint workload (2D Euler level 6, polydeg 4) over `steps` RK steps, store-all
+        r = adjoint_path(device, nsteps=max(2, args.steps), snapshots=max(1, args.steps - 1), ndirs=0)
+        print(json.dumps({"profile": "adjoint", **r}))
+        return 0
     if args.profile and args.profile.startswith("batched"):
         r = batched_path(args.profile.split("-")[1], args.steps, args.warmup, device, flush)
         print(json.dumps({"profile": args.profile, **r}))

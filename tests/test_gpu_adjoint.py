@@ -20,6 +20,9 @@ def _semi(kind, d, level, p=3, ic=None, **kw):
 CASES = [("euler_fd", 2, 2, 3, None, {}), ("euler_fd", 3, 1, 3, None, {}), ("euler_fd", 2, 2, 4, None, {}),
          ("euler_fd", 2, 2, 3, "blast", {}),  # large ratios: the log branch of the means
          ("euler_fd", 2, 2, 3, None, dict(surface_flux=T.flux_central, volume_flux=T.flux_central)),
+         # one flux with primitive-variable cotangents, the other with conservative ones
+         ("euler_fd", 2, 2, 3, None, dict(surface_flux=T.flux_ranocha, volume_flux=T.flux_central)),
+         ("euler_fd", 2, 2, 4, None, dict(surface_flux=T.flux_central, volume_flux=T.flux_ranocha)),
          ("adv_weak", 2, 2, 3, None, {}), ("adv_weak", 1, 3, 3, None, {}), ("adv_fd", 3, 1, 3, None, {}),
          ("adv_weak", 2, 2, 3, None, dict(surface_flux=T.flux_central))]
 

@@ -29,10 +29,10 @@ __device__ __forceinline__ void ln_mean_grad(double x, double y, double r, doubl
     dx = 0.5 * h + 2.0 * f * y * hp * r;
     dy = 0.5 * h - 2.0 * f * x * hp * r;
   } else {
-    const double l = log(x / y);
-    L = d / l;
-    dx = (1.0 - L / x) / l;
-    dy = (L / y - 1.0) / l;
+    const double l = log(x * rcp_newton(y)), il = rcp_newton(l);
+    L = d * il;
+    dx = (1.0 - L * rcp_newton(x)) * il;
+    dy = (L * rcp_newton(y) - 1.0) * il;
   }
 }
 
@@ -45,10 +45,10 @@ __device__ __forceinline__ void inv_ln_mean_grad(double x, double y, double r, d
     dx = -2.0 * r * r * g + 8.0 * f * y * r * r * r * gp;
     dy = -2.0 * r * r * g - 8.0 * f * x * r * r * r * gp;
   } else {
-    const double l = log(x / y);
-    Q = l / d;
-    dx = (1.0 / x - Q) / d;
-    dy = (Q - 1.0 / y) / d;
+    const double l = log(x * rcp_newton(y)), id = rcp_newton(d);
+    Q = l * id;
+    dx = (rcp_newton(x) - Q) * id;
+    dy = (Q - rcp_newton(y)) * id;
   }
 }
 
@@ -107,7 +107,7 @@ struct Adjoint<DIM, EQ_EULER> {
     const double rl = wl[0], rr = wr[0], pl = wl[DIM + 1], pr = wr[DIM + 1];
     double L, dLl, dLr, Q, dQx, dQy;
     const double x2 = rl * pr, y2 = rr * pl;
-    const double s1 = rl + rr, s2 = x2 + y2, qq = 1.0 / (s1 * s2);  // one division for both means
+    const double s1 = rl + rr, s2 = x2 + y2, qq = rcp_newton(s1 * s2);  // one reciprocal for both means
     ln_mean_grad(rl, rr, s2 * qq, L, dLl, dLr);
     inv_ln_mean_grad(x2, y2, s1 * qq, Q, dQx, dQy);
     const double ipm = pl * pr * Q;
@@ -279,7 +279,7 @@ struct AdjointKernel {
 #pragma unroll
       for (int v = 0; v < NV; ++v) uu[v] = p.u[g0 + v];
       P::prim(uu, ww, p.pp);
-      s_ir[el * NN + n] = 1.0 / uu[0];
+      s_ir[el * NN + n] = rcp_newton(uu[0]);
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         U(el, v, n) = uu[v];
@@ -338,16 +338,23 @@ struct AdjointKernel {
           tface[2] = coord[0] + N * coord[1];
         }
       }
-      double ub[NV];
+      // cotangents of the node: conservative (ub) and primitive-variable (pb,
+      // from flux_ranocha items, mapped to conservative once below)
+      double ub[NV], pb[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) ub[v] = 0.0;
+      for (int v = 0; v < NV; ++v) ub[v] = pb[v] = 0.0;
+      double *vacc = ub, *sacc = ub;
+      if constexpr (EQ == EQ_EULER) {
+        if (VOL != VOL_WEAK && p.volume_flux == FLUX_RANOCHA) vacc = pb;
+        if (p.surface_flux == FLUX_RANOCHA) sacc = pb;
+      }
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
         const int ci = coord[d];
         if constexpr (VOL == VOL_WEAK) {
           const double *B = s_vb + ((el * DIM + d) * VOL_PER_DIR + node) * NV;
 #pragma unroll
-          for (int v = 0; v < NV; ++v) ub[v] += B[v];
+          for (int v = 0; v < NV; ++v) vacc[v] += B[v];
         } else {
 #pragma unroll
           for (int m = 0; m < N; ++m) {
@@ -356,18 +363,28 @@ struct AdjointKernel {
             // the pair stores (i<m): slot 0 = cotangent of its left state, 1 = right
             const double *B = s_vb + (((el * DIM + d) * VOL_PER_DIR + pidx) * 2 + (ci < m ? 0 : 1)) * NV;
 #pragma unroll
-            for (int v = 0; v < NV; ++v) ub[v] += B[v];
+            for (int v = 0; v < NV; ++v) vacc[v] += B[v];
           }
         }
         if (ci == 0) {
           const double *B = s_sb + ((el * 2 * DIM + 2 * d) * NF + tface[d]) * NV;
 #pragma unroll
-          for (int v = 0; v < NV; ++v) ub[v] += B[v];
+          for (int v = 0; v < NV; ++v) sacc[v] += B[v];
         }
         if (ci == N - 1) {
           const double *B = s_sb + ((el * 2 * DIM + 2 * d + 1) * NF + tface[d]) * NV;
 #pragma unroll
-          for (int v = 0; v < NV; ++v) ub[v] += B[v];
+          for (int v = 0; v < NV; ++v) sacc[v] += B[v];
+        }
+      }
+      if constexpr (EQ == EQ_EULER) {
+        if (vacc == pb || sacc == pb) {
+          double w[NV], cb[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) w[v] = W(el, v, node);
+          A::prim_vjp(w, s_ir[el * NN + node], pb, cb, p.pp);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) ub[v] += cb[v];
         }
       }
       const int64_t g0 = ((e0 + el) * NN + node) * NV;
@@ -423,8 +440,20 @@ struct AdjointKernel {
         um[v] = s_u[(el * NV + v) * NN + nm];
         wm[v] = s_w[(el * NV + v) * NN + nm];
       }
-      A::template two_point_vjp<O>(p.volume_flux, ui, wi, s_ir[el * NN + ni], um, wm, s_ir[el * NN + nm], g, bi, bm,
-                                   p.pp);
+      if constexpr (EQ == EQ_EULER) {
+        if (p.volume_flux == FLUX_RANOCHA) {
+          // primitive-variable cotangents: the node phase sums them over the
+          // pairs and maps the sum to conservative variables once per node
+          // (the map is linear in the cotangent)
+          A::template ranocha_vjp<O>(wi, wm, g, bi, bm, p.pp);
+        } else {
+          A::template two_point_vjp<O>(p.volume_flux, ui, wi, s_ir[el * NN + ni], um, wm, s_ir[el * NN + nm], g, bi,
+                                       bm, p.pp);
+        }
+      } else {
+        A::template two_point_vjp<O>(p.volume_flux, ui, wi, s_ir[el * NN + ni], um, wm, s_ir[el * NN + nm], g, bi, bm,
+                                     p.pp);
+      }
       double *dst = s_vb + ((el * DIM + O) * VOL_PER_DIR + r) * 2 * NV;
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
@@ -459,8 +488,20 @@ struct AdjointKernel {
                          : (-ij_own * p.lhat_r * lown + ij_nb * p.lhat_l * lnb);
     }
     P::prim(un, wn, p.pp);
-    const double irn = 1.0 / un[0], iro = s_ir[el * NN + own];
+    const double irn = rcp_newton(un[0]), iro = s_ir[el * NN + own];
     double *dst = s_sb + ((el * 2 * DIM + 2 * O + side) * NF + t) * NV;
+    if constexpr (EQ == EQ_EULER) {
+      if (p.surface_flux == FLUX_RANOCHA) {
+        // the owner's primitive-variable cotangent (mapped once per node)
+        if (side == 0)
+          A::template ranocha_vjp<O>(wn, wo, g, bl, br, p.pp);
+        else
+          A::template ranocha_vjp<O>(wo, wn, g, bl, br, p.pp);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) dst[v] = side == 0 ? br[v] : bl[v];
+        return;
+      }
+    }
     if (side == 0) {
       A::template two_point_vjp<O>(p.surface_flux, un, wn, irn, uo, wo, iro, g, bl, br, p.pp);
 #pragma unroll

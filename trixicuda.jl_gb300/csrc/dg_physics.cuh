@@ -137,8 +137,15 @@ __device__ __forceinline__ void ranocha_means(R x1, R y1, R x2, R y2, R &mean1, 
   const R r1 = s2 * q, r2 = s1 * q;
   const R f1 = d1 * r1, f2 = d2 * r2;
   const R u1 = f1 * f1, u2 = f2 * f2;
-  mean1 = (u1 < LnMeanThreshold<R>::value) ? ln_mean_series(s1, u1) : dev_div(d1, dev_log(dev_div(x1, y1)));
-  inv_mean2 = (u2 < LnMeanThreshold<R>::value) ? inv_ln_mean_series(r2, u2) : dev_div(dev_log(dev_div(x2, y2)), d2);
+  const bool series1 = u1 < LnMeanThreshold<R>::value, series2 = u2 < LnMeanThreshold<R>::value;
+  mean1 = ln_mean_series(s1, u1);
+  inv_mean2 = inv_ln_mean_series(r2, u2);
+  // the logarithmic forms only when a lane of the warp needs one (smooth
+  // states stay on the series; each lane's result is the same either way)
+  if (__any_sync(__activemask(), !(series1 && series2))) {
+    if (!series1) mean1 = dev_div(d1, dev_log(dev_div(x1, y1)));
+    if (!series2) inv_mean2 = dev_div(dev_log(dev_div(x2, y2)), d2);
+  }
 }
 
 // Physics of one equation system.  States: `u` conservative, `w` primitive
