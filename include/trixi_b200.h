@@ -106,7 +106,7 @@ typedef struct trixi_problem_desc {
   int64_t ninterfaces;
   const int64_t *interface_neighbor_ids; /* [2, ninterfaces] */
   const int64_t *interface_orientations; /* [ninterfaces] */
-  int64_t nboundaries;                   /* must be 0: periodic TreeMesh */
+  int64_t nboundaries;                   /* boundary faces (0: periodic TreeMesh); tables at the end */
   int64_t nmortars;
   const int64_t *mortar_neighbor_ids;    /* [2^(ndims-1)+1, nmortars] */
   const int64_t *mortar_large_sides;     /* [nmortars] */
@@ -127,6 +127,29 @@ typedef struct trixi_problem_desc {
    * of another rank's elements, refreshed by a halo exchange).  Their faces
    * may be left unconnected and their rhs is not meaningful. */
   int64_t nghost_elements;
+  /* Non-periodic meshes and source terms: the reference's boundaries
+   * container (src/solvers/containers_2d.jl) and the boundary_conditions /
+   * source_terms of SemidiscretizationHyperbolicGPU
+   * (src/semidiscretization/semidiscretization_hyperbolic.jl:60-87).
+   * nboundaries entries: 1-based element ids; sides 1 = the element lies on
+   * the boundary's left (the boundary is its upper face), 2 = on its right;
+   * orientations 1..ndims.  Every boundary face gets the Dirichlet state of
+   * boundary_function -- a trixi_initial_condition_kind evaluated at the face
+   * node and the time of the rhs, with the first nboundary_params of
+   * boundary_params (0: the defaults of trixi_compute_coefficients) -- through
+   * the surface flux, as BoundaryConditionDirichlet does.  source_terms (a
+   * trixi_source_terms_kind) adds a source to du after the Jacobian; its
+   * parameters (c, A, L) default to the convergence test's.  Both need
+   * node_coordinates. */
+  const int64_t *boundary_neighbor_ids;
+  const int64_t *boundary_neighbor_sides;
+  const int64_t *boundary_orientations;
+  int32_t boundary_function;   /* -1: no boundaries */
+  int32_t source_terms;
+  int32_t nboundary_params;
+  int32_t nsource_params;
+  double boundary_params[8];
+  double source_params[3];
 } trixi_problem_desc;
 
 /* Library version string ("trixi_b200 <semver> sm_103a"). */
@@ -198,7 +221,8 @@ typedef enum trixi_container_id {
   TRIXI_CONTAINER_MORTARS_U = 2,           /* 2D: +0 u_upper, +1 u_lower; 3D: +0 u_upper_left,
                                               +1 u_upper_right, +2 u_lower_left, +3 u_lower_right */
   TRIXI_CONTAINER_ALPHA = 8,               /* shock-capturing blending factor [nelements] */
-  TRIXI_CONTAINER_INVERSE_JACOBIAN = 9
+  TRIXI_CONTAINER_INVERSE_JACOBIAN = 9,
+  TRIXI_CONTAINER_BOUNDARIES_U = 10        /* cache.boundaries.u [2, nvars, N^(ndims-1), nboundaries] */
 } trixi_container_id;
 int trixi_container(trixi_handle *h, int which, void **dev_ptr, int64_t *count);
 
@@ -217,6 +241,14 @@ typedef enum trixi_initial_condition_kind {
   TRIXI_IC_CONVERGENCE_TEST = 1,
   TRIXI_IC_WEAK_BLAST_WAVE = 2
 } trixi_initial_condition_kind;
+
+/* Source terms (desc.source_terms): the Euler convergence test's
+ * source_terms_convergence_test, the source of its manufactured solution
+ * rho = rho v_d = c + A sin(2 pi/L (sum_d x_d - t)), E = rho^2. */
+typedef enum trixi_source_terms_kind {
+  TRIXI_SOURCE_NONE = 0,
+  TRIXI_SOURCE_CONVERGENCE_TEST = 1
+} trixi_source_terms_kind;
 
 /* u = initial condition at the nodes (needs desc.node_coordinates); 1D
  * moves element end points one ulp inwards like the reference.  Replaces

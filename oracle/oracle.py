@@ -31,6 +31,12 @@ class OracleDesc(C.Structure):
         ("interface_neighbor_ids", C.POINTER(C.c_int64)), ("interface_orientations", C.POINTER(C.c_int64)),
         ("mortar_neighbor_ids", C.POINTER(C.c_int64)), ("mortar_large_sides", C.POINTER(C.c_int64)),
         ("mortar_orientations", C.POINTER(C.c_int64)),
+        ("nboundaries", C.c_int64),
+        ("boundary_neighbor_ids", C.POINTER(C.c_int64)), ("boundary_neighbor_sides", C.POINTER(C.c_int64)),
+        ("boundary_orientations", C.POINTER(C.c_int64)),
+        ("boundary_function", C.c_int32), ("source_terms", C.c_int32),
+        ("boundary_params", C.c_double * 8), ("source_params", C.c_double * 3),
+        ("node_coordinates", C.POINTER(C.c_double)),
     ]
 
 
@@ -61,6 +67,10 @@ def load():
             ("oracle_indicator_hg", [C.c_void_p, _PD, _PD]),
             ("oracle_rhs", [C.c_void_p, _PD, _PD, C.c_double]),
             ("oracle_rk_ck2n54", [C.c_void_p, _PD, _PD, C.c_double, C.c_double, C.c_int]),
+            ("oracle_prolong2boundaries", [C.c_void_p, _PD, _PD]),
+            ("oracle_boundary_flux", [C.c_void_p, _PD, C.c_double, _PD]),
+            ("oracle_sources", [C.c_void_p, _PD, C.c_double]),
+            ("oracle_eval_ic", [C.c_void_p, C.c_int, _PD, _PD, C.c_double, _PD]),
         ]:
             fn = getattr(lib, name)
             fn.restype = None
@@ -94,7 +104,8 @@ class Oracle:
 
     def __init__(self, containers, ndims, polydeg, nvars, equation, gamma=1.4, advection_velocity=(0, 0, 0),
                  volume_integral=VOL_WEAK, volume_flux=FLUX_CENTRAL, surface_flux=FLUX_LLF,
-                 volume_flux_fv=FLUX_LLF, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True):
+                 volume_flux_fv=FLUX_LLF, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+                 boundary_function=-1, boundary_params=None, source_terms=0, source_params=None):
         lib = load()
         self._keep = dict(
             inv=np.ascontiguousarray(containers.inverse_jacobian, dtype=np.float64),
@@ -103,6 +114,10 @@ class Oracle:
             mo_nid=np.ascontiguousarray(containers.mortar_neighbor_ids, dtype=np.int64),
             mo_ls=np.ascontiguousarray(containers.mortar_large_sides, dtype=np.int64),
             mo_ori=np.ascontiguousarray(containers.mortar_orientations, dtype=np.int64),
+            b_nid=np.ascontiguousarray(containers.boundary_neighbor_ids, dtype=np.int64),
+            b_side=np.ascontiguousarray(containers.boundary_neighbor_sides, dtype=np.int64),
+            b_ori=np.ascontiguousarray(containers.boundary_orientations, dtype=np.int64),
+            coords=np.ascontiguousarray(containers.node_coordinates, dtype=np.float64),
         )
         k = self._keep
         d = OracleDesc()
@@ -121,6 +136,15 @@ class Oracle:
         ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))  # noqa: E731
         d.interface_neighbor_ids, d.interface_orientations = ip(k["if_nid"]), ip(k["if_ori"])
         d.mortar_neighbor_ids, d.mortar_large_sides, d.mortar_orientations = ip(k["mo_nid"]), ip(k["mo_ls"]), ip(k["mo_ori"])
+        d.nboundaries = containers.nboundaries
+        d.boundary_neighbor_ids, d.boundary_neighbor_sides = ip(k["b_nid"]), ip(k["b_side"])
+        d.boundary_orientations = ip(k["b_ori"])
+        d.boundary_function, d.source_terms = int(boundary_function), int(source_terms)
+        for i, v in enumerate(boundary_params if boundary_params is not None else []):
+            d.boundary_params[i] = float(v)
+        for i, v in enumerate(source_params if source_params is not None else (2.0, 0.1, 2.0)):
+            d.source_params[i] = float(v)
+        d.node_coordinates = _pd(k["coords"])
         self._desc = d
         self._h = lib.oracle_create(C.byref(d))
         if not self._h:
@@ -145,6 +169,19 @@ class Oracle:
                       alpha_max=vi.indicator.alpha_max, alpha_min=vi.indicator.alpha_min,
                       alpha_smooth=vi.indicator.alpha_smooth)
         av = tuple(getattr(eq, "advection_velocity", np.zeros(eq.ndims)))
+        # boundary function and source terms, with the library's parameters
+        d = getattr(semi, "_desc", None)
+        if d is not None and d.nboundaries > 0:
+            code = int(d.boundary_function)
+            if code == 1:  # convergence test defaults (advection: 1, 0.5, 2; Euler: 2, 0.1, 2)
+                params = (1.0, 0.5, 2.0) if eq.nvariables == 1 else (2.0, 0.1, 2.0)
+            else:
+                params = [d.boundary_params[i] for i in range(8)]
+            if d.nboundary_params > 0:
+                params = [d.boundary_params[i] for i in range(8)]
+            kw.update(boundary_function=code, boundary_params=params)
+        if d is not None and d.source_terms:
+            kw.update(source_terms=int(d.source_terms))
         return cls(semi.containers, eq.ndims, sol.polydeg, eq.nvariables, eq.code,
                    gamma=getattr(eq, "gamma", 1.4), advection_velocity=av, **kw)
 
@@ -183,6 +220,20 @@ class Oracle:
         sfv = np.zeros(self.lib.oracle_size(self._h, 2)) if sfv is None else sfv
         self.lib.oracle_interface_flux(self._h, _pd(np.ascontiguousarray(iu)), _pd(sfv))
         return sfv
+
+    def prolong2boundaries(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        bu = np.zeros(max(self.lib.oracle_size(self._h, 5), 1))
+        self.lib.oracle_prolong2boundaries(self._h, _pd(u), _pd(bu))
+        return bu
+
+    def boundary_flux(self, bu, t, sfv):
+        self.lib.oracle_boundary_flux(self._h, _pd(np.ascontiguousarray(bu)), float(t), _pd(sfv))
+        return sfv
+
+    def sources(self, du, t):
+        self.lib.oracle_sources(self._h, _pd(du), float(t))
+        return du
 
     def prolong2mortars(self, u):
         u = np.ascontiguousarray(u, dtype=np.float64)

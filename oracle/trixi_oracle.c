@@ -40,6 +40,8 @@
  */
 #include "trixi_oracle.h"
 
+#define ORC_PI 3.14159265358979323846
+
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -355,7 +357,7 @@ struct oracle_handle {
   double dsplit[NMAX * NMAX], dhat[NMAX * NMAX], ivdm[NMAX * NMAX];
   double fup[NMAX * NMAX], flo[NMAX * NMAX], rup[NMAX * NMAX], rlo[NMAX * NMAX];
   /* scratch for oracle_rhs */
-  double *interfaces_u, *sfv, *alpha, *mortar_u[4];
+  double *interfaces_u, *sfv, *alpha, *mortar_u[4], *boundaries_u;
 };
 
 int oracle_set_threads(int nthreads) {
@@ -387,6 +389,7 @@ oracle_handle *oracle_create(const oracle_desc *desc) {
   h->interfaces_u = (double *)calloc((size_t)(2 * h->NV * h->NF * (desc->ninterfaces > 0 ? desc->ninterfaces : 1)), sizeof(double));
   h->sfv = (double *)calloc((size_t)(h->NV * h->NF * 2 * h->DIM * desc->nelements), sizeof(double));
   h->alpha = (double *)calloc((size_t)desc->nelements, sizeof(double));
+  h->boundaries_u = (double *)calloc((size_t)(2 * h->NV * h->NF * (desc->nboundaries > 0 ? desc->nboundaries : 1)), sizeof(double));
   for (int c = 0; c < h->nchild; ++c)
     h->mortar_u[c] = (double *)calloc((size_t)(2 * h->NV * h->NF * (desc->nmortars > 0 ? desc->nmortars : 1)), sizeof(double));
   return h;
@@ -394,7 +397,7 @@ oracle_handle *oracle_create(const oracle_desc *desc) {
 
 void oracle_destroy(oracle_handle *h) {
   if (!h) return;
-  free(h->interfaces_u); free(h->sfv); free(h->alpha);
+  free(h->interfaces_u); free(h->sfv); free(h->alpha); free(h->boundaries_u);
   for (int c = 0; c < 4; ++c) free(h->mortar_u[c]);
   free(h);
 }
@@ -406,6 +409,7 @@ int64_t oracle_size(oracle_handle *h, int which) {
     case 2: return (int64_t)h->NV * h->NF * 2 * h->DIM * h->d.nelements; /* surface_flux_values */
     case 3: return (int64_t)2 * h->NV * h->NF * h->d.nmortars;     /* one mortar u array */
     case 4: return h->nchild;
+    case 5: return (int64_t)2 * h->NV * h->NF * h->d.nboundaries;  /* boundaries_u */
     default: return -1;
   }
 }
@@ -752,20 +756,173 @@ void oracle_indicator_hg(oracle_handle *h, const double *u, double *alpha) {
   }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Boundary states, boundary fluxes and source terms                        */
+/* ------------------------------------------------------------------------ */
+
+/* The built-in initial conditions, also the Dirichlet boundary functions:
+ * constant state; the convergence test (advection: c + A sin(omega sum_d
+ * (x_d - a_d t)); Euler: rho = rho v_d = c + A sin(omega (sum_d x_d - t)),
+ * E = rho^2 -- a manufactured solution of the Euler equations with the
+ * source term of oracle_sources); the weak blast wave. */
+void oracle_eval_ic(oracle_handle *h, int kind, const double *params, const double *x, double t, double *u) {
+  const int DIM = h->DIM, NV = h->NV;
+  if (kind == ORC_IC_CONSTANT) {
+    for (int v = 0; v < NV; ++v) u[v] = params[v];
+    return;
+  }
+  if (kind == ORC_IC_CONVERGENCE_TEST) {
+    const double c = params[0], A = params[1], L = params[2];
+    const double omega = 2.0 * ORC_PI / L;
+    double s = 0.0;
+    if (h->P.eq == ORC_EQ_ADVECTION) {
+      for (int d = 0; d < DIM; ++d) s += x[d] - h->P.a[d] * t;
+      u[0] = c + A * sin(omega * s);
+      return;
+    }
+    for (int d = 0; d < DIM; ++d) s += x[d];
+    const double ini = c + A * sin(omega * (s - t));
+    u[0] = ini;
+    for (int d = 0; d < DIM; ++d) u[1 + d] = ini;
+    u[DIM + 1] = ini * ini;
+    return;
+  }
+  /* weak blast wave: r <= 0.5: rho 1.1691, radial velocity 0.1882, p 1.245; else 1, 0, 1.
+   * The radial direction from the polar angles phi = atan2(y, x) (and
+   * theta = acos(z / r) in 3D), so that the centre itself moves along phi = 0
+   * (theta = 0 in 3D), as the angle-based definition gives there. */
+  double r2 = 0.0, v[3] = {0.0, 0.0, 0.0};
+  for (int d = 0; d < DIM; ++d) r2 += x[d] * x[d];
+  const double r = sqrt(r2);
+  const int inside = r <= 0.5;
+  const double rho = inside ? 1.1691 : 1.0, p = inside ? 1.245 : 1.0;
+  if (inside) {
+    if (DIM == 1) {
+      v[0] = x[0] > 0.0 ? 0.1882 : (x[0] < 0.0 ? -0.1882 : 0.0);
+    } else if (DIM == 2) {
+      const double phi = atan2(x[1], x[0]);
+      v[0] = 0.1882 * cos(phi);
+      v[1] = 0.1882 * sin(phi);
+    } else {
+      const double phi = atan2(x[1], x[0]);
+      double c = r > 0.0 ? x[2] / r : 1.0;
+      c = c > 1.0 ? 1.0 : (c < -1.0 ? -1.0 : c);
+      const double theta = r > 0.0 ? acos(c) : 0.0;
+      v[0] = 0.1882 * cos(phi) * sin(theta);
+      v[1] = 0.1882 * sin(phi) * sin(theta);
+      v[2] = 0.1882 * cos(theta);
+    }
+  }
+  double kin = 0.0;
+  u[0] = rho;
+  for (int d = 0; d < DIM; ++d) {
+    u[1 + d] = rho * v[d];
+    kin += v[d] * v[d];
+  }
+  u[DIM + 1] = p / (h->P.gamma - 1.0) + 0.5 * rho * kin;
+}
+
+static const double *node_x(const oracle_handle *h, int64_t e, int n) {
+  return h->d.node_coordinates + (size_t)h->DIM * ((size_t)n + (size_t)h->NN * (size_t)e);
+}
+
+/* boundaries_u[2, nv, N^(d-1), nboundaries]: the element's trace on its side
+ * of the boundary, zero on the other (prolong_boundaries_kernel!). */
+void oracle_prolong2boundaries(oracle_handle *h, const double *u, double *bu) {
+  const int N = h->N, NN = h->NN, NF = h->NF, NV = h->NV, DIM = h->DIM;
+  const int64_t B = h->d.nboundaries;
+#pragma omp parallel for schedule(static)
+  for (int64_t b = 0; b < B; ++b) {
+    const int64_t e = h->d.boundary_neighbor_ids[b] - 1;
+    const int side = (int)h->d.boundary_neighbor_sides[b], o = (int)h->d.boundary_orientations[b] - 1;
+    for (int f = 0; f < NF; ++f)
+      for (int v = 0; v < NV; ++v) {
+        const double in = u[v + NV * (node_of(DIM, N, o, side == 1 ? N - 1 : 0, f) + (int64_t)NN * e)];
+        bu[0 + 2 * (v + NV * (f + (int64_t)NF * b))] = side == 1 ? in : 0.0;
+        bu[1 + 2 * (v + NV * (f + (int64_t)NF * b))] = side == 2 ? in : 0.0;
+      }
+  }
+}
+
+/* Dirichlet boundaries: the numerical flux between the inner trace and the
+ * boundary function's state at the face node, the inner state on the left
+ * for a boundary on the element's upper face (directions 2, 4, 6). */
+void oracle_boundary_flux(oracle_handle *h, const double *bu, double t, double *sfv) {
+  const int N = h->N, NF = h->NF, NV = h->NV, DIM = h->DIM;
+  const int64_t B = h->d.nboundaries;
+#pragma omp parallel for schedule(static)
+  for (int64_t b = 0; b < B; ++b) {
+    const int64_t e = h->d.boundary_neighbor_ids[b] - 1;
+    const int side = (int)h->d.boundary_neighbor_sides[b], o = (int)h->d.boundary_orientations[b] - 1;
+    const int dir = 2 * o + (side == 1 ? 1 : 0);
+    for (int f = 0; f < NF; ++f) {
+      double ui[NVMAX], ub[NVMAX], fs[NVMAX];
+      for (int v = 0; v < NV; ++v) ui[v] = bu[(side - 1) + 2 * (v + NV * (f + (int64_t)NF * b))];
+      const double *x = node_x(h, e, node_of(DIM, N, o, side == 1 ? N - 1 : 0, f));
+      oracle_eval_ic(h, h->d.boundary_function, h->d.boundary_params, x, t, ub);
+      if (side == 1)
+        two_point_flux(&h->P, h->d.surface_flux, ui, ub, o, fs);
+      else
+        two_point_flux(&h->P, h->d.surface_flux, ub, ui, o, fs);
+      for (int v = 0; v < NV; ++v) sfv[v + NV * (f + (int64_t)NF * (dir + 2 * DIM * e))] = fs[v];
+    }
+  }
+}
+
+/* Source term of the Euler convergence test: S = du/dt + div F(u) of the
+ * manufactured solution rho = rho v_d = c + A sin(omega (sum x - t)),
+ * E = rho^2 (derived symbolically; rho_x = omega A cos(omega (sum x - t))):
+ *   1D: (0, rho_x (g-1)(4 rho - 1)/2, same)
+ *   2D: (rho_x, rho_x (2 g rho - g - 2 rho + 2) [x2], 2 rho_x (2 g rho - g - rho + 1))
+ *   3D: (2 rho_x, rho_x (4 g rho - 3 g - 4 rho + 7)/2 [x3], rho_x (12 g rho - 9 g - 4 rho + 9)/2)
+ * added to du after the Jacobian, as calc_sources! does. */
+static void source_convergence(int DIM, double g, const double *prm, const double *x, double t, double *s) {
+  const double c = prm[0], A = prm[1], L = prm[2], omega = 2.0 * ORC_PI / L;
+  double sx = 0.0;
+  for (int d = 0; d < DIM; ++d) sx += x[d];
+  const double rho = c + A * sin(omega * (sx - t)), rx = omega * A * cos(omega * (sx - t));
+  if (DIM == 1) {
+    s[0] = 0.0;
+    s[1] = s[2] = 0.5 * rx * (g - 1.0) * (4.0 * rho - 1.0);
+  } else if (DIM == 2) {
+    s[0] = rx;
+    s[1] = s[2] = rx * (2.0 * g * rho - g - 2.0 * rho + 2.0);
+    s[3] = 2.0 * rx * (2.0 * g * rho - g - rho + 1.0);
+  } else {
+    s[0] = 2.0 * rx;
+    s[1] = s[2] = s[3] = 0.5 * rx * (4.0 * g * rho - 3.0 * g - 4.0 * rho + 7.0);
+    s[4] = 0.5 * rx * (12.0 * g * rho - 9.0 * g - 4.0 * rho + 9.0);
+  }
+}
+
+void oracle_sources(oracle_handle *h, double *du, double t) {
+  if (h->d.source_terms != ORC_SRC_CONVERGENCE_TEST || h->P.eq != ORC_EQ_EULER) return;
+  const int NN = h->NN, NV = h->NV;
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < h->d.nelements; ++e)
+    for (int n = 0; n < NN; ++n) {
+      double s[NVMAX];
+      source_convergence(h->DIM, h->P.gamma, h->d.source_params, node_x(h, e, n), t, s);
+      for (int v = 0; v < NV; ++v) du[v + NV * (n + (int64_t)NN * e)] += s[v];
+    }
+}
+
 void oracle_rhs(oracle_handle *h, double *du, const double *u, double t) {
-  (void)t;
   if (h->d.volume_integral == ORC_VOL_SHOCK_HG) oracle_indicator_hg(h, u, h->alpha);
   oracle_volume_integral(h, du, u, h->alpha);
   oracle_prolong2interfaces(h, u, h->interfaces_u);
   oracle_interface_flux(h, h->interfaces_u, h->sfv);
-  /* periodic TreeMesh: prolong2boundaries / boundary_flux are no-ops (src/solvers/dg_2d.jl:419-450) */
+  if (h->d.nboundaries > 0) {  /* periodic meshes have none (src/solvers/dg_2d.jl:419-450) */
+    oracle_prolong2boundaries(h, u, h->boundaries_u);
+    oracle_boundary_flux(h, h->boundaries_u, t, h->sfv);
+  }
   if (h->d.nmortars > 0) {
     oracle_prolong2mortars(h, u, h->mortar_u);
     oracle_mortar_flux(h, h->mortar_u, h->sfv);
   }
   oracle_surface_integral(h, du, h->sfv);
   oracle_jacobian(h, du);
-  /* no source terms */
+  oracle_sources(h, du, t);
 }
 
 /* CarpenterKennedy2N54 (Carpenter & Kennedy 1994, five-stage fourth-order,

@@ -36,6 +36,8 @@ extern "C" {
 enum { ORC_EQ_ADVECTION = 0, ORC_EQ_EULER = 1 };
 enum { ORC_VOL_WEAK = 0, ORC_VOL_FLUXDIFF = 1, ORC_VOL_SHOCK_HG = 2 };
 enum { ORC_FLUX_LLF = 0, ORC_FLUX_RANOCHA = 1, ORC_FLUX_CENTRAL = 2, ORC_FLUX_LLF_NAIVE = 3 };
+enum { ORC_IC_CONSTANT = 0, ORC_IC_CONVERGENCE_TEST = 1, ORC_IC_WEAK_BLAST_WAVE = 2 };
+enum { ORC_SRC_NONE = 0, ORC_SRC_CONVERGENCE_TEST = 1 };
 
 typedef struct {
   int32_t ndims, polydeg, nvars, equation;
@@ -51,6 +53,17 @@ typedef struct {
   const int64_t *mortar_neighbor_ids;       /* [2^(ndims-1)+1, nmortars], 1-based */
   const int64_t *mortar_large_sides;        /* [nmortars], 1 or 2 */
   const int64_t *mortar_orientations;       /* [nmortars], 1..ndims */
+  /* non-periodic meshes: the boundaries container (containers_2d.jl) and the
+   * Dirichlet boundary function, an ORC_IC_* kind evaluated at (x, t) */
+  int64_t nboundaries;
+  const int64_t *boundary_neighbor_ids;     /* [nboundaries], 1-based */
+  const int64_t *boundary_neighbor_sides;   /* [nboundaries], 1: element left of it, 2: right */
+  const int64_t *boundary_orientations;     /* [nboundaries], 1..ndims */
+  int32_t boundary_function;                /* ORC_IC_* */
+  int32_t source_terms;                     /* ORC_SRC_* */
+  double boundary_params[8];                /* constant state, or (c, A, L) of the convergence test */
+  double source_params[3];                  /* (c, A, L) of the manufactured solution */
+  const double *node_coordinates;           /* [ndims, N^ndims, nelements] (needed with boundaries / sources) */
 } oracle_desc;
 
 typedef struct oracle_handle oracle_handle;
@@ -75,6 +88,11 @@ void oracle_mortar_flux(oracle_handle *h, double *const *mortar_u, double *surfa
 void oracle_surface_integral(oracle_handle *h, double *du, const double *surface_flux_values);
 void oracle_jacobian(oracle_handle *h, double *du);
 void oracle_indicator_hg(oracle_handle *h, const double *u, double *alpha);
+void oracle_prolong2boundaries(oracle_handle *h, const double *u, double *boundaries_u);
+void oracle_boundary_flux(oracle_handle *h, const double *boundaries_u, double t, double *surface_flux_values);
+void oracle_sources(oracle_handle *h, double *du, double t);
+/* the boundary function / initial conditions at one point */
+void oracle_eval_ic(oracle_handle *h, int kind, const double *params, const double *x, double t, double *u);
 
 /* Whole right-hand side and the CarpenterKennedy2N54 time stepper. */
 void oracle_rhs(oracle_handle *h, double *du, const double *u, double t);

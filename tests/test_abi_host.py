@@ -62,7 +62,8 @@ def _create(d):
 
 @pytest.mark.parametrize("field,value,status", [
     ("ndims", 4, 1), ("polydeg", 9, 2), ("nvars", 3, 1), ("equation", 7, 1),
-    ("volume_integral", 5, 1), ("surface_flux", 9, 1), ("precision", 3, 1), ("nboundaries", 4, 2),
+    ("volume_integral", 5, 1), ("surface_flux", 9, 1), ("precision", 3, 1), ("nboundaries", 4, 1),
+    ("source_terms", 3, 1), ("nboundary_params", 9, 1),
     ("gamma", 1.0, 1), ("nelements", 0, 1),
 ])
 def test_create_rejects_bad_fields(field, value, status):
@@ -71,6 +72,39 @@ def test_create_rejects_bad_fields(field, value, status):
     st, msg = _create(d)
     assert st == status, msg
     assert msg
+
+
+def test_create_rejects_bad_boundaries():
+    import trixicuda as T
+    from trixicuda.semidiscretization import build_problem_desc
+
+    # a boundary declared on a face that a (periodic) interface already connects
+    d, keep, _ = _desc_from_mesh()
+    keep["fake_b"] = np.array([1], dtype=np.int64)
+    ptr = keep["fake_b"].ctypes.data_as(C.POINTER(C.c_int64))
+    d.nboundaries, d.boundary_function = 1, 1
+    d.boundary_neighbor_ids = d.boundary_neighbor_sides = d.boundary_orientations = ptr
+    st, msg = _create(d)
+    assert st == 7 and "already connected" in msg
+    # a non-periodic mesh needs a boundary function, and each boundary face a declaration
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEMGPU(polydeg=2)
+    mesh = T.TreeMesh((0, 0), (2, 2), initial_refinement_level=2, periodicity=False)
+    bc = T.BoundaryConditionDirichlet(T.initial_condition_convergence_test)
+    d, keep, _ = build_problem_desc(mesh, eq, solver, boundary_conditions=bc)
+    d.boundary_function = 7
+    st, msg = _create(d)
+    assert st == 1 and "boundary_function" in msg
+    d, keep, _ = build_problem_desc(mesh, eq, solver, boundary_conditions=bc)
+    d.nboundaries = d.nboundaries - 1
+    st, msg = _create(d)
+    assert st == 7 and "no interface, mortar or boundary" in msg
+    # the convergence-test source is defined for the Euler equations only
+    adv = T.LinearScalarAdvectionEquation2D((1.0, 1.0))
+    d, keep, _ = build_problem_desc(mesh, adv, solver, boundary_conditions=bc)
+    d.source_terms = 1
+    st, msg = _create(d)
+    assert st == 2 and "Euler" in msg
 
 
 def test_create_rejects_corrupted_connectivity():

@@ -17,6 +17,7 @@
 #include "basis.h"
 #include "dg_analysis.h"
 #include "dg_host.h"
+#include "dg_ic.cuh"
 #include "dg_physics.cuh"
 
 namespace trixi {
@@ -204,64 +205,7 @@ __global__ void reduce_columns(int64_t E, int nq, const double *__restrict__ par
   }
 }
 
-// ---------------------------------------------------------------------------
-// initial conditions
-// ---------------------------------------------------------------------------
-template <int DIM, int EQ>
-__device__ void eval_ic(int kind, const double *x, double t, const IcParams &ip, double *u) {
-  constexpr int NV = NVarsOf<DIM, EQ>::value;
-  if (kind == IC_CONSTANT) {
-    for (int v = 0; v < NV; ++v) u[v] = ip.p[v];
-    return;
-  }
-  if (kind == IC_CONVERGENCE_TEST) {
-    const double c = ip.p[0], A = ip.p[1], L = ip.p[2];
-    const double omega = 2.0 * 3.14159265358979323846 / L;
-    if (EQ == EQ_ADV) {
-      double s = 0.0;
-      for (int d = 0; d < DIM; ++d) s += x[d] - ip.a[d] * t;
-      u[0] = c + A * sin(omega * s);
-    } else {
-      double s = 0.0;
-      for (int d = 0; d < DIM; ++d) s += x[d];
-      const double ini = c + A * sin(omega * (s - t));
-      u[0] = ini;
-      for (int d = 0; d < DIM; ++d) u[1 + d] = ini;
-      u[DIM + 1] = ini * ini;
-    }
-    return;
-  }
-  // IC_WEAK_BLAST_WAVE (Euler): inside r <= 0.5 rho 1.1691, radial v 0.1882, p 1.245
-  double r2 = 0.0;
-  for (int d = 0; d < DIM; ++d) r2 += x[d] * x[d];
-  const double r = sqrt(r2);
-  const bool out = r > 0.5;
-  const double rho = out ? 1.0 : 1.1691, p = out ? 1.0 : 1.245;
-  double v[3] = {0.0, 0.0, 0.0};
-  if (!out) {
-    if (DIM == 1) {
-      v[0] = 0.1882 * (x[0] > 0 ? 1.0 : (x[0] < 0 ? -1.0 : 0.0));
-    } else if (DIM == 2) {
-      const double phi = atan2(x[1], x[0]);
-      v[0] = 0.1882 * cos(phi);
-      v[1] = 0.1882 * sin(phi);
-    } else {
-      const double phi = atan2(x[1], x[0]);
-      const double theta = (r == 0.0) ? 0.0 : acos(fmin(1.0, fmax(-1.0, x[2] / r)));
-      v[0] = 0.1882 * cos(phi) * sin(theta);
-      v[1] = 0.1882 * sin(phi) * sin(theta);
-      v[2] = 0.1882 * cos(theta);
-    }
-  }
-  double kin = 0.0;
-  u[0] = rho;
-  for (int d = 0; d < DIM; ++d) {
-    u[1 + d] = rho * v[d];
-    kin += v[d] * v[d];
-  }
-  u[DIM + 1] = p / (ip.gamma - 1.0) + 0.5 * rho * kin;
-}
-
+// initial conditions: eval_ic (dg_ic.cuh)
 // one ulp towards +inf / -inf for finite x (IEEE-754 bit-pattern order)
 __device__ __forceinline__ double next_up(double x) {
   if (x == 0.0) return 4.9406564584124654e-324;

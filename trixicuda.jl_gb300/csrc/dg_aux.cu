@@ -6,6 +6,7 @@
 #include <algorithm>
 
 #include "dg_host.h"
+#include "dg_ic.cuh"
 #include "dg_physics.cuh"
 
 namespace trixi {
@@ -258,7 +259,7 @@ __global__ void indicator_smooth_kernel(int dim, int64_t E, const double *__rest
       const int32_t nb = face_table[e * 2 * dim + f];
       if (nb >= 0) {
         a = fmax(a, 0.5 * alpha_raw[nb]);
-      } else {
+      } else if (nb != FACE_BOUNDARY) {  // a domain boundary has no neighbour to smooth with
         const int32_t slot = -nb - 1;
         for (int j = 0; j < 4; ++j) {
           const int32_t n2 = slot_nbrs[slot * 4 + j];
@@ -316,6 +317,77 @@ __global__ void prolong_interfaces_kernel(int dim, int N, int nv, int64_t I, con
   const int64_t left = nid[2 * k] - 1, right = nid[2 * k + 1] - 1;
   iu[2 * idx + 0] = u[(left * NN + node_of(dim, N, o, N - 1, f)) * nv + v];
   iu[2 * idx + 1] = u[(right * NN + node_of(dim, N, o, 0, f)) * nv + v];
+}
+
+// prolong_boundaries_kernel! (dg_2d_kernel.jl:1037-1064): boundaries_u[2, nv,
+// NF, B] holds the element's trace on its side of the boundary (index 1 when
+// the element lies on the left, 2 on the right) and zero on the other side
+__global__ void prolong_boundaries_kernel(int dim, int N, int nv, int64_t B, const double *__restrict__ u,
+                                          const int64_t *__restrict__ nid, const int64_t *__restrict__ side,
+                                          const int64_t *__restrict__ ori, double *__restrict__ bu) {
+  int NF = 1;
+  for (int d = 1; d < dim; ++d) NF *= N;
+  const int NN = NF * N;
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= B * NF * nv) return;
+  const int v = (int)(idx % nv);
+  const int f = (int)((idx / nv) % NF);
+  const int64_t b = idx / ((int64_t)nv * NF);
+  const int o = (int)ori[b] - 1, sd = (int)side[b];
+  const int64_t e = nid[b] - 1;
+  const double in = u[(e * NN + node_of(dim, N, o, sd == 1 ? N - 1 : 0, f)) * nv + v];
+  bu[2 * idx + 0] = sd == 1 ? in : 0.0;
+  bu[2 * idx + 1] = sd == 2 ? in : 0.0;
+}
+
+// boundary_flux_kernel! (dg_2d_kernel.jl:1067-1110) for Dirichlet boundaries:
+// the surface flux between the inner trace and the boundary function's state
+// at the face node, the inner state on the left when the boundary is the
+// element's upper face (directions 2, 4, 6)
+template <int DIM, int EQ>
+__global__ void boundary_flux_kernel(int N, int64_t B, const double *__restrict__ bu,
+                                     const double *__restrict__ coords, const int64_t *__restrict__ nid,
+                                     const int64_t *__restrict__ side, const int64_t *__restrict__ ori, double t,
+                                     int bc_kind, IcParams bc, int kind, PhysParams<double> pp,
+                                     double *__restrict__ sfv) {
+  constexpr int NV = NVarsOf<DIM, EQ>::value;
+  const int NF = (DIM == 1) ? 1 : (DIM == 2 ? N : N * N);
+  const int NN = NF * N;
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= B * NF) return;
+  const int f = (int)(idx % NF);
+  const int64_t b = idx / NF;
+  const int o = (int)ori[b] - 1, sd = (int)side[b];
+  const int64_t e = nid[b] - 1;
+  double ui[NV], wi[NV], ub[NV], wb[NV], fs[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) ui[v] = bu[2 * ((b * NF + f) * NV + v) + (sd - 1)];
+  eval_ic<DIM, EQ>(bc_kind, coords + (e * NN + node_of(DIM, N, o, sd == 1 ? N - 1 : 0, f)) * DIM, t, bc, ub);
+  Physics<DIM, EQ, double>::prim(ui, wi, pp);
+  Physics<DIM, EQ, double>::prim(ub, wb, pp);
+  if (sd == 1)
+    flux_dispatch<DIM, EQ, double>(kind, o, ui, wi, ub, wb, fs, pp);
+  else
+    flux_dispatch<DIM, EQ, double>(kind, o, ub, wb, ui, wi, fs, pp);
+  const int dir = 2 * o + (sd == 1 ? 1 : 0);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) sfv[v + NV * (f + (int64_t)NF * (dir + 2 * DIM * e))] = fs[v];
+}
+
+// calc_sources!: du += source(x, t) at every node (after the Jacobian)
+template <int DIM, int EQ>
+__global__ void sources_kernel(int N, int64_t E, const double *__restrict__ coords, double t, double c, double A,
+                               double L, double gamma, double *__restrict__ du) {
+  constexpr int NV = NVarsOf<DIM, EQ>::value;
+  int NN = 1;
+  for (int d = 0; d < DIM; ++d) NN *= N;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= E * NN) return;
+  const double prm[3] = {c, A, L};
+  double s[NV];
+  source_convergence<DIM, EQ>(prm, gamma, coords + q * DIM, t, s);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) du[q * NV + v] += s[v];
 }
 
 // surface_flux_kernel! + interface_flux_kernel! (dg_2d_kernel.jl:938-1006)
@@ -533,6 +605,58 @@ cudaError_t stage_interface_flux(const StageHost &sh, cudaStream_t s) {
     case 3: return adv ? launch_iflux<3, EQ_ADV>(sh, s) : launch_iflux<3, EQ_EULER>(sh, s);
   }
   return cudaErrorNotSupported;
+}
+
+cudaError_t stage_prolong2boundaries(const StageHost &sh, const double *u, cudaStream_t s) {
+  if (sh.nboundaries == 0) return cudaSuccess;
+  const int NF = (sh.dim == 1) ? 1 : (sh.dim == 2 ? sh.N : sh.N * sh.N);
+  const int64_t n = sh.nboundaries * NF * sh.nv;
+  prolong_boundaries_kernel<<<blocks_for(n, 256), 256, 0, s>>>(sh.dim, sh.N, sh.nv, sh.nboundaries, u,
+                                                             sh.bnd_neighbor_ids, sh.bnd_sides, sh.bnd_orientations,
+                                                             sh.boundaries_u);
+  return cudaGetLastError();
+}
+
+template <int DIM, int EQ>
+static cudaError_t launch_bflux(const StageHost &sh, double t, cudaStream_t s) {
+  const int NF = (DIM == 1) ? 1 : (DIM == 2 ? sh.N : sh.N * sh.N);
+  const int64_t n = sh.nboundaries * NF;
+  boundary_flux_kernel<DIM, EQ><<<blocks_for(n, 128), 128, 0, s>>>(
+      sh.N, sh.nboundaries, sh.boundaries_u, sh.coords, sh.bnd_neighbor_ids, sh.bnd_sides, sh.bnd_orientations, t,
+      sh.bc_kind, sh.bc, sh.surface_flux, make_pp<double>(sh.gamma, sh.adv), sh.sfv);
+  return cudaGetLastError();
+}
+
+cudaError_t stage_boundary_flux(const StageHost &sh, double t, cudaStream_t s) {
+  if (sh.nboundaries == 0) return cudaSuccess;
+  const bool adv = sh.eq == EQ_ADV;
+  switch (sh.dim) {
+    case 1: return adv ? launch_bflux<1, EQ_ADV>(sh, t, s) : launch_bflux<1, EQ_EULER>(sh, t, s);
+    case 2: return adv ? launch_bflux<2, EQ_ADV>(sh, t, s) : launch_bflux<2, EQ_EULER>(sh, t, s);
+    case 3: return adv ? launch_bflux<3, EQ_ADV>(sh, t, s) : launch_bflux<3, EQ_EULER>(sh, t, s);
+  }
+  return cudaErrorNotSupported;
+}
+
+cudaError_t stage_sources(const StageHost &sh, double *du, double t, cudaStream_t s) {
+  if (sh.src_kind != SRC_CONVERGENCE_TEST || sh.eq != EQ_EULER) return cudaSuccess;
+  int NN = 1;
+  for (int d = 0; d < sh.dim; ++d) NN *= sh.N;
+  const int64_t n = sh.nelements * NN;
+  switch (sh.dim) {
+    case 1:
+      sources_kernel<1, EQ_EULER><<<blocks_for(n, 256), 256, 0, s>>>(sh.N, sh.nelements, sh.coords, t, sh.src[0],
+                                                                     sh.src[1], sh.src[2], sh.gamma, du);
+      break;
+    case 2:
+      sources_kernel<2, EQ_EULER><<<blocks_for(n, 256), 256, 0, s>>>(sh.N, sh.nelements, sh.coords, t, sh.src[0],
+                                                                     sh.src[1], sh.src[2], sh.gamma, du);
+      break;
+    default:
+      sources_kernel<3, EQ_EULER><<<blocks_for(n, 256), 256, 0, s>>>(sh.N, sh.nelements, sh.coords, t, sh.src[0],
+                                                                     sh.src[1], sh.src[2], sh.gamma, du);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t stage_prolong2mortars(const StageHost &sh, const double *u, cudaStream_t s) {

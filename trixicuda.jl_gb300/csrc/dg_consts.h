@@ -1,6 +1,7 @@
 // dg_consts.h -- enumerations shared by host code and kernels.  The numeric
 // values equal the public trixi_* enums of include/trixi_b200.h.
 #pragma once
+#include <cstdint>
 
 namespace trixi {
 
@@ -19,5 +20,9 @@ constexpr int VOL_SC = 2;    // TRIXI_VOLUME_SHOCK_CAPTURING_HG
 constexpr int MODE_VOLUME = 0;  // du = volume integral only (stage API)
 constexpr int MODE_RHS = 1;     // du = full rhs
 constexpr int MODE_RK = 2;      // k = a k + dt rhs; u_out = u_in + b k
+
+// face-table entry of a face on a non-periodic domain boundary (neighbours
+// are >= 0, mortar slots -(slot+1))
+constexpr int32_t FACE_BOUNDARY = INT32_MIN;
 
 }  // namespace trixi

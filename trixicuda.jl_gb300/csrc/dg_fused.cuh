@@ -28,6 +28,7 @@
 // performs the RK update, in the reference layout.
 #pragma once
 #include "dg_convert.cuh"
+#include "dg_ic.cuh"
 #include "dg_physics.cuh"
 
 namespace trixi {
@@ -52,6 +53,13 @@ struct FusedParams {
   double rk_a, rk_b, dt;
   int use_k;                                // RK: read k (rk_a != 0)
   int wpg, gpb;                             // tile: warps per group, groups per block
+  // non-periodic meshes and source terms
+  const double *__restrict__ coords;        // [E][NN][DIM] node coordinates (boundaries / sources)
+  double t;                                 // time of this rhs evaluation
+  int bc_kind;                              // Dirichlet boundary function (IC_* kind)
+  int src_kind;                             // SRC_*
+  IcParams bc;                              // its parameters
+  double src[3];                            // (c, A, L) of the convergence-test source
   int vec16;                                // u_in, out, k, mortar_flux 16-byte aligned
   double atol;                              // dg-only test for alpha
   PhysParams<R> pp;
@@ -182,7 +190,11 @@ __device__ __forceinline__ void stg_node(double *dst, const double *src, bool ve
 
 constexpr int round_up4(int x) { return (x + 3) & ~3; }
 
-template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX>
+// BND = 1: the instantiation for non-periodic meshes and source terms (the
+// Dirichlet states of boundary faces in phase A, the source in phase C);
+// BND = 0 carries none of that code, so the periodic kernels keep their
+// registers.
+template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX, int BND = 0>
 struct FusedKernel {
   using P = Physics<DIM, EQ, R>;
   static constexpr int NV = P::NV;
@@ -433,21 +445,28 @@ struct FusedKernel {
         const int el = j / PER_EL, r = j - (j / PER_EL) * PER_EL;
         const int face = r / NF, t = r - (r / NF) * NF;
         const int32_t nb = p.face_table[(e0 + el) * (2 * DIM) + face];
-        const double *src;
+        double tv[NV];
         if (nb >= 0) {
           const int o = face >> 1;
           const int other = line_node_rt<DIM, N>(o, t, (face & 1) ? 0 : N - 1);
-          src = p.u_in + ((int64_t)nb * NN + other) * NV;
+          ldg_node<NV>(p.u_in + ((int64_t)nb * NN + other) * NV, tv, vec);
+        } else if (BND && nb == FACE_BOUNDARY) {
+          // Dirichlet boundary: the boundary function's state at the face node
+          // plays the neighbour's trace (the surface flux then follows the
+          // interface convention: inner state on the left of an upper face)
+          if constexpr (BND) {
+            const int o = face >> 1;
+            const int own = line_node_rt<DIM, N>(o, t, (face & 1) ? N - 1 : 0);
+            eval_ic<DIM, EQ>(p.bc_kind, p.coords + ((e0 + el) * NN + own) * DIM, p.t, p.bc, tv);
+          }
         } else {
-          src = p.mortar_flux + ((int64_t)(-nb - 1) * NF + t) * NV;
+          ldg_node<NV>(p.mortar_flux + ((int64_t)(-nb - 1) * NF + t) * NV, tv, vec);
         }
-        double tv[NV];
-        ldg_node<NV>(src, tv, vec);
         R tr[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) tr[v] = from_double<R>(tv[v]);
         sts_rec<NV>(s.tr(el, face, t), tr);
-        if (t == 0) s.conforming[el * 2 * DIM + face] = (nb >= 0);
+        if (t == 0) s.conforming[el * 2 * DIM + face] = (nb >= 0 || (BND && nb == FACE_BOUNDARY));
       }
     }
     if (has_node) {
@@ -614,9 +633,16 @@ struct FusedKernel {
     } else if constexpr (sizeof(R) == sizeof(double)) {
       const double sc = -p.inv_jac[e0 + el];
       const double dte = p.dt_elem ? p.dt_elem[e0 + el] : p.dt;
+      double src[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) src[v] = 0.0;
+      if constexpr (BND) {
+        if (p.src_kind == SRC_CONVERGENCE_TEST)
+          source_convergence<DIM, EQ>(p.src, p.bc.gamma, p.coords + ((e0 + el) * NN + node) * DIM, p.t, src);
+      }
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        const double du = double(acc[v]) * sc;
+        const double du = double(acc[v]) * sc + src[v];
         if (mode == MODE_RHS) {
           o[v] = du;
         } else {
@@ -630,9 +656,20 @@ struct FusedKernel {
       // mixed precision: scale in FP32, widen exactly, accumulate the RK
       // register and the state in FP64 (two FMAs on the FP64 pipe)
       const R sc = s.scale[el];
+      double src[NV];  // FP64 source term, times dt in the RK form (sc holds -J^{-1} dt there)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) src[v] = 0.0;
+      if constexpr (BND) {
+        if (p.src_kind == SRC_CONVERGENCE_TEST) {
+          source_convergence<DIM, EQ>(p.src, p.bc.gamma, p.coords + ((e0 + el) * NN + node) * DIM, p.t, src);
+          const double f = (mode == MODE_RK) ? (p.dt_elem ? p.dt_elem[e0 + el] : p.dt) : 1.0;
+#pragma unroll
+          for (int v = 0; v < NV; ++v) src[v] *= f;
+        }
+      }
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        const double dd = to_double(acc[v] * sc);
+        const double dd = to_double(acc[v] * sc) + src[v];
         if (mode == MODE_RHS) {
           o[v] = dd;
         } else {
@@ -646,9 +683,9 @@ struct FusedKernel {
   }
 };
 
-template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX>
+template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX, int BND>
 __global__ void __launch_bounds__(512) dg_fused_kernel(const FusedParams<R> p) {
-  FusedKernel<DIM, N, EQ, R, VOL, VFLUX>::run(p);
+  FusedKernel<DIM, N, EQ, R, VOL, VFLUX, BND>::run(p);
 }
 
 }  // namespace trixi

@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "dg_analysis.h"
 #include "dg_consts.h"
 
 namespace trixi {
@@ -40,6 +41,12 @@ struct FusedHost {
   // kernel's tile limits instead of launching
   int wpg = 0, gpb = 0;
   struct FusedTile *tile_out = nullptr;
+  // non-periodic meshes and source terms
+  const double *coords = nullptr;  // [E][NN][DIM]
+  double t = 0.0;
+  int bc_kind = -1, src_kind = 0;
+  IcParams bc{};
+  double src[3] = {0, 0, 0};
 };
 
 // Tile limits of one fused-kernel instantiation.
@@ -56,6 +63,12 @@ cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed,
 bool fused_supported(int dim, int N, int eq, int vol, int vflux);
 
 cudaError_t launch_fused_1d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_1d_f32_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_1d_f64_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_2d_f32_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_2d_f64_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_3d_f32_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_3d_f64_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 cudaError_t launch_fused_2d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 cudaError_t launch_fused_3d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 cudaError_t launch_fused_1d_f32(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
@@ -111,8 +124,19 @@ struct StageHost {
   double rev_up[HOST_NMAX * HOST_NMAX] = {}, rev_lo[HOST_NMAX * HOST_NMAX] = {};
   double lhat_l = 0, lhat_r = 0;
   const double *inv_jac = nullptr;
+  // non-periodic meshes and source terms
+  int64_t nboundaries = 0;
+  const int64_t *bnd_neighbor_ids = nullptr, *bnd_sides = nullptr, *bnd_orientations = nullptr;
+  double *boundaries_u = nullptr;  // [B][NF][nv][2]
+  const double *coords = nullptr;  // [E][NN][DIM]
+  int bc_kind = -1, src_kind = 0;
+  IcParams bc{};
+  double src[3] = {0, 0, 0};
 };
 cudaError_t stage_prolong2interfaces(const StageHost &sh, const double *u, cudaStream_t s);
+cudaError_t stage_prolong2boundaries(const StageHost &sh, const double *u, cudaStream_t s);
+cudaError_t stage_boundary_flux(const StageHost &sh, double t, cudaStream_t s);
+cudaError_t stage_sources(const StageHost &sh, double *du, double t, cudaStream_t s);
 cudaError_t stage_interface_flux(const StageHost &sh, cudaStream_t s);
 cudaError_t stage_prolong2mortars(const StageHost &sh, const double *u, cudaStream_t s);
 cudaError_t stage_mortar_flux(const StageHost &sh, cudaStream_t s);

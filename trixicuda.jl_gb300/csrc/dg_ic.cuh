@@ -1,0 +1,105 @@
+// dg_ic.cuh -- the built-in initial conditions (also the Dirichlet boundary
+// functions of non-periodic meshes) and the source term of the Euler
+// convergence test, evaluated pointwise on the device in FP64.
+#pragma once
+#include "dg_analysis.h"
+#include "dg_physics.cuh"
+
+namespace trixi {
+
+constexpr int SRC_NONE = 0;              // TRIXI_SOURCE_NONE
+constexpr int SRC_CONVERGENCE_TEST = 1;  // TRIXI_SOURCE_CONVERGENCE_TEST
+
+template <int DIM, int EQ>
+__device__ void eval_ic(int kind, const double *x, double t, const IcParams &ip, double *u) {
+  constexpr int NV = NVarsOf<DIM, EQ>::value;
+  if (kind == IC_CONSTANT) {
+    for (int v = 0; v < NV; ++v) u[v] = ip.p[v];
+    return;
+  }
+  if (kind == IC_CONVERGENCE_TEST) {
+    const double c = ip.p[0], A = ip.p[1], L = ip.p[2];
+    const double omega = 2.0 * 3.14159265358979323846 / L;
+    if (EQ == EQ_ADV) {
+      double s = 0.0;
+      for (int d = 0; d < DIM; ++d) s += x[d] - ip.a[d] * t;
+      u[0] = c + A * sin(omega * s);
+    } else {
+      double s = 0.0;
+      for (int d = 0; d < DIM; ++d) s += x[d];
+      const double ini = c + A * sin(omega * (s - t));
+      u[0] = ini;
+      for (int d = 0; d < DIM; ++d) u[1 + d] = ini;
+      u[DIM + 1] = ini * ini;
+    }
+    return;
+  }
+  // IC_WEAK_BLAST_WAVE (Euler): inside r <= 0.5 rho 1.1691, radial v 0.1882, p 1.245
+  double r2 = 0.0;
+  for (int d = 0; d < DIM; ++d) r2 += x[d] * x[d];
+  const double r = sqrt(r2);
+  const bool out = r > 0.5;
+  const double rho = out ? 1.0 : 1.1691, p = out ? 1.0 : 1.245;
+  double v[3] = {0.0, 0.0, 0.0};
+  if (!out) {
+    if (DIM == 1) {
+      v[0] = 0.1882 * (x[0] > 0 ? 1.0 : (x[0] < 0 ? -1.0 : 0.0));
+    } else if (DIM == 2) {
+      const double phi = atan2(x[1], x[0]);
+      v[0] = 0.1882 * cos(phi);
+      v[1] = 0.1882 * sin(phi);
+    } else {
+      const double phi = atan2(x[1], x[0]);
+      const double theta = (r == 0.0) ? 0.0 : acos(fmin(1.0, fmax(-1.0, x[2] / r)));
+      v[0] = 0.1882 * cos(phi) * sin(theta);
+      v[1] = 0.1882 * sin(phi) * sin(theta);
+      v[2] = 0.1882 * cos(theta);
+    }
+  }
+  double kin = 0.0;
+  u[0] = rho;
+  for (int d = 0; d < DIM; ++d) {
+    u[1 + d] = rho * v[d];
+    kin += v[d] * v[d];
+  }
+  u[DIM + 1] = p / (ip.gamma - 1.0) + 0.5 * rho * kin;
+}
+
+
+// Source term of the Euler convergence test: S = du/dt + div F(u) for the
+// manufactured solution rho = rho v_d = c + A sin(omega (sum_d x_d - t)),
+// E = rho^2 (derived symbolically; rho_x = omega A cos(omega (sum_d x_d - t)),
+// g = gamma):
+//   1D: (0, rho_x (g-1)(4 rho - 1)/2, same)
+//   2D: (rho_x, rho_x (2 g rho - g - 2 rho + 2) [x2], 2 rho_x (2 g rho - g - rho + 1))
+//   3D: (2 rho_x, rho_x (4 g rho - 3 g - 4 rho + 7)/2 [x3], rho_x (12 g rho - 9 g - 4 rho + 9)/2)
+// prm = (c, A, L).  Linear advection has none (its convergence test is exact).
+template <int DIM, int EQ>
+__device__ __forceinline__ void source_convergence(const double *prm, double g, const double *x, double t,
+                                                   double *s) {
+  if constexpr (EQ == EQ_EULER) {
+    const double omega = 2.0 * 3.14159265358979323846 / prm[2];
+    double sx = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) sx += x[d];
+    double sn, cs;
+    sincos(omega * (sx - t), &sn, &cs);
+    const double rho = prm[0] + prm[1] * sn, rx = omega * prm[1] * cs;
+    if constexpr (DIM == 1) {
+      s[0] = 0.0;
+      s[1] = s[2] = 0.5 * rx * (g - 1.0) * (4.0 * rho - 1.0);
+    } else if constexpr (DIM == 2) {
+      s[0] = rx;
+      s[1] = s[2] = rx * (2.0 * g * rho - g - 2.0 * rho + 2.0);
+      s[3] = 2.0 * rx * (2.0 * g * rho - g - rho + 1.0);
+    } else {
+      s[0] = 2.0 * rx;
+      s[1] = s[2] = s[3] = 0.5 * rx * (4.0 * g * rho - 3.0 * g - 4.0 * rho + 7.0);
+      s[4] = 0.5 * rx * (12.0 * g * rho - 9.0 * g - 4.0 * rho + 9.0);
+    }
+  } else {
+    s[0] = 0.0;
+  }
+}
+
+}  // namespace trixi

@@ -9,9 +9,9 @@
 
 namespace trixi {
 
-template <int DIM, int N, int EQ, typename R, int VOL, int VF>
+template <int DIM, int N, int EQ, typename R, int VOL, int VF, int BND>
 cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
-  using K = FusedKernel<DIM, N, EQ, R, VOL, VF>;
+  using K = FusedKernel<DIM, N, EQ, R, VOL, VF, BND>;
   FusedParams<R> p;
   p.u_in = h.u_in;
   p.out = h.out;
@@ -30,6 +30,12 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   p.rk_b = h.rk_b;
   p.dt = h.dt;
   p.use_k = (h.rk_a != 0.0);
+  p.coords = h.coords;
+  p.t = h.t;
+  p.bc_kind = h.bc_kind;
+  p.src_kind = h.src_kind;
+  p.bc = h.bc;
+  for (int i = 0; i < 3; ++i) p.src[i] = h.src[i];
   const uintptr_t addr_bits = (uintptr_t)h.u_in | (uintptr_t)h.out | (uintptr_t)h.k | (uintptr_t)h.mortar_flux;
   p.vec16 = (addr_bits & 15u) == 0;
   p.atol = h.atol;
@@ -70,45 +76,45 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   const int block = 32 * wpg * gpb;
   const size_t smem = (size_t)gpb * K::GROUP_SMEM;
   // opt in once per instantiation to the large dynamic shared-memory carve-out
-  static const cudaError_t attr = cudaFuncSetAttribute(dg_fused_kernel<DIM, N, EQ, R, VOL, VF>,
+  static const cudaError_t attr = cudaFuncSetAttribute(dg_fused_kernel<DIM, N, EQ, R, VOL, VF, BND>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (attr != cudaSuccess) return attr;
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   const int64_t grid = (h.nelements + epb - 1) / epb;
   if (grid <= 0) return cudaSuccess;
   if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
-  dg_fused_kernel<DIM, N, EQ, R, VOL, VF><<<(unsigned)grid, block, smem, s>>>(p);
+  dg_fused_kernel<DIM, N, EQ, R, VOL, VF, BND><<<(unsigned)grid, block, smem, s>>>(p);
   return cudaGetLastError();
 }
 
-template <int DIM, int N, typename R>
+template <int DIM, int N, typename R, int BND>
 cudaError_t launch_n(int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s) {
   if (eq == EQ_ADV) {
-    if (vol == VOL_WEAK) return launch_one<DIM, N, EQ_ADV, R, VOL_WEAK, FLUX_CENTRAL>(h, s);
-    if (vol == VOL_FD) return launch_one<DIM, N, EQ_ADV, R, VOL_FD, FLUX_CENTRAL>(h, s);
+    if (vol == VOL_WEAK) return launch_one<DIM, N, EQ_ADV, R, VOL_WEAK, FLUX_CENTRAL, BND>(h, s);
+    if (vol == VOL_FD) return launch_one<DIM, N, EQ_ADV, R, VOL_FD, FLUX_CENTRAL, BND>(h, s);
     return cudaErrorNotSupported;
   }
-  if (vol == VOL_WEAK) return launch_one<DIM, N, EQ_EULER, R, VOL_WEAK, FLUX_CENTRAL>(h, s);
+  if (vol == VOL_WEAK) return launch_one<DIM, N, EQ_EULER, R, VOL_WEAK, FLUX_CENTRAL, BND>(h, s);
   if (vol == VOL_FD) {
-    if (vflux == FLUX_RANOCHA) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_RANOCHA>(h, s);
-    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_CENTRAL>(h, s);
+    if (vflux == FLUX_RANOCHA) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_RANOCHA, BND>(h, s);
+    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_CENTRAL, BND>(h, s);
     return cudaErrorNotSupported;
   }
   if (vol == VOL_SC) {
-    if (vflux == FLUX_RANOCHA) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_RANOCHA>(h, s);
-    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_CENTRAL>(h, s);
+    if (vflux == FLUX_RANOCHA) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_RANOCHA, BND>(h, s);
+    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_CENTRAL, BND>(h, s);
   }
   return cudaErrorNotSupported;
 }
 
-template <int DIM, typename R>
+template <int DIM, typename R, int BND>
 cudaError_t launch_dim(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s) {
   switch (N) {
-    case 2: return launch_n<DIM, 2, R>(eq, vol, vflux, h, s);
-    case 3: return launch_n<DIM, 3, R>(eq, vol, vflux, h, s);
-    case 4: return launch_n<DIM, 4, R>(eq, vol, vflux, h, s);
-    case 5: return launch_n<DIM, 5, R>(eq, vol, vflux, h, s);
-    case 6: return launch_n<DIM, 6, R>(eq, vol, vflux, h, s);
+    case 2: return launch_n<DIM, 2, R, BND>(eq, vol, vflux, h, s);
+    case 3: return launch_n<DIM, 3, R, BND>(eq, vol, vflux, h, s);
+    case 4: return launch_n<DIM, 4, R, BND>(eq, vol, vflux, h, s);
+    case 5: return launch_n<DIM, 5, R, BND>(eq, vol, vflux, h, s);
+    case 6: return launch_n<DIM, 6, R, BND>(eq, vol, vflux, h, s);
     default: return cudaErrorNotSupported;
   }
 }

@@ -1,8 +1,8 @@
-// Fused DGSEM kernels for 1D, compute type double.
+// Fused DGSEM kernels for 1D, compute type double: periodic meshes without source terms.
 #include "dg_launch.cuh"
 
 namespace trixi {
 cudaError_t launch_fused_1d_f64(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s) {
-  return launch_dim<1, double>(N, eq, vol, vflux, h, s);
+  return launch_dim<1, double, 0>(N, eq, vol, vflux, h, s);
 }
 }  // namespace trixi

@@ -1,8 +1,8 @@
-// Fused DGSEM kernels for 2D, compute type float.
+// Fused DGSEM kernels for 2D, compute type float: periodic meshes without source terms.
 #include "dg_launch.cuh"
 
 namespace trixi {
 cudaError_t launch_fused_2d_f32(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s) {
-  return launch_dim<2, float>(N, eq, vol, vflux, h, s);
+  return launch_dim<2, float, 0>(N, eq, vol, vflux, h, s);
 }
 }  // namespace trixi

@@ -48,6 +48,9 @@ const double kCK_A[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.
 const double kCK_B[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
                          1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
                          2277821191437.0 / 14882151754819.0};
+// stage times t + c_s dt of CarpenterKennedy2N54
+const double kCK_C[5] = {0.0, 1432997174477.0 / 9575080441755.0, 2526269341429.0 / 6820363962896.0,
+                         2006345519317.0 / 3224310063776.0, 2802321613138.0 / 2924317926251.0};
 
 }  // namespace
 
@@ -73,8 +76,14 @@ struct trixi_handle {
   double gamma = 1.4, adv[3] = {0, 0, 0};
   double alpha_max = 0.5, alpha_min = 0.001;
   int alpha_smooth = 1;
-  int64_t E = 0, I = 0, M = 0;
+  int64_t E = 0, I = 0, M = 0, B = 0;
   Basis basis;
+  // non-periodic meshes and source terms
+  int bc_kind = -1, src_kind = 0;
+  IcParams bc{};
+  double src[3] = {2.0, 0.1, 2.0};
+  int64_t *d_bnd_nid = nullptr, *d_bnd_side = nullptr, *d_bnd_ori = nullptr;
+  double *d_boundaries_u = nullptr;
   // device tables
   int32_t *d_face_table = nullptr;
   int32_t *d_slot_nbrs = nullptr;
@@ -159,7 +168,8 @@ void free_all(trixi_handle *h) {
                   h->d_mo_ls, h->d_mo_ori, h->d_mortar_flux, h->d_alpha_raw, h->d_alpha, h->d_err,
                   h->d_scratch_u, h->d_interfaces_u, h->d_sfv, h->d_mortar_u[0], h->d_mortar_u[1],
                   h->d_mortar_u[2], h->d_mortar_u[3], h->d_coords, h->d_acc, h->d_partial, h->d_partial2,
-                  h->d_red_out, h->d_vdm, h->d_wa, h->d_w};
+                  h->d_red_out, h->d_vdm, h->d_wa, h->d_w, h->d_bnd_nid, h->d_bnd_side, h->d_bnd_ori,
+                  h->d_boundaries_u};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -175,6 +185,8 @@ int64_t ipow64(int64_t b, int e) {
   while (e-- > 0) r *= b;
   return r;
 }
+
+IcParams ic_params(const trixi_handle *h, int kind, const double *params, int64_t nparams);
 
 int check_u_args(trixi_handle *h, const void *a, const char *name) {
   if (!aligned8(a)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "%s is null or not 8-byte aligned", name);
@@ -224,8 +236,22 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   if (!d->inverse_jacobian) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "inverse_jacobian is null");
   if (d->ninterfaces < 0 || (d->ninterfaces > 0 && (!d->interface_neighbor_ids || !d->interface_orientations)))
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "interface tables");
-  if (d->nboundaries != 0)
-    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "non-periodic boundaries (nboundaries=%lld)", (long long)d->nboundaries);
+  if (d->nboundaries < 0 || (d->nboundaries > 0 && (!d->boundary_neighbor_ids || !d->boundary_neighbor_sides ||
+                                                    !d->boundary_orientations)))
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "boundary tables");
+  if (d->nboundaries > 0 && (d->boundary_function < TRIXI_IC_CONSTANT || d->boundary_function > TRIXI_IC_WEAK_BLAST_WAVE))
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "boundary_function %d", d->boundary_function);
+  if (d->nboundaries > 0 && d->boundary_function == TRIXI_IC_WEAK_BLAST_WAVE && d->equation != TRIXI_EQ_COMPRESSIBLE_EULER)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "the weak blast wave needs the Euler equations");
+  if (d->nboundary_params < 0 || d->nboundary_params > 8 || d->nsource_params < 0 || d->nsource_params > 3)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "nboundary_params %d / nsource_params %d", d->nboundary_params,
+                d->nsource_params);
+  if (d->source_terms != TRIXI_SOURCE_NONE && d->source_terms != TRIXI_SOURCE_CONVERGENCE_TEST)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "source_terms %d", d->source_terms);
+  if (d->source_terms == TRIXI_SOURCE_CONVERGENCE_TEST && d->equation != TRIXI_EQ_COMPRESSIBLE_EULER)
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "source_terms_convergence_test is defined for the Euler equations");
+  if ((d->nboundaries > 0 || d->source_terms != TRIXI_SOURCE_NONE) && !d->node_coordinates)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "boundaries and source terms need node_coordinates");
   if (d->nmortars < 0 || (d->nmortars > 0 && (!d->mortar_neighbor_ids || !d->mortar_large_sides || !d->mortar_orientations)))
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "mortar tables");
   if (d->nmortars > 0 && d->ndims == 1) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "mortars in 1D");
@@ -255,6 +281,9 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   h->E = d->nelements;
   h->I = d->ninterfaces;
   h->M = d->nmortars;
+  h->B = d->nboundaries;
+  h->src_kind = d->source_terms;
+  for (int i = 0; i < d->nsource_params; ++i) h->src[i] = d->source_params[i];
   if (!fused_supported(h->dim, h->N, h->eq, h->vol, h->vflux)) {
     int st = fail(nullptr, TRIXI_ERR_UNSUPPORTED, "volume integral %d with volume flux %d for equation %d",
                   h->vol, h->vflux, h->eq);
@@ -324,16 +353,27 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
     if (f != INT32_MIN) return bad("mortar %lld: large face already connected (element %lld)", (long long)m + 1, (long long)large);
     f = (int32_t)(-(base + nc) - 1);
   }
+  // boundary faces keep the FACE_BOUNDARY (= INT32_MIN) entry, once declared
+  std::vector<char> declared(ft.size(), 0);
+  for (int64_t b = 0; b < h->B; ++b) {
+    const int64_t e = d->boundary_neighbor_ids[b], side = d->boundary_neighbor_sides[b], o = d->boundary_orientations[b];
+    if (e < 1 || e > h->E) return bad("boundary %lld: element id %lld", (long long)b + 1, (long long)e);
+    if (side != 1 && side != 2) return bad("boundary %lld: side %lld", (long long)b + 1, (long long)side);
+    if (o < 1 || o > h->dim) return bad("boundary %lld: orientation %lld", (long long)b + 1, (long long)o);
+    const size_t fi = (size_t)(e - 1) * nfaces + 2 * (o - 1) + (side == 1 ? 1 : 0);
+    if (ft[fi] != INT32_MIN || declared[fi]) return bad("boundary %lld: face already connected (element %lld)", (long long)b + 1, (long long)e);
+    declared[fi] = 1;
+  }
   if (d->nghost_elements < 0 || d->nghost_elements >= h->E) return bad("nghost_elements %lld of %lld", (long long)d->nghost_elements, (long long)h->E);
   const int64_t first_ghost = h->E - d->nghost_elements;
   for (size_t i = 0; i < ft.size(); ++i)
-    if (ft[i] == INT32_MIN) {
+    if (ft[i] == INT32_MIN && !declared[i]) {
       const int64_t e = (int64_t)(i / nfaces);
       if (e >= first_ghost) {
         ft[i] = (int32_t)e;  // open ghost face: read the ghost itself (its rhs is discarded)
         continue;
       }
-      return bad("element %lld face %lld has no interface or mortar (non-periodic meshes are not supported)",
+      return bad("element %lld face %lld has no interface, mortar or boundary",
                  (long long)(i / nfaces) + 1, (long long)(i % nfaces) + 1);
     }
 
@@ -360,6 +400,11 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   }
   if (d->node_coordinates)
     ok(upload(&h->d_coords, d->node_coordinates, (size_t)(h->dim * h->NN * h->E)));
+  if (h->B > 0) {
+    ok(upload(&h->d_bnd_nid, d->boundary_neighbor_ids, (size_t)h->B));
+    ok(upload(&h->d_bnd_side, d->boundary_neighbor_sides, (size_t)h->B));
+    ok(upload(&h->d_bnd_ori, d->boundary_orientations, (size_t)h->B));
+  }
   ok(upload(&h->d_w, h->basis.weights.data(), (size_t)h->N));
   ok(cudaMalloc(&h->d_err, sizeof(int)));
   if (h->d_err) ok(cudaMemset(h->d_err, 0, sizeof(int)));
@@ -391,6 +436,13 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   for (int i = 0; i < h->N; ++i) f.invw[i] = 1.0 / h->basis.weights[i];
   f.lhat_l = 1.0 / h->basis.weights[0];          // boundary_interpolation[1, 1]
   f.lhat_r = 1.0 / h->basis.weights[h->N - 1];   // boundary_interpolation[N, 2]
+  h->bc_kind = h->B > 0 ? d->boundary_function : -1;
+  h->bc = ic_params(h, h->bc_kind, d->boundary_params, d->nboundary_params);
+  f.coords = h->d_coords;
+  f.bc_kind = h->bc_kind;
+  f.bc = h->bc;
+  f.src_kind = h->src_kind;
+  for (int i = 0; i < 3; ++i) f.src[i] = h->src[i];
   *out = h;
   return TRIXI_OK;
 }
@@ -457,7 +509,7 @@ int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStrea
 
 // Kernels of one rhs evaluation (mode RHS/RK/VOLUME) on u_in.
 int run_rhs(trixi_handle *h, int mode, const double *u_in, double *out, double *k, double a, double b, double dt,
-            cudaStream_t s) {
+            cudaStream_t s, double t = 0.0) {
   if (h->vol == TRIXI_VOLUME_SHOCK_CAPTURING_HG) {
     int st = run_indicator(h, u_in, h->d_alpha, s);
     if (st) return st;
@@ -475,6 +527,7 @@ int run_rhs(trixi_handle *h, int mode, const double *u_in, double *out, double *
   f.rk_a = a;
   f.rk_b = b;
   f.dt = dt;
+  f.t = t;
   f.epb = h->epb;
   TRIXI_CUDA(h, launch_fused(h->dim, h->N, h->eq, h->vol, h->vflux, h->mixed, f, s), "fused rhs");
   return TRIXI_OK;
@@ -584,6 +637,16 @@ StageHost stage_of(trixi_handle *h) {
   sh.lhat_l = 1.0 / h->basis.weights[0];
   sh.lhat_r = 1.0 / h->basis.weights[h->N - 1];
   sh.inv_jac = h->d_inv_jac;
+  sh.nboundaries = h->B;
+  sh.bnd_neighbor_ids = h->d_bnd_nid;
+  sh.bnd_sides = h->d_bnd_side;
+  sh.bnd_orientations = h->d_bnd_ori;
+  sh.boundaries_u = h->d_boundaries_u;
+  sh.coords = h->d_coords;
+  sh.bc_kind = h->bc_kind;
+  sh.bc = h->bc;
+  sh.src_kind = h->src_kind;
+  for (int i = 0; i < 3; ++i) sh.src[i] = h->src[i];
   return sh;
 }
 
@@ -602,6 +665,11 @@ int ensure_stage_containers(trixi_handle *h) {
       TRIXI_CUDA(h, cudaMalloc(&h->d_mortar_u[c], sizeof(double) * n), "alloc mortar u");
       TRIXI_CUDA(h, cudaMemset(h->d_mortar_u[c], 0, sizeof(double) * n), "init mortar u");
     }
+  if (h->B > 0) {
+    const size_t n = (size_t)(2 * h->nv * h->NF * h->B);
+    TRIXI_CUDA(h, cudaMalloc(&h->d_boundaries_u, sizeof(double) * n), "alloc boundaries u");
+    TRIXI_CUDA(h, cudaMemset(h->d_boundaries_u, 0, sizeof(double) * n), "init boundaries u");
+  }
   return TRIXI_OK;
 }
 
@@ -615,7 +683,7 @@ int trixi_rhs(trixi_handle *h, double *du, const double *u, double t, void *stre
   if (int st = check_u_args(h, du, "du")) return st;
   if (int st = check_u_args(h, u, "u")) return st;
   if ((const void *)du == (const void *)u) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "du aliases u");
-  return run_rhs(h, MODE_RHS, u, du, nullptr, 0, 0, 0, (cudaStream_t)stream);
+  return run_rhs(h, MODE_RHS, u, du, nullptr, 0, 0, 0, (cudaStream_t)stream, t);
 }
 
 int trixi_rk_stage(trixi_handle *h, double *u_out, const double *u_in, double *k, double a, double b, double dt,
@@ -628,7 +696,7 @@ int trixi_rk_stage(trixi_handle *h, double *u_out, const double *u_in, double *k
   if ((const void *)u_out == (const void *)u_in) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "u_out aliases u_in");
   if (!std::isfinite(a) || !std::isfinite(b) || !std::isfinite(dt))
     return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "non-finite RK coefficient");
-  return run_rhs(h, MODE_RK, u_in, u_out, k, a, b, dt, (cudaStream_t)stream);
+  return run_rhs(h, MODE_RK, u_in, u_out, k, a, b, dt, (cudaStream_t)stream, t);
 }
 
 int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt, int64_t nsteps, void *stream) {
@@ -643,7 +711,7 @@ int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt, i
   double *cur = u, *nxt = h->d_scratch_u;
   for (int64_t step = 0; step < nsteps; ++step) {
     for (int st = 0; st < 5; ++st) {
-      int r = run_rhs(h, MODE_RK, cur, nxt, k, kCK_A[st], kCK_B[st], dt, s);
+      int r = run_rhs(h, MODE_RK, cur, nxt, k, kCK_A[st], kCK_B[st], dt, s, t + kCK_C[st] * dt);
       if (r) return r;
       std::swap(cur, nxt);
     }
@@ -676,17 +744,20 @@ int trixi_interface_flux(trixi_handle *h, void *stream) {
 }
 
 int trixi_prolong2boundaries(trixi_handle *h, const double *u, void *stream) {
-  (void)u;
-  (void)stream;
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
-  return TRIXI_OK;  // periodic TreeMesh: no boundaries (src/solvers/dg_2d.jl:419-422)
+  if (h->B == 0) return TRIXI_OK;  // periodic TreeMesh: no boundaries (src/solvers/dg_2d.jl:419-422)
+  if (int st = check_u_args(h, u, "u")) return st;
+  if (int st = ensure_stage_containers(h)) return st;
+  TRIXI_CUDA(h, stage_prolong2boundaries(stage_of(h), u, (cudaStream_t)stream), "prolong2boundaries");
+  return TRIXI_OK;
 }
 
 int trixi_boundary_flux(trixi_handle *h, double t, void *stream) {
-  (void)t;
-  (void)stream;
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
-  return TRIXI_OK;  // periodic TreeMesh: no boundaries (src/solvers/dg_2d.jl:447-450)
+  if (h->B == 0) return TRIXI_OK;  // periodic TreeMesh: no boundaries (src/solvers/dg_2d.jl:447-450)
+  if (int st = ensure_stage_containers(h)) return st;
+  TRIXI_CUDA(h, stage_boundary_flux(stage_of(h), t, (cudaStream_t)stream), "boundary_flux");
+  return TRIXI_OK;
 }
 
 int trixi_prolong2mortars(trixi_handle *h, const double *u, void *stream) {
@@ -720,12 +791,12 @@ int trixi_jacobian(trixi_handle *h, double *du, void *stream) {
 }
 
 int trixi_sources(trixi_handle *h, double *du, const double *u, double t, void *stream) {
-  (void)du;
-  (void)u;
-  (void)t;
-  (void)stream;
+  (void)u;  // the convergence-test source depends on (x, t) only
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
-  return TRIXI_OK;  // source_terms = nothing (src/solvers/dg_2d.jl:741-743)
+  if (h->src_kind == 0) return TRIXI_OK;  // source_terms = nothing (src/solvers/dg_2d.jl:741-743)
+  if (int st = check_u_args(h, du, "du")) return st;
+  TRIXI_CUDA(h, stage_sources(stage_of(h), du, t, (cudaStream_t)stream), "sources");
+  return TRIXI_OK;
 }
 
 int trixi_container(trixi_handle *h, int which, void **dev_ptr, int64_t *count) {
@@ -744,6 +815,11 @@ int trixi_container(trixi_handle *h, int which, void **dev_ptr, int64_t *count) 
   if (which == TRIXI_CONTAINER_INTERFACES_U) {
     *dev_ptr = h->d_interfaces_u;
     *count = 2 * h->nv * h->NF * h->I;
+    return TRIXI_OK;
+  }
+  if (which == TRIXI_CONTAINER_BOUNDARIES_U) {
+    *dev_ptr = h->d_boundaries_u;
+    *count = 2 * h->nv * h->NF * h->B;
     return TRIXI_OK;
   }
   if (which == TRIXI_CONTAINER_SURFACE_FLUX_VALUES) {
@@ -1568,6 +1644,8 @@ AdjointHost adjoint_host(const trixi_handle *h) {
 
 int check_adjoint_supported(trixi_handle *h) {
   if (h->mixed) return fail(h, TRIXI_ERR_UNSUPPORTED, "the adjoint runs in FP64 (precision = FP64)");
+  if (h->B > 0 || h->src_kind != 0)
+    return fail(h, TRIXI_ERR_UNSUPPORTED, "adjoint: periodic meshes without source terms only");
   if (!adjoint_supported(h->dim, h->N, h->eq, h->vol, h->vflux, h->sflux, h->M > 0))
     return fail(h, TRIXI_ERR_UNSUPPORTED,
                 "adjoint: supported are Euler flux differencing with flux_ranocha/flux_central and linear "

@@ -64,6 +64,15 @@ mutable struct ProblemDesc
     reverse_lower::Ptr{Float64}
     node_coordinates::Ptr{Float64}
     nghost_elements::Int64
+    boundary_neighbor_ids::Ptr{Int64}
+    boundary_neighbor_sides::Ptr{Int64}
+    boundary_orientations::Ptr{Int64}
+    boundary_function::Int32
+    source_terms::Int32
+    nboundary_params::Int32
+    nsource_params::Int32
+    boundary_params::NTuple{8, Float64}
+    source_params::NTuple{3, Float64}
 end
 
 flux_code(::typeof(Trixi.flux_ranocha)) = FLUX_RANOCHA
@@ -104,6 +113,9 @@ function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
     dsplit = Matrix{Float64}(Array(basis.derivative_split))
     dhat = Matrix{Float64}(Array(basis.derivative_dhat))
     weights = Vector{Float64}(basis.weights)
+    # periodic TreeMesh (boundary_function = -1, no source terms); a
+    # non-periodic mesh passes cache_cpu.boundaries' neighbor_ids,
+    # neighbor_sides and orientations and the Dirichlet function's kind
     desc = ProblemDesc(0, ndims(mesh), Trixi.polydeg(basis), nvariables(equations), eq, vol, vflux,
                        flux_code(solver.surface_integral.surface_flux), fvflux, Int32(precision), gamma, adv,
                        amax, amin, asmooth, Int32(0),
@@ -111,7 +123,9 @@ function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
                        ninterfaces(interfaces), pointer(interfaces.neighbor_ids), pointer(interfaces.orientations),
                        0, Trixi.nmortars(mortars), pointer(mortars.neighbor_ids), pointer(mortars.large_sides),
                        pointer(mortars.orientations), pointer(weights), pointer(dsplit), pointer(dhat),
-                       C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, pointer(elements.node_coordinates), 0)
+                       C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, pointer(elements.node_coordinates), 0,
+                       C_NULL, C_NULL, C_NULL, Int32(-1), Int32(0), Int32(0), Int32(0),
+                       ntuple(_ -> 0.0, 8), ntuple(_ -> 0.0, 3))
     desc.struct_size = Int32(sizeof(ProblemDesc))
     handle = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve elements interfaces mortars dsplit dhat weights desc begin

@@ -25,6 +25,9 @@ from .equations import (
     initial_condition_fourier_advection,
     initial_condition_fourier_euler,
     initial_condition_weak_blast_wave,
+    BoundaryConditionDirichlet,
+    boundary_condition_periodic,
+    source_terms_convergence_test,
 )
 from .mesh import TreeMesh
 from .semidiscretization import (

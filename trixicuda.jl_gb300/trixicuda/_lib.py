@@ -30,6 +30,7 @@ FLUX_LAX_FRIEDRICHS, FLUX_RANOCHA, FLUX_CENTRAL, FLUX_LAX_FRIEDRICHS_NAIVE = 0, 
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 IC_CONSTANT, IC_CONVERGENCE_TEST, IC_WEAK_BLAST_WAVE = 0, 1, 2
+SOURCE_NONE, SOURCE_CONVERGENCE_TEST = 0, 1
 INTEGRAL_STATE, INTEGRAL_ENTROPY, INTEGRAL_ENTROPY_PRODUCTION, INTEGRAL_DU = 0, 1, 2, 3
 
 CONTAINER_INTERFACES_U = 0
@@ -37,6 +38,7 @@ CONTAINER_SURFACE_FLUX_VALUES = 1
 CONTAINER_MORTARS_U = 2
 CONTAINER_ALPHA = 8
 CONTAINER_INVERSE_JACOBIAN = 9
+CONTAINER_BOUNDARIES_U = 10
 
 BASIS_ITEMS = {
     "nodes": 0, "weights": 1, "derivative_split": 2, "derivative_dhat": 3,
@@ -89,6 +91,15 @@ class ProblemDesc(C.Structure):
         ("reverse_lower", C.POINTER(C.c_double)),
         ("node_coordinates", C.POINTER(C.c_double)),
         ("nghost_elements", C.c_int64),
+        ("boundary_neighbor_ids", C.POINTER(C.c_int64)),
+        ("boundary_neighbor_sides", C.POINTER(C.c_int64)),
+        ("boundary_orientations", C.POINTER(C.c_int64)),
+        ("boundary_function", C.c_int32),
+        ("source_terms", C.c_int32),
+        ("nboundary_params", C.c_int32),
+        ("nsource_params", C.c_int32),
+        ("boundary_params", C.c_double * 8),
+        ("source_params", C.c_double * 3),
     ]
 
 

@@ -218,3 +218,62 @@ def initial_condition_fourier_advection(equations, seed=20261203, kmax=8, xmin=-
         return (1.0 + amplitude * f(np.atleast_2d(x)))[None, :]
 
     return ic
+
+
+# --- boundary conditions and source terms --------------------------------------
+boundary_condition_periodic = "periodic"
+
+
+class BoundaryConditionDirichlet:
+    """Trixi's `BoundaryConditionDirichlet(boundary_value_function)`: the
+    boundary value function's state at the face node and time t enters the
+    surface flux as the outer state.  The library evaluates built-in
+    functions on the device: initial_condition_convergence_test,
+    initial_condition_constant, initial_condition_weak_blast_wave."""
+
+    def __init__(self, boundary_value_function):
+        self.boundary_value_function = boundary_value_function
+
+    def __eq__(self, other):
+        return (isinstance(other, BoundaryConditionDirichlet)
+                and other.boundary_value_function is self.boundary_value_function)
+
+    def __hash__(self):
+        return hash(self.boundary_value_function)
+
+
+def source_terms_convergence_test(u, x, t, equations):
+    """Source of the Euler convergence test's manufactured solution
+    rho = rho v_d = 2 + 0.1 sin(pi (sum_d x_d - t)), E = rho^2 (host version;
+    the library evaluates it on the device).  x: (ndims, n)."""
+    x = np.atleast_2d(x)
+    d = equations.ndims
+    g = equations.gamma
+    c, A, L = 2.0, 0.1, 2.0
+    omega = 2 * np.pi / L
+    arg = omega * (np.sum(x, axis=0) - t)
+    rho = c + A * np.sin(arg)
+    rx = omega * A * np.cos(arg)
+    s = np.empty((d + 2,) + rho.shape)
+    if d == 1:
+        s[0] = 0.0
+        s[1] = s[2] = 0.5 * rx * (g - 1) * (4 * rho - 1)
+    elif d == 2:
+        s[0] = rx
+        s[1] = s[2] = rx * (2 * g * rho - g - 2 * rho + 2)
+        s[3] = 2 * rx * (2 * g * rho - g - rho + 1)
+    else:
+        s[0] = 2 * rx
+        s[1] = s[2] = s[3] = 0.5 * rx * (4 * g * rho - 3 * g - 4 * rho + 7)
+        s[4] = 0.5 * rx * (12 * g * rho - 9 * g - 4 * rho + 9)
+    return s
+
+
+def boundary_function_code(func):
+    """trixi_initial_condition_kind of a built-in boundary value function."""
+    codes = {initial_condition_constant: _lib.IC_CONSTANT,
+             initial_condition_convergence_test: _lib.IC_CONVERGENCE_TEST,
+             initial_condition_weak_blast_wave: _lib.IC_WEAK_BLAST_WAVE}
+    if func not in codes:
+        raise NotImplementedError("Dirichlet boundary values: the built-in initial conditions only")
+    return codes[func]

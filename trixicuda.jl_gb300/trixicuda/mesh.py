@@ -18,8 +18,11 @@ GPU (src/solvers/cache.jl:60-88, containers_{1,2,3}d.jl):
   second tangential dimension) and then the large element; large_side 1
   means the large element is on the left (lower coordinate).
 
-Only periodic meshes are supported (the hot-path configurations are all
-periodic); other boundary conditions raise NotImplementedError.
+* boundaries (non-periodic dimensions): one entry per element face on the
+  domain boundary, ordered by direction (x_neg, x_pos, y_neg, y_pos, z_neg,
+  z_pos) and by element within a direction, with neighbor_sides 2 when the
+  boundary is the element's lower face (the element lies on its right) and 1
+  when it is the upper face -- the layout of Trixi's boundaries container.
 
 Arrays are numpy arrays in C order whose memory layout equals the reference's
 Julia column-major arrays: e.g. node_coordinates [ndims, N, N, E] is stored as
@@ -47,6 +50,14 @@ class Containers:
     mortar_large_sides: np.ndarray          # (M,)
     mortar_orientations: np.ndarray         # (M,)
     element_neighbors: dict = field(default_factory=dict)
+    boundary_neighbor_ids: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=np.int64))  # (B,) 1-based
+    boundary_neighbor_sides: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=np.int64))  # (B,) 1 or 2
+    boundary_orientations: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=np.int64))  # (B,) 1..ndims
+    n_boundaries_per_direction: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=np.int64))  # (2 ndims,)
+
+    @property
+    def nboundaries(self) -> int:
+        return int(self.boundary_orientations.shape[0])
 
     @property
     def ninterfaces(self) -> int:
@@ -70,8 +81,8 @@ class TreeMesh:
         if self.ndims not in (1, 2, 3):
             raise ValueError("TreeMesh supports 1, 2, 3 dimensions")
         per = periodicity if isinstance(periodicity, (tuple, list)) else (periodicity,) * self.ndims
-        if not all(per):
-            raise NotImplementedError("non-periodic TreeMesh boundaries are not supported")
+        if len(per) != self.ndims:
+            raise ValueError("periodicity needs one flag per dimension")
         self.periodicity = tuple(bool(p) for p in per)
         self.length_level_0 = float(np.max(cmax - cmin))
         self.center_level_0 = 0.5 * (cmin + cmax)
@@ -134,10 +145,16 @@ class TreeMesh:
         return lo + (np.asarray(cell[1], dtype=np.float64) + 0.5) * h
 
     def _neighbor_cell(self, cell, dim, side):
+        """The same-level cell across face (dim, side), or None beyond a
+        non-periodic domain boundary."""
         level, c = cell
         n = 2 ** level
         cc = list(c)
-        cc[dim] = (cc[dim] + (1 if side > 0 else -1)) % n
+        cc[dim] = cc[dim] + (1 if side > 0 else -1)
+        if not 0 <= cc[dim] < n:
+            if not self.periodicity[dim]:
+                return None
+            cc[dim] %= n
         return (level, tuple(cc))
 
     def _check_balance(self):
@@ -145,7 +162,7 @@ class TreeMesh:
             for d in range(self.ndims):
                 for side in (-1, 1):
                     nb = self._neighbor_cell(leaf, d, side)
-                    if nb in self.cells and nb not in self.leaves:
+                    if nb is not None and nb in self.cells and nb not in self.leaves:
                         for ch in self._face_children(nb, d, side):
                             if ch not in self.leaves:
                                 raise ValueError("TreeMesh is not 2:1 balanced")
@@ -195,21 +212,28 @@ class TreeMesh:
                 coords[(e,) + (Ellipsis,) + (k,)] = (ctr[k] + 0.5 * h * grids[k]).transpose(tuple(range(d))[::-1])
         if_nid, if_ori = [], []
         mo_nid, mo_ls, mo_ori = [], [], []
+        bnd = [[] for _ in range(2 * d)]  # per direction: element ids (1-based)
         for e, cell in enumerate(self.elements):
             for dim in range(d):
                 nb = self._neighbor_cell(cell, dim, +1)
-                if nb in self.leaves:
+                if nb is not None and nb in self.leaves:
                     if_nid.append((e + 1, self.element_index[nb] + 1))
                     if_ori.append(dim + 1)
             for dir_ in range(2 * d):
                 dim, side = dir_ // 2, (1 if dir_ % 2 else -1)
                 nb = self._neighbor_cell(cell, dim, side)
+                if nb is None:
+                    bnd[dir_].append(e + 1)
+                    continue
                 if nb in self.cells and nb not in self.leaves:
                     smalls = [self.element_index[ch] + 1 for ch in self._face_children(nb, dim, side)]
                     mo_nid.append(tuple(smalls) + (e + 1,))
                     mo_ls.append(1 if side > 0 else 2)
                     mo_ori.append(dim + 1)
         nc = 2 ** (d - 1)
+        b_nid = [e for dir_ in range(2 * d) for e in bnd[dir_]]
+        b_side = [2 if dir_ % 2 == 0 else 1 for dir_ in range(2 * d) for _ in bnd[dir_]]
+        b_ori = [dir_ // 2 + 1 for dir_ in range(2 * d) for _ in bnd[dir_]]
         return Containers(
             ndims=d, nnodes=N, nelements=E,
             inverse_jacobian=inv_jac,
@@ -220,4 +244,8 @@ class TreeMesh:
             mortar_neighbor_ids=np.asarray(mo_nid, dtype=np.int64).reshape(-1, nc + 1),
             mortar_large_sides=np.asarray(mo_ls, dtype=np.int64),
             mortar_orientations=np.asarray(mo_ori, dtype=np.int64),
+            boundary_neighbor_ids=np.asarray(b_nid, dtype=np.int64),
+            boundary_neighbor_sides=np.asarray(b_side, dtype=np.int64),
+            boundary_orientations=np.asarray(b_ori, dtype=np.int64),
+            n_boundaries_per_direction=np.asarray([len(b) for b in bnd], dtype=np.int64),
         )

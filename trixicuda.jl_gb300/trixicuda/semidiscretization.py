@@ -47,8 +47,33 @@ def _stream_handle(stream=None):
     return C.c_void_p(s.cuda_stream)
 
 
+def _boundary_spec(boundary_conditions, cont, equations):
+    """(code, params) of the Dirichlet boundary function, or (-1, None) on a
+    periodic mesh.  One boundary function serves every non-periodic direction."""
+    from .equations import BoundaryConditionDirichlet, boundary_function_code
+
+    if cont.nboundaries == 0:
+        return -1, None
+    bcs = boundary_conditions
+    if isinstance(bcs, dict):
+        vals = list(bcs.values())
+    elif isinstance(bcs, (tuple, list)):
+        vals = list(bcs)
+    else:
+        vals = [bcs]
+    vals = [b for b in vals if b not in ("periodic", None)]
+    if not vals or not all(isinstance(b, BoundaryConditionDirichlet) for b in vals) or any(b != vals[0] for b in vals):
+        raise NotImplementedError("non-periodic meshes need one BoundaryConditionDirichlet for all boundaries")
+    code = boundary_function_code(vals[0].boundary_value_function)
+    params = None
+    if code == _lib.IC_CONSTANT:
+        x = np.zeros((equations.ndims, 1))
+        params = np.asarray(vals[0].boundary_value_function(x, 0.0, equations))[:, 0]
+    return code, params
+
+
 def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver: DGSEMGPU,
-                       precision: str = "fp64"):
+                       precision: str = "fp64", boundary_conditions="periodic", source_terms=None):
     """trixi_problem_desc for a mesh (or prebuilt containers).  Returns the
     ctypes struct and the numpy arrays it points into (keep them alive)."""
     if isinstance(mesh_or_containers, Containers):
@@ -105,6 +130,28 @@ def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver:
     d.mortar_orientations = _ptr_i(keep["mo_ori"])
     d.node_coordinates = _ptr_d(keep["coords"])
     d.nghost_elements = int(getattr(cont, "nghost_elements", 0))
+    # non-periodic meshes and source terms
+    keep["b_nid"] = np.ascontiguousarray(cont.boundary_neighbor_ids, dtype=np.int64)
+    keep["b_side"] = np.ascontiguousarray(cont.boundary_neighbor_sides, dtype=np.int64)
+    keep["b_ori"] = np.ascontiguousarray(cont.boundary_orientations, dtype=np.int64)
+    d.nboundaries = cont.nboundaries
+    d.boundary_neighbor_ids = _ptr_i(keep["b_nid"])
+    d.boundary_neighbor_sides = _ptr_i(keep["b_side"])
+    d.boundary_orientations = _ptr_i(keep["b_ori"])
+    code, params = _boundary_spec(boundary_conditions, cont, equations)
+    d.boundary_function = code
+    d.nboundary_params = 0 if params is None else len(params)
+    for i in range(d.nboundary_params):
+        d.boundary_params[i] = float(params[i])
+    from .equations import source_terms_convergence_test
+
+    if source_terms is None:
+        d.source_terms = _lib.SOURCE_NONE
+    elif source_terms is source_terms_convergence_test:
+        d.source_terms = _lib.SOURCE_CONVERGENCE_TEST
+    else:
+        raise NotImplementedError("source terms: source_terms_convergence_test only")
+    d.nsource_params = 0
     return d, keep, cont
 
 
@@ -117,19 +164,15 @@ class SemidiscretizationHyperbolicGPU:
                  precision: str = "fp64", device=None, containers=None):
         if mesh.ndims != equations.ndims:
             raise ValueError("mesh and equations dimension differ")
-        if source_terms is not None:
-            raise NotImplementedError("source terms are not part of the GB300 hot path")
-        if boundary_conditions not in ("periodic", None):
-            raise NotImplementedError("only periodic boundary conditions are supported")
         self.mesh = mesh
         self.equations = equations
         self.initial_condition = initial_condition
         self.solver = solver
         self.source_terms = source_terms
-        self.boundary_conditions = "periodic"
+        self.boundary_conditions = boundary_conditions
         self.precision = precision
         desc, keep, cont = build_problem_desc(containers if containers is not None else mesh, equations, solver,
-                                              precision)
+                                              precision, boundary_conditions, source_terms)
         self.containers = cont
         self._desc, self._keep = desc, keep
         torch = _torch()
