@@ -131,7 +131,8 @@ def _tile_report(semi):
 
 def time_gpu_path(precision, steps, warmup, device, flush, tile=None):
     """Device-timed CK2N54 steps through trixi_rk_stage (ping-pong buffers).
-    Returns per-step ms, per-launch ms of the fused kernel, the semi, final u."""
+    Returns per-step ms (back-to-back launches), per-launch ms of the fused
+    kernel (a second loop with events around every launch), the semi, final u."""
     import torch
 
     import trixicuda as T
@@ -164,17 +165,28 @@ def time_gpu_path(precision, steps, warmup, device, flush, tile=None):
         for s in range(5):
             stage(s)
     torch.cuda.synchronize()
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(steps)]
+    # throughput: whole steps, back-to-back stage launches, events only at the
+    # step boundaries (L2 flushed before every step)
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        for s in range(5):
+            stage(s)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    # roofline: the duration of every stage launch (events around each one)
+    evl = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(steps)]
     for i in range(steps):
         flush.zero_()
         for s in range(5):
-            ev[i][s].record(stream)
+            evl[i][s].record(stream)
             stage(s)
-        ev[i][5].record(stream)
+        evl[i][5].record(stream)
     torch.cuda.synchronize()
     T.synchronize(semi)
-    step_ms = [ev[i][0].elapsed_time(ev[i][5]) for i in range(steps)]
-    launch_ms = [ev[i][s].elapsed_time(ev[i][s + 1]) for i in range(steps) for s in range(5)]
+    launch_ms = [evl[i][s].elapsed_time(evl[i][s + 1]) for i in range(steps) for s in range(5)]
     return step_ms, launch_ms, semi, bufs[cur], dt
 
 

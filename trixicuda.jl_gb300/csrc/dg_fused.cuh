@@ -47,7 +47,6 @@ struct FusedParams {
   const double *__restrict__ dt_elem;       // [E] per-element time step (batched ensembles) or null
   int *err;                                 // device error word
   int64_t nelements;
-  int epb;                                  // elements per block
   int mode;
   int surface_flux, fv_flux;
   double rk_a, rk_b, dt;

@@ -35,7 +35,6 @@ struct FusedHost {
   double dhat[HOST_NMAX * HOST_NMAX] = {};    // row-major
   double invw[HOST_NMAX] = {};
   double lhat_l = 0, lhat_r = 0;
-  int epb = 0;  // elements per block, 0 = default
   // tile of the fused kernel: warps per group and groups per block (0 = the
   // compile-time defaults); a non-null tile_out makes launch_fused report the
   // kernel's tile limits instead of launching

@@ -72,7 +72,6 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   p.wpg = wpg;
   p.gpb = gpb;
   const int epb = gpb * K::EPG;  // elements per block
-  p.epb = epb;
   const int block = 32 * wpg * gpb;
   const size_t smem = (size_t)gpb * K::GROUP_SMEM;
   // opt in once per instantiation to the large dynamic shared-memory carve-out

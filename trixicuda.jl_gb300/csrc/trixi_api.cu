@@ -96,7 +96,6 @@ struct trixi_handle {
   double *d_scratch_u = nullptr;
   // stage containers (allocated on first use)
   double *d_interfaces_u = nullptr, *d_sfv = nullptr, *d_mortar_u[4] = {nullptr, nullptr, nullptr, nullptr};
-  int epb = 0;
   // analysis / initial conditions (allocated on first use)
   double *d_coords = nullptr;
   unsigned long long *d_acc = nullptr;
@@ -528,7 +527,6 @@ int run_rhs(trixi_handle *h, int mode, const double *u_in, double *out, double *
   f.rk_b = b;
   f.dt = dt;
   f.t = t;
-  f.epb = h->epb;
   TRIXI_CUDA(h, launch_fused(h->dim, h->N, h->eq, h->vol, h->vflux, h->mixed, f, s), "fused rhs");
   return TRIXI_OK;
 }
