@@ -52,6 +52,7 @@ struct FusedParams {
   double rk_a, rk_b, dt;
   int use_k;                                // RK: read k (rk_a != 0)
   int wpg, gpb;                             // tile: warps per group, groups per block
+  int pdl;                                  // launched as a programmatic dependent launch
   // non-periodic meshes and source terms
   const double *__restrict__ coords;        // [E][NN][DIM] node coordinates (boundaries / sources)
   double t;                                 // time of this rhs evaluation
@@ -424,6 +425,14 @@ struct FusedKernel {
     const bool surface = (mode != MODE_VOLUME);
     const bool vec = p.vec16 != 0;
     const bool use_k = (mode == MODE_RK) && p.use_k;
+    if (p.pdl) {
+      // programmatic dependent launch: the next kernel in the stream may start
+      // launching now (it waits below before its own reads), and this grid
+      // waits until the previous kernel has completed and its writes are
+      // visible before reading u, k, mortar fluxes or alpha
+      asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+      asm volatile("griddepcontrol.wait;" ::: "memory");
+    }
 
     // phase A: every global read of the group is issued here.  Owner thread
     // (el, node) keeps its node's u and k in registers until phase C; all

@@ -39,6 +39,7 @@ struct FusedHost {
   // compile-time defaults); a non-null tile_out makes launch_fused report the
   // kernel's tile limits instead of launching
   int wpg = 0, gpb = 0;
+  int pdl = 0;  // launch as a programmatic dependent launch (overlaps the launch with the previous kernel's tail)
   struct FusedTile *tile_out = nullptr;
   // non-periodic meshes and source terms
   const double *coords = nullptr;  // [E][NN][DIM]

@@ -82,6 +82,21 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   const int64_t grid = (h.nelements + epb - 1) / epb;
   if (grid <= 0) return cudaSuccess;
   if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+  if (h.pdl) {
+    p.pdl = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, dg_fused_kernel<DIM, N, EQ, R, VOL, VF, BND>, p);
+  }
+  p.pdl = 0;
   dg_fused_kernel<DIM, N, EQ, R, VOL, VF, BND><<<(unsigned)grid, block, smem, s>>>(p);
   return cudaGetLastError();
 }

@@ -438,6 +438,7 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   h->bc_kind = h->B > 0 ? d->boundary_function : -1;
   h->bc = ic_params(h, h->bc_kind, d->boundary_params, d->nboundary_params);
   f.coords = h->d_coords;
+  f.pdl = 1;  // programmatic dependent launches: stage s+1 overlaps its launch with stage s's last wave
   f.bc_kind = h->bc_kind;
   f.bc = h->bc;
   f.src_kind = h->src_kind;
