@@ -60,7 +60,8 @@ typedef enum trixi_status {
 
 typedef enum trixi_equation_kind {
   TRIXI_EQ_LINEAR_ADVECTION = 0,   /* LinearScalarAdvectionEquation{1,2,3}D */
-  TRIXI_EQ_COMPRESSIBLE_EULER = 1  /* CompressibleEulerEquations{1,2,3}D */
+  TRIXI_EQ_COMPRESSIBLE_EULER = 1, /* CompressibleEulerEquations{1,2,3}D */
+  TRIXI_EQ_IDEAL_GLM_MHD = 2       /* IdealGlmMhdEquations{1,2,3}D: 8 variables in 1D, 9 (with psi) in 2D/3D */
 } trixi_equation_kind;
 
 typedef enum trixi_volume_integral_kind {
@@ -73,8 +74,20 @@ typedef enum trixi_flux_kind {
   TRIXI_FLUX_LAX_FRIEDRICHS = 0,        /* flux_lax_friedrichs, Davis wave speed max(|v|+c) */
   TRIXI_FLUX_RANOCHA = 1,               /* flux_ranocha */
   TRIXI_FLUX_CENTRAL = 2,               /* flux_central */
-  TRIXI_FLUX_LAX_FRIEDRICHS_NAIVE = 3   /* LLF with max(|v_ll|,|v_rr|) + max(c_ll,c_rr) */
+  TRIXI_FLUX_LAX_FRIEDRICHS_NAIVE = 3,  /* LLF with max(|v_ll|,|v_rr|) + max(c_ll,c_rr) */
+  TRIXI_FLUX_HINDENLANG_GASSNER = 4     /* flux_hindenlang_gassner (ideal GLM-MHD) */
 } trixi_flux_kind;
+
+/* The nonconservative half of a (flux, nonconservative_flux) pair.  Ideal
+ * GLM-MHD in 2D/3D has nonconservative terms and pairs every volume, surface
+ * and FV flux with flux_nonconservative_powell (the reference's
+ * noncons_volume_flux_kernel!, surface_noncons_flux_kernel!,
+ * mortar_flux_kernel!: src/solvers/dg_2d_kernel.jl:228-367, 958-1035,
+ * 1290-1345); every other system has none. */
+typedef enum trixi_nonconservative_kind {
+  TRIXI_NONCONSERVATIVE_NONE = 0,
+  TRIXI_NONCONSERVATIVE_POWELL = 1  /* flux_nonconservative_powell */
+} trixi_nonconservative_kind;
 
 typedef enum trixi_precision_kind {
   TRIXI_PRECISION_FP64 = 0,  /* everything in FP64 */
@@ -89,7 +102,7 @@ typedef struct trixi_problem_desc {
   int32_t struct_size;          /* sizeof(trixi_problem_desc) */
   int32_t ndims;                /* 1, 2, 3 */
   int32_t polydeg;              /* 1..5 */
-  int32_t nvars;                /* 1 (advection) or ndims+2 (Euler) */
+  int32_t nvars;                /* 1 (advection), ndims+2 (Euler), 8 / 9 (ideal GLM-MHD 1D / 2D, 3D) */
   int32_t equation;             /* trixi_equation_kind */
   int32_t volume_integral;      /* trixi_volume_integral_kind */
   int32_t volume_flux;          /* DG volume flux (flux differencing / shock capturing) */
@@ -150,6 +163,12 @@ typedef struct trixi_problem_desc {
   int32_t nsource_params;
   double boundary_params[8];
   double source_params[3];
+  /* Ideal GLM-MHD: the nonconservative flux (trixi_nonconservative_kind) and
+   * the GLM cleaning speed c_h (equations.c_h; trixi_set_glm_speed changes it
+   * between steps, as a GlmSpeedCallback does). */
+  int32_t nonconservative_flux;
+  int32_t reserved0;            /* 0 */
+  double glm_speed;
 } trixi_problem_desc;
 
 /* Library version string ("trixi_b200 <semver> sm_103a"). */
@@ -199,6 +218,11 @@ int trixi_autotune(trixi_handle *h, const double *u, void *stream);
 int trixi_set_tile(trixi_handle *h, int wpg, int gpb);
 int trixi_tile(trixi_handle *h, int *epg, int *wpg, int *gpb, int *cand_wpg, int *cand_gpb, double *cand_ms,
                int64_t max, int64_t *count);
+
+/* Sets the GLM cleaning speed c_h of an ideal GLM-MHD handle for the
+ * following calls (Trixi's GlmSpeedCallback assigns equations.c_h between
+ * steps; the reference's kernels read it from `equations` at every call). */
+int trixi_set_glm_speed(trixi_handle *h, double c_h);
 
 /* Stage entry points with the reference's stage split (the de-facto API used
  * by the reference tests, src/solvers/dg.jl:181-301, docs/src/reference.md:14-30).

@@ -14,9 +14,10 @@ import numpy as np
 
 from . import build as _build_mod
 
-EQ_ADVECTION, EQ_EULER = 0, 1
+EQ_ADVECTION, EQ_EULER, EQ_MHD = 0, 1, 2
 VOL_WEAK, VOL_FLUXDIFF, VOL_SHOCK_HG = 0, 1, 2
-FLUX_LLF, FLUX_RANOCHA, FLUX_CENTRAL, FLUX_LLF_NAIVE = 0, 1, 2, 3
+FLUX_LLF, FLUX_RANOCHA, FLUX_CENTRAL, FLUX_LLF_NAIVE, FLUX_HINDENLANG_GASSNER = 0, 1, 2, 3, 4
+NONCONS_NONE, NONCONS_POWELL = 0, 1
 
 
 class OracleDesc(C.Structure):
@@ -37,6 +38,7 @@ class OracleDesc(C.Structure):
         ("boundary_function", C.c_int32), ("source_terms", C.c_int32),
         ("boundary_params", C.c_double * 8), ("source_params", C.c_double * 3),
         ("node_coordinates", C.POINTER(C.c_double)),
+        ("nonconservative_flux", C.c_int32), ("glm_speed", C.c_double),
     ]
 
 
@@ -105,7 +107,8 @@ class Oracle:
     def __init__(self, containers, ndims, polydeg, nvars, equation, gamma=1.4, advection_velocity=(0, 0, 0),
                  volume_integral=VOL_WEAK, volume_flux=FLUX_CENTRAL, surface_flux=FLUX_LLF,
                  volume_flux_fv=FLUX_LLF, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
-                 boundary_function=-1, boundary_params=None, source_terms=0, source_params=None):
+                 boundary_function=-1, boundary_params=None, source_terms=0, source_params=None,
+                 nonconservative_flux=NONCONS_NONE, glm_speed=0.0):
         lib = load()
         self._keep = dict(
             inv=np.ascontiguousarray(containers.inverse_jacobian, dtype=np.float64),
@@ -145,6 +148,7 @@ class Oracle:
         for i, v in enumerate(source_params if source_params is not None else (2.0, 0.1, 2.0)):
             d.source_params[i] = float(v)
         d.node_coordinates = _pd(k["coords"])
+        d.nonconservative_flux, d.glm_speed = int(nonconservative_flux), float(glm_speed)
         self._desc = d
         self._h = lib.oracle_create(C.byref(d))
         if not self._h:
@@ -157,16 +161,17 @@ class Oracle:
     @classmethod
     def from_semi(cls, semi):
         """Oracle for the same problem as a SemidiscretizationHyperbolicGPU."""
-        from trixicuda.solver import VolumeIntegralFluxDifferencing, VolumeIntegralShockCapturingHG
+        from trixicuda.semidiscretization import flux_codes
+        from trixicuda.solver import VolumeIntegralShockCapturingHG
 
         eq, sol = semi.equations, semi.solver
         vi = sol.volume_integral
-        kw = dict(volume_integral=vi.code, surface_flux=sol.surface_flux.code)
-        if isinstance(vi, VolumeIntegralFluxDifferencing):
-            kw["volume_flux"] = vi.volume_flux.code
+        codes = flux_codes(sol, eq)
+        kw = dict(volume_integral=vi.code, surface_flux=codes["surface_flux"], volume_flux=codes["volume_flux"],
+                  volume_flux_fv=codes["volume_flux_fv"], nonconservative_flux=codes["nonconservative_flux"],
+                  glm_speed=float(getattr(eq, "c_h", 0.0)))
         if isinstance(vi, VolumeIntegralShockCapturingHG):
-            kw.update(volume_flux=vi.volume_flux_dg.code, volume_flux_fv=vi.volume_flux_fv.code,
-                      alpha_max=vi.indicator.alpha_max, alpha_min=vi.indicator.alpha_min,
+            kw.update(alpha_max=vi.indicator.alpha_max, alpha_min=vi.indicator.alpha_min,
                       alpha_smooth=vi.indicator.alpha_smooth)
         av = tuple(getattr(eq, "advection_velocity", np.zeros(eq.ndims)))
         # boundary function and source terms, with the library's parameters

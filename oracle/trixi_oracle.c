@@ -50,7 +50,7 @@
 #endif
 
 #define NMAX 16
-#define NVMAX 5
+#define NVMAX 9
 
 typedef long double ld;
 
@@ -261,9 +261,127 @@ typedef struct {
   int dim, nv, eq;
   double gamma;
   double a[3];
+  double c_h;    /* GLM cleaning speed (ideal GLM-MHD) */
+  int noncons;   /* ORC_NONCONS_* */
 } phys_t;
 
+/* ---- ideal GLM-MHD --------------------------------------------------------
+ * IdealGlmMhdEquations{1,2,3}D.  State (rho, rho v1, rho v2, rho v3, E, B1, B2,
+ * B3, psi) in 2D/3D; 1D has no psi (8 variables).  Velocities and magnetic
+ * fields always have three components.  The GLM formulation follows Derigs,
+ * Winters, Gassner, Walch, Bohm, "Ideal GLM-MHD: about the entropy consistent
+ * nine-wave magnetic field divergence diminishing ideal magnetohydrodynamics
+ * equations", JCP 364 (2018): E = p/(gamma-1) + rho|v|^2/2 + |B|^2/2 + psi^2/2,
+ * the conservative flux carries c_h psi and c_h B_o for the cleaning, and the
+ * transport of psi (v . grad psi) sits in the nonconservative term with the
+ * Powell source. */
+static int mhd_has_psi(const phys_t *P) { return P->nv == 9; }
+
+/* primitive (rho, v1, v2, v3, p, B1, B2, B3, psi) */
+static void mhd_prim(const phys_t *P, const double *u, double *w) {
+  const double rho = u[0];
+  const double v1 = u[1] / rho, v2 = u[2] / rho, v3 = u[3] / rho;
+  const double psi = mhd_has_psi(P) ? u[8] : 0.0;
+  const double kin = 0.5 * rho * (v1 * v1 + v2 * v2 + v3 * v3);
+  const double mag = 0.5 * (u[5] * u[5] + u[6] * u[6] + u[7] * u[7]);
+  w[0] = rho; w[1] = v1; w[2] = v2; w[3] = v3;
+  w[4] = (P->gamma - 1) * (u[4] - kin - mag - 0.5 * psi * psi);
+  w[5] = u[5]; w[6] = u[6]; w[7] = u[7]; w[8] = psi;
+}
+
+/* physical flux along o of ideal GLM-MHD */
+static void mhd_flux(const phys_t *P, const double *u, int o, double *f) {
+  double w[9];
+  mhd_prim(P, u, w);
+  const double rho = w[0], p = w[4], psi = w[8];
+  const double *v = w + 1, *B = w + 5;
+  const double mag = 0.5 * (B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+  const double kin = 0.5 * rho * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  const double vB = v[0] * B[0] + v[1] * B[1] + v[2] * B[2];
+  const double ch = mhd_has_psi(P) ? P->c_h : 0.0;
+  f[0] = rho * v[o];
+  for (int d = 0; d < 3; ++d) f[1 + d] = rho * v[o] * v[d] - B[o] * B[d] + (d == o ? p + mag : 0.0);
+  f[4] = (kin + P->gamma * p / (P->gamma - 1) + 2 * mag) * v[o] - B[o] * vB + ch * psi * B[o];
+  for (int d = 0; d < 3; ++d) f[5 + d] = (d == o) ? ch * psi : v[o] * B[d] - v[d] * B[o];
+  if (mhd_has_psi(P)) f[8] = ch * B[o];
+}
+
+/* Hindenlang & Gassner (2019), "A new entropy conservative two-point flux for
+ * ideal MHD equations derived from first principles" (HONOM 2019): the
+ * logarithmic mean of rho and of rho/p (Ismail-Roe), arithmetic means of v,
+ * p, psi, product means of the magnetic terms, and the energy flux fixed by
+ * the entropy-conservation condition with the nonconservative Powell term. */
+static double ln_mean(double x, double y);
+static double inv_ln_mean(double x, double y);
+static void mhd_flux_hindenlang_gassner(const phys_t *P, const double *ul, const double *ur, int o, double *f) {
+  double wl[9], wr[9];
+  mhd_prim(P, ul, wl);
+  mhd_prim(P, ur, wr);
+  const double rl = wl[0], rr = wr[0], pl = wl[4], pr = wr[4];
+  const double *vl = wl + 1, *vr = wr + 1, *Bl = wl + 5, *Br = wr + 5;
+  const double psil = wl[8], psir = wr[8];
+  const double ch = mhd_has_psi(P) ? P->c_h : 0.0;
+  const double rho_mean = ln_mean(rl, rr);
+  const double inv_rho_p_mean = pl * pr * inv_ln_mean(rl * pr, rr * pl);
+  double vavg[3];
+  for (int d = 0; d < 3; ++d) vavg[d] = 0.5 * (vl[d] + vr[d]);
+  const double pavg = 0.5 * (pl + pr), psiavg = 0.5 * (psil + psir);
+  const double v2avg = 0.5 * (vl[0] * vr[0] + vl[1] * vr[1] + vl[2] * vr[2]);
+  const double b2avg = 0.5 * (Bl[0] * Br[0] + Bl[1] * Br[1] + Bl[2] * Br[2]);
+  const double f0 = rho_mean * vavg[o];
+  f[0] = f0;
+  for (int d = 0; d < 3; ++d)
+    f[1 + d] = f0 * vavg[d] + (d == o ? pavg + b2avg : 0.0) - 0.5 * (Bl[o] * Br[d] + Br[o] * Bl[d]);
+  for (int d = 0; d < 3; ++d)
+    f[5 + d] = (d == o) ? ch * psiavg : 0.5 * (vl[o] * Bl[d] - vl[d] * Bl[o] + vr[o] * Br[d] - vr[d] * Br[o]);
+  if (mhd_has_psi(P)) f[8] = ch * 0.5 * (Bl[o] + Br[o]);
+  double e = pl * vr[o] + pr * vl[o];
+  for (int d = 0; d < 3; ++d) {
+    if (d == o) continue;
+    e += vl[o] * Bl[d] * Br[d] + vr[o] * Br[d] * Bl[d];
+    e -= vl[d] * Bl[o] * Br[d] + vr[d] * Br[o] * Bl[d];
+  }
+  e += ch * (Bl[o] * psir + Br[o] * psil);
+  f[4] = f0 * (v2avg + inv_rho_p_mean / (P->gamma - 1)) + 0.5 * e;
+}
+
+/* fast magnetosonic speed along o */
+static double mhd_fast_speed(const phys_t *P, const double *w, int o) {
+  const double rho = w[0], p = w[4];
+  const double a2 = P->gamma * p / rho;
+  const double b2 = (w[5] * w[5] + w[6] * w[6] + w[7] * w[7]) / rho;
+  const double bo2 = w[5 + o] * w[5 + o] / rho;
+  const double s = a2 + b2;
+  return sqrt(0.5 * (s + sqrt(s * s - 4.0 * a2 * bo2)));
+}
+
+/* Powell + GLM (Galilean) nonconservative two-point term along o with the
+ * local state u_l (Derigs et al. 2018, Bohm et al. JCP 422 (2020)):
+ * phi_Powell(u_l) B_o(u_r) + v_o(u_l) phi_GLM(u_l) psi(u_r), with
+ * phi_Powell = (0, B, v.B, v, 0) and phi_GLM = (0, 0, 0, 0, psi, 0, 0, 0, 1). */
+static void mhd_noncons_powell(const phys_t *P, const double *ul, const double *ur, int o, double *f) {
+  double wl[9], wr[9];
+  mhd_prim(P, ul, wl);
+  mhd_prim(P, ur, wr);
+  const double *vl = wl + 1, *Bl = wl + 5;
+  const double Bo = wr[5 + o], psir = wr[8];
+  const double vB = vl[0] * Bl[0] + vl[1] * Bl[1] + vl[2] * Bl[2];
+  f[0] = 0.0;
+  for (int d = 0; d < 3; ++d) f[1 + d] = Bl[d] * Bo;
+  f[4] = vB * Bo + vl[o] * wl[8] * psir;
+  for (int d = 0; d < 3; ++d) f[5 + d] = vl[d] * Bo;
+  f[8] = vl[o] * psir;
+}
+
 static void cons2prim(const phys_t *P, const double *u, double *rho, double *v, double *p) {
+  if (P->eq == ORC_EQ_MHD) {
+    double w[9];
+    mhd_prim(P, u, w);
+    *rho = w[0];
+    for (int d = 0; d < 3; ++d) v[d] = w[1 + d];
+    *p = w[4];
+    return;
+  }
   double r = u[0], kin = 0;
   for (int d = 0; d < P->dim; ++d) { v[d] = u[1 + d] / r; kin += u[1 + d] * v[d]; }
   *rho = r;
@@ -273,6 +391,7 @@ static void cons2prim(const phys_t *P, const double *u, double *rho, double *v, 
 /* physical flux f_o(u) */
 static void flux_phys(const phys_t *P, const double *u, int o, double *f) {
   if (P->eq == ORC_EQ_ADVECTION) { f[0] = P->a[o] * u[0]; return; }
+  if (P->eq == ORC_EQ_MHD) { mhd_flux(P, u, o, f); return; }
   double rho, v[3], p;
   cons2prim(P, u, &rho, v, &p);
   f[0] = u[1 + o];
@@ -322,6 +441,14 @@ static void flux_central(const phys_t *P, const double *ul, const double *ur, in
 
 static double max_abs_speed(const phys_t *P, const double *ul, const double *ur, int o, int naive) {
   if (P->eq == ORC_EQ_ADVECTION) return fabs(P->a[o]);
+  if (P->eq == ORC_EQ_MHD) {
+    double wl[9], wr[9];
+    mhd_prim(P, ul, wl);
+    mhd_prim(P, ur, wr);
+    const double cl = mhd_fast_speed(P, wl, o), cr = mhd_fast_speed(P, wr, o);
+    if (naive) return fmax(fabs(wl[1 + o]), fabs(wr[1 + o])) + fmax(cl, cr);
+    return fmax(fabs(wl[1 + o]) + cl, fabs(wr[1 + o]) + cr);
+  }
   double rl, rr, vl[3], vr[3], pl, pr;
   cons2prim(P, ul, &rl, vl, &pl);
   cons2prim(P, ur, &rr, vr, &pr);
@@ -339,10 +466,21 @@ static void flux_llf(const phys_t *P, const double *ul, const double *ur, int o,
 static void two_point_flux(const phys_t *P, int kind, const double *ul, const double *ur, int o, double *f) {
   switch (kind) {
     case ORC_FLUX_RANOCHA: flux_ranocha(P, ul, ur, o, f); break;
+    case ORC_FLUX_HINDENLANG_GASSNER: mhd_flux_hindenlang_gassner(P, ul, ur, o, f); break;
     case ORC_FLUX_CENTRAL: flux_central(P, ul, ur, o, f); break;
     case ORC_FLUX_LLF_NAIVE: flux_llf(P, ul, ur, o, 1, f); break;
     default: flux_llf(P, ul, ur, o, 0, f); break;
   }
+}
+
+/* f += 0.5 Phi(u_own, u_other): the nonconservative part of a surface or FV
+ * subcell flux seen from the element (node) holding u_own
+ * (src/solvers/dg_2d_kernel.jl:958-1035) */
+static void add_half_noncons(const phys_t *P, const double *uown, const double *uother, int o, double *f) {
+  if (P->noncons != ORC_NONCONS_POWELL) return;
+  double nc[NVMAX];
+  mhd_noncons_powell(P, uown, uother, o, nc);
+  for (int v = 0; v < P->nv; ++v) f[v] += 0.5 * nc[v];
 }
 
 /* ------------------------------------------------------------------------ */
@@ -383,6 +521,7 @@ oracle_handle *oracle_create(const oracle_desc *desc) {
   h->NV = desc->nvars;
   h->nchild = (int)ipow(2, h->DIM - 1);
   h->P.dim = h->DIM; h->P.nv = h->NV; h->P.eq = desc->equation; h->P.gamma = desc->gamma;
+  h->P.c_h = desc->glm_speed; h->P.noncons = desc->nonconservative_flux;
   for (int d = 0; d < 3; ++d) h->P.a[d] = desc->advection_velocity[d];
   oracle_basis(desc->polydeg, h->nodes, h->w, NULL, h->dsplit, h->dhat, h->ivdm, h->fup, h->flo, h->rup, h->rlo);
   for (int i = 0; i < h->N; ++i) h->invw[i] = 1.0 / h->w[i];
@@ -480,16 +619,24 @@ void oracle_volume_integral(oracle_handle *h, double *du, const double *u, const
       dg_only = fabs(a - 0.0) <= atol;
     }
     for (int n = 0; n < NN; ++n) {
-      double val[NVMAX] = {0, 0, 0, 0, 0};
+      double val[NVMAX] = {0};
       if (!dg_only) {
         /* FV subcell fluxes between neighbouring LGL nodes on each line; the
          * element-boundary ones are zero (volume_flux_integral_dgfv_kernel!):
          * alpha * sum_d inv_w[i_d] * (fstar_d[i_d+1] - fstar_d[i_d]) */
         for (int d = 0; d < DIM; ++d) {
           int i = coord_of(N, n, d);
-          double fr[NVMAX] = {0, 0, 0, 0, 0}, fl[NVMAX] = {0, 0, 0, 0, 0};
-          if (i + 1 < N) two_point_flux(P, h->d.volume_flux_fv, ue + NV * n, ue + NV * with_coord(N, n, d, i + 1), d, fr);
-          if (i > 0) two_point_flux(P, h->d.volume_flux_fv, ue + NV * with_coord(N, n, d, i - 1), ue + NV * n, d, fl);
+          double fr[NVMAX] = {0}, fl[NVMAX] = {0};
+          if (i + 1 < N) {
+            const double *un = ue + NV * with_coord(N, n, d, i + 1);
+            two_point_flux(P, h->d.volume_flux_fv, ue + NV * n, un, d, fr);
+            add_half_noncons(P, ue + NV * n, un, d, fr);  /* fstar_L (dg_2d_kernel.jl:650-656) */
+          }
+          if (i > 0) {
+            const double *un = ue + NV * with_coord(N, n, d, i - 1);
+            two_point_flux(P, h->d.volume_flux_fv, un, ue + NV * n, d, fl);
+            add_half_noncons(P, ue + NV * n, un, d, fl);  /* fstar_R */
+          }
           for (int v = 0; v < NV; ++v) val[v] += h->invw[i] * (fr[v] - fl[v]);
         }
         for (int v = 0; v < NV; ++v) val[v] = a * val[v];
@@ -513,6 +660,20 @@ void oracle_volume_integral(oracle_handle *h, double *du, const double *u, const
             s += (dg_only ? Dm : (1 - a) * Dm) * f[d][v];
           }
           val[v] += s;
+        }
+      }
+      /* nonconservative terms: 0.5 sum_d sum_m D_split[i_d, m] Phi_d(u_n, u_m), the
+       * full D_split row (dg_2d_kernel.jl:269-292, 729-741), weighted like the DG part */
+      if (P->noncons == ORC_NONCONS_POWELL) {
+        const double wdg = dg_only ? 1.0 : (1 - a);
+        for (int d = 0; d < DIM; ++d) {
+          int i = coord_of(N, n, d);
+          for (int m = 0; m < N; ++m) {
+            double nc[NVMAX];
+            mhd_noncons_powell(P, ue + NV * n, ue + NV * with_coord(N, n, d, m), d, nc);
+            const double Dm = h->dsplit[i + N * m];
+            for (int v = 0; v < NV; ++v) val[v] += wdg * 0.5 * Dm * nc[v];
+          }
         }
       }
       for (int v = 0; v < NV; ++v) due[NV * n + v] = val[v];
@@ -549,9 +710,15 @@ void oracle_interface_flux(oracle_handle *h, const double *iu, double *sfv) {
         ur[v] = iu[1 + 2 * (v + NV * (f + (int64_t)NF * k))];
       }
       two_point_flux(&h->P, h->d.surface_flux, ul, ur, o, fs);
+      /* with nonconservative terms each side adds 0.5 Phi(own, other)
+       * (interface_flux_kernel!, dg_2d_kernel.jl:1009-1035) */
+      double fl[NVMAX], fr[NVMAX];
+      for (int v = 0; v < NV; ++v) fl[v] = fr[v] = fs[v];
+      add_half_noncons(&h->P, ul, ur, o, fl);
+      add_half_noncons(&h->P, ur, ul, o, fr);
       for (int v = 0; v < NV; ++v) {
-        sfv[v + NV * (f + (int64_t)NF * ((2 * o + 1) + 2 * DIM * left))] = fs[v];
-        sfv[v + NV * (f + (int64_t)NF * ((2 * o) + 2 * DIM * right))] = fs[v];
+        sfv[v + NV * (f + (int64_t)NF * ((2 * o + 1) + 2 * DIM * left))] = fl[v];
+        sfv[v + NV * (f + (int64_t)NF * ((2 * o) + 2 * DIM * right))] = fr[v];
       }
     }
   }
@@ -621,9 +788,18 @@ void oracle_mortar_flux(oracle_handle *h, double *const *mu, double *sfv) {
           ur[v] = mu[c][1 + 2 * (v + NV * (f + (int64_t)NF * m))];
         }
         two_point_flux(&h->P, h->d.surface_flux, ul, ur, o, fs);
+        /* nonconservative terms (mortar_flux_kernel!, dg_2d_kernel.jl:1290-1344):
+         * the small elements get 0.5 Phi(u_large, u_small) ("primary"), the
+         * projection to the large element 0.5 Phi(u_small, u_large) ("secondary"),
+         * u_large being the large element's trace projected onto the mortar */
+        double fp[NVMAX], fsec[NVMAX];
+        for (int v = 0; v < NV; ++v) fp[v] = fsec[v] = fs[v];
+        const double *u_large = (ls == 1) ? ul : ur, *u_small = (ls == 1) ? ur : ul;
+        add_half_noncons(&h->P, u_large, u_small, o, fp);
+        add_half_noncons(&h->P, u_small, u_large, o, fsec);
         for (int v = 0; v < NV; ++v) {
-          fstar[c][v + NV * f] = fs[v];
-          sfv[v + NV * (f + (int64_t)NF * (small_dir + 2 * DIM * small))] = fs[v];
+          fstar[c][v + NV * f] = fsec[v];
+          sfv[v + NV * (f + (int64_t)NF * (small_dir + 2 * DIM * small))] = fp[v];
         }
       }
     }

@@ -33,9 +33,11 @@
 extern "C" {
 #endif
 
-enum { ORC_EQ_ADVECTION = 0, ORC_EQ_EULER = 1 };
+enum { ORC_EQ_ADVECTION = 0, ORC_EQ_EULER = 1, ORC_EQ_MHD = 2 };
+enum { ORC_NONCONS_NONE = 0, ORC_NONCONS_POWELL = 1 };
 enum { ORC_VOL_WEAK = 0, ORC_VOL_FLUXDIFF = 1, ORC_VOL_SHOCK_HG = 2 };
-enum { ORC_FLUX_LLF = 0, ORC_FLUX_RANOCHA = 1, ORC_FLUX_CENTRAL = 2, ORC_FLUX_LLF_NAIVE = 3 };
+enum { ORC_FLUX_LLF = 0, ORC_FLUX_RANOCHA = 1, ORC_FLUX_CENTRAL = 2, ORC_FLUX_LLF_NAIVE = 3,
+       ORC_FLUX_HINDENLANG_GASSNER = 4 };
 enum { ORC_IC_CONSTANT = 0, ORC_IC_CONVERGENCE_TEST = 1, ORC_IC_WEAK_BLAST_WAVE = 2 };
 enum { ORC_SRC_NONE = 0, ORC_SRC_CONVERGENCE_TEST = 1 };
 
@@ -64,6 +66,10 @@ typedef struct {
   double boundary_params[8];                /* constant state, or (c, A, L) of the convergence test */
   double source_params[3];                  /* (c, A, L) of the manufactured solution */
   const double *node_coordinates;           /* [ndims, N^ndims, nelements] (needed with boundaries / sources) */
+  /* ideal GLM-MHD: the nonconservative flux paired with the volume and surface
+   * fluxes (flux_nonconservative_powell) and the GLM cleaning speed c_h */
+  int32_t nonconservative_flux;             /* ORC_NONCONS_* */
+  double glm_speed;
 } oracle_desc;
 
 typedef struct oracle_handle oracle_handle;

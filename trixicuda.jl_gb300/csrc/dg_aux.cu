@@ -32,13 +32,26 @@ __device__ __forceinline__ void flux_dispatch(int kind, int o, const R *ul, cons
   if constexpr (DIM > 2) if (o == 2) two_point_flux<DIM, EQ, R, 2>(kind, ul, wl, ur, wr, f, pp);
 }
 
+// f += s * Phi_o(own, other), the nonconservative term of ideal GLM-MHD in
+// 2D/3D (nothing for the other systems)
+template <int DIM, int EQ, typename R>
+__device__ __forceinline__ void add_noncons_rt(int o, const R *wown, const R *wother, R s, R *f) {
+  if constexpr (EQ == EQ_MHD && DIM > 1) {
+    using P = Physics<DIM, EQ, R>;
+    if (o == 0) P::template add_noncons<0>(wown, wother, s, f);
+    if (o == 1) P::template add_noncons<1>(wown, wother, s, f);
+    if constexpr (DIM > 2) if (o == 2) P::template add_noncons<2>(wown, wother, s, f);
+  }
+}
+
 template <typename R>
-static PhysParams<R> make_pp(double gamma, const double *adv) {
+static PhysParams<R> make_pp(double gamma, const double *adv, double c_h = 0.0) {
   PhysParams<R> pp;
   pp.gamma = R(gamma);
   pp.gm1 = R(gamma - 1.0);
   pp.inv_gm1 = R(1.0 / (gamma - 1.0));
   for (int d = 0; d < 3; ++d) pp.a[d] = R(adv[d]);
+  pp.c_h = R(c_h);
   return pp;
 }
 
@@ -116,10 +129,22 @@ __global__ void mortar_prepass_kernel(int N, int64_t M, const double *__restrict
     Physics<DIM, EQ, R>::prim(ul, wl, pp);
     Physics<DIM, EQ, R>::prim(ur, wr, pp);
     flux_dispatch<DIM, EQ, R>(surface_flux, o, ul, wl, ur, wr, fs, pp);
+    // nonconservative terms (mortar_flux_kernel!, src/solvers/dg_2d_kernel.jl:1290-1344):
+    // the small element's flux adds 0.5 Phi(u_large, u_small) ("primary"), the
+    // one projected to the large element 0.5 Phi(u_small, u_large) ("secondary"),
+    // u_large being the large element's trace projected onto the small face
+    R fsec[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) fsec[v] = fs[v];
+    if constexpr (EQ == EQ_MHD && DIM > 1) {
+      const R *w_large = (ls == 1) ? wl : wr, *w_small = (ls == 1) ? wr : wl;
+      add_noncons_rt<DIM, EQ, R>(o, w_large, w_small, R(0.5), fs);
+      add_noncons_rt<DIM, EQ, R>(o, w_small, w_large, R(0.5), fsec);
+    }
     double *dst = out + ((m * (NC + 1) + c) * NF + f) * NV;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      s_fstar[(c * NF + f) * NV + v] = double(fs[v]);
+      s_fstar[(c * NF + f) * NV + v] = double(fsec[v]);
       dst[v] = double(fs[v]);
     }
   }
@@ -162,12 +187,17 @@ static cudaError_t launch_mortar_t(const MortarHost &mh, cudaStream_t s) {
   const int block = std::max(32, std::min(256, ((NC * NF + 31) / 32) * 32));
   mortar_prepass_kernel<DIM, EQ, R><<<(unsigned)mh.nmortars, block, smem, s>>>(
       mh.N, mh.nmortars, mh.u, mh.neighbor_ids, mh.large_sides, mh.orientations, mh.mortar_flux, mh.surface_flux,
-      make_pp<R>(mh.gamma, mh.adv), mats, mh.err);
+      make_pp<R>(mh.gamma, mh.adv, mh.c_h), mats, mh.err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mortar_flux(const MortarHost &mh, cudaStream_t s) {
   if (mh.nmortars <= 0) return cudaSuccess;
+  if (mh.eq == EQ_MHD) {
+    if (mh.dim == 2) return mh.mixed ? launch_mortar_t<2, EQ_MHD, float>(mh, s) : launch_mortar_t<2, EQ_MHD, double>(mh, s);
+    if (mh.dim == 3) return mh.mixed ? launch_mortar_t<3, EQ_MHD, float>(mh, s) : launch_mortar_t<3, EQ_MHD, double>(mh, s);
+    return cudaErrorNotSupported;
+  }
   if (mh.dim == 2) {
     if (mh.eq == EQ_ADV) return mh.mixed ? launch_mortar_t<2, EQ_ADV, float>(mh, s) : launch_mortar_t<2, EQ_ADV, double>(mh, s);
     return mh.mixed ? launch_mortar_t<2, EQ_EULER, float>(mh, s) : launch_mortar_t<2, EQ_EULER, double>(mh, s);
@@ -192,8 +222,8 @@ struct IvdmMat {
 template <int DIM>
 __global__ void indicator_raw_kernel(int N, int64_t E, int epb, const double *__restrict__ u, double *__restrict__ alpha_raw,
                                      double gamma, double amax, double amin, double threshold, double param_s,
-                                     IvdmMat ivdm) {
-  constexpr int NV = DIM + 2;
+                                     IvdmMat ivdm, int mhd) {
+  const int NV = mhd ? (DIM == 1 ? 8 : 9) : DIM + 2;
   extern __shared__ __align__(16) double sm[];
   int NN = N;
   for (int d = 1; d < DIM; ++d) NN *= N;
@@ -205,9 +235,19 @@ __global__ void indicator_raw_kernel(int N, int64_t E, int epb, const double *__
     const int el = i / NN, n = i - el * NN;
     const double *un = u + ((e0 + el) * NN + n) * NV;
     const double rho = un[0];
-    double kin = 0.0;
-    for (int d = 0; d < DIM; ++d) kin += un[1 + d] * (un[1 + d] / rho);
-    const double p = (gamma - 1.0) * (un[DIM + 1] - 0.5 * kin);
+    double kin = 0.0, p;
+    if (mhd) {  // p = (gamma-1)(E - rho|v|^2/2 - |B|^2/2 - psi^2/2)
+      double mag = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        kin += un[1 + d] * (un[1 + d] / rho);
+        mag += un[5 + d] * un[5 + d];
+      }
+      if (NV == 9) mag += un[8] * un[8];
+      p = (gamma - 1.0) * (un[4] - 0.5 * kin - 0.5 * mag);
+    } else {
+      for (int d = 0; d < DIM; ++d) kin += un[1 + d] * (un[1 + d] / rho);
+      p = (gamma - 1.0) * (un[DIM + 1] - 0.5 * kin);
+    }
     s_a[i] = rho * p;
   }
   __syncthreads();
@@ -283,13 +323,16 @@ cudaError_t launch_indicator(const IndicatorHost &ih, cudaStream_t s) {
   std::copy(ih.ivdm, ih.ivdm + HOST_NMAX * HOST_NMAX, iv.m);
   if (ih.dim == 1)
     indicator_raw_kernel<1><<<(unsigned)grid, block, smem, s>>>(ih.N, ih.nelements, epb, ih.u, ih.alpha_raw, ih.gamma,
-                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv);
+                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
+                                                              ih.eq == EQ_MHD ? 1 : 0);
   else if (ih.dim == 2)
     indicator_raw_kernel<2><<<(unsigned)grid, block, smem, s>>>(ih.N, ih.nelements, epb, ih.u, ih.alpha_raw, ih.gamma,
-                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv);
+                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
+                                                              ih.eq == EQ_MHD ? 1 : 0);
   else
     indicator_raw_kernel<3><<<(unsigned)grid, block, smem, s>>>(ih.N, ih.nelements, epb, ih.u, ih.alpha_raw, ih.gamma,
-                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv);
+                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
+                                                              ih.eq == EQ_MHD ? 1 : 0);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   indicator_smooth_kernel<<<(unsigned)((ih.nelements + 255) / 256), 256, 0, s>>>(
@@ -412,10 +455,17 @@ __global__ void interface_flux_kernel(int N, int64_t I, const double *__restrict
   Physics<DIM, EQ, double>::prim(ur, wr, pp);
   flux_dispatch<DIM, EQ, double>(kind, o, ul, wl, ur, wr, fs, pp);
   const int64_t left = nid[2 * k] - 1, right = nid[2 * k + 1] - 1;
+  // nonconservative terms: left adds 0.5 Phi(u_ll, u_rr), right 0.5 Phi(u_rr, u_ll)
+  // (surface_noncons_flux_kernel! + interface_flux_kernel!, dg_2d_kernel.jl:958-1035)
+  double fr[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) fr[v] = fs[v];
+  add_noncons_rt<DIM, EQ, double>(o, wl, wr, 0.5, fs);
+  add_noncons_rt<DIM, EQ, double>(o, wr, wl, 0.5, fr);
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
     sfv[v + NV * (f + (int64_t)NF * ((2 * o + 1) + 2 * DIM * left))] = fs[v];
-    sfv[v + NV * (f + (int64_t)NF * ((2 * o) + 2 * DIM * right))] = fs[v];
+    sfv[v + NV * (f + (int64_t)NF * ((2 * o) + 2 * DIM * right))] = fr[v];
   }
 }
 
@@ -493,9 +543,19 @@ __global__ void mortar_flux_stage_kernel(int N, int64_t M, MortarArrays arr, con
     Physics<DIM, EQ, double>::prim(ur, wr, pp);
     flux_dispatch<DIM, EQ, double>(kind, o, ul, wl, ur, wr, fs, pp);
     const int64_t small = nid[c + (NC + 1) * m] - 1;
+    // nonconservative terms: primary 0.5 Phi(u_large, u_small) to the small
+    // element, secondary 0.5 Phi(u_small, u_large) projected to the large one
+    double fsec[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) fsec[v] = fs[v];
+    if constexpr (EQ == EQ_MHD) {
+      const double *w_large = (ls == 1) ? wl : wr, *w_small = (ls == 1) ? wr : wl;
+      add_noncons_rt<DIM, EQ, double>(o, w_large, w_small, 0.5, fs);
+      add_noncons_rt<DIM, EQ, double>(o, w_small, w_large, 0.5, fsec);
+    }
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      sm[(c * NF + f) * NV + v] = fs[v];
+      sm[(c * NF + f) * NV + v] = fsec[v];
       sfv[v + NV * (f + (int64_t)NF * (small_dir + 2 * DIM * small))] = fs[v];
     }
   }
@@ -593,12 +653,20 @@ static cudaError_t launch_iflux(const StageHost &sh, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   interface_flux_kernel<DIM, EQ><<<blocks_for(n, 128), 128, 0, s>>>(sh.N, sh.ninterfaces, sh.interfaces_u,
                                                                    sh.if_neighbor_ids, sh.if_orientations, sh.sfv,
-                                                                   sh.surface_flux, make_pp<double>(sh.gamma, sh.adv));
+                                                                   sh.surface_flux, make_pp<double>(sh.gamma, sh.adv, sh.c_h));
   return cudaGetLastError();
 }
 
 cudaError_t stage_interface_flux(const StageHost &sh, cudaStream_t s) {
   const bool adv = sh.eq == EQ_ADV;
+  if (sh.eq == EQ_MHD) {
+    switch (sh.dim) {
+      case 1: return launch_iflux<1, EQ_MHD>(sh, s);
+      case 2: return launch_iflux<2, EQ_MHD>(sh, s);
+      case 3: return launch_iflux<3, EQ_MHD>(sh, s);
+    }
+    return cudaErrorNotSupported;
+  }
   switch (sh.dim) {
     case 1: return adv ? launch_iflux<1, EQ_ADV>(sh, s) : launch_iflux<1, EQ_EULER>(sh, s);
     case 2: return adv ? launch_iflux<2, EQ_ADV>(sh, s) : launch_iflux<2, EQ_EULER>(sh, s);
@@ -629,6 +697,7 @@ static cudaError_t launch_bflux(const StageHost &sh, double t, cudaStream_t s) {
 
 cudaError_t stage_boundary_flux(const StageHost &sh, double t, cudaStream_t s) {
   if (sh.nboundaries == 0) return cudaSuccess;
+  if (sh.eq == EQ_MHD) return cudaErrorNotSupported;
   const bool adv = sh.eq == EQ_ADV;
   switch (sh.dim) {
     case 1: return adv ? launch_bflux<1, EQ_ADV>(sh, t, s) : launch_bflux<1, EQ_EULER>(sh, t, s);
@@ -681,12 +750,13 @@ static cudaError_t launch_mflux(const StageHost &sh, cudaStream_t s) {
   const size_t smem = sizeof(double) * (size_t)NC * NF * NV;
   mortar_flux_stage_kernel<DIM, EQ><<<(unsigned)sh.nmortars, 128, smem, s>>>(
       sh.N, sh.nmortars, arr, sh.mo_neighbor_ids, sh.mo_large_sides, sh.mo_orientations, sh.sfv, sh.surface_flux,
-      make_pp<double>(sh.gamma, sh.adv), mats_of(sh));
+      make_pp<double>(sh.gamma, sh.adv, sh.c_h), mats_of(sh));
   return cudaGetLastError();
 }
 
 cudaError_t stage_mortar_flux(const StageHost &sh, cudaStream_t s) {
   if (sh.nmortars == 0 || sh.dim < 2) return cudaSuccess;
+  if (sh.eq == EQ_MHD) return sh.dim == 2 ? launch_mflux<2, EQ_MHD>(sh, s) : launch_mflux<3, EQ_MHD>(sh, s);
   const bool adv = sh.eq == EQ_ADV;
   if (sh.dim == 2) return adv ? launch_mflux<2, EQ_ADV>(sh, s) : launch_mflux<2, EQ_EULER>(sh, s);
   return adv ? launch_mflux<3, EQ_ADV>(sh, s) : launch_mflux<3, EQ_EULER>(sh, s);

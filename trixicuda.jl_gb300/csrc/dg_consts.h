@@ -7,11 +7,16 @@ namespace trixi {
 
 constexpr int EQ_ADV = 0;    // TRIXI_EQ_LINEAR_ADVECTION
 constexpr int EQ_EULER = 1;  // TRIXI_EQ_COMPRESSIBLE_EULER
+constexpr int EQ_MHD = 2;    // TRIXI_EQ_IDEAL_GLM_MHD
 
 constexpr int FLUX_LLF = 0;        // TRIXI_FLUX_LAX_FRIEDRICHS
 constexpr int FLUX_RANOCHA = 1;    // TRIXI_FLUX_RANOCHA
 constexpr int FLUX_CENTRAL = 2;    // TRIXI_FLUX_CENTRAL
 constexpr int FLUX_LLF_NAIVE = 3;  // TRIXI_FLUX_LAX_FRIEDRICHS_NAIVE
+constexpr int FLUX_HG = 4;         // TRIXI_FLUX_HINDENLANG_GASSNER
+
+constexpr int NONCONS_NONE = 0;    // TRIXI_NONCONSERVATIVE_NONE
+constexpr int NONCONS_POWELL = 1;  // TRIXI_NONCONSERVATIVE_POWELL
 
 constexpr int VOL_WEAK = 0;  // TRIXI_VOLUME_WEAK_FORM
 constexpr int VOL_FD = 1;    // TRIXI_VOLUME_FLUX_DIFFERENCING

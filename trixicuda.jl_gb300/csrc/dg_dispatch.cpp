@@ -6,6 +6,11 @@ namespace trixi {
 bool fused_supported(int dim, int N, int eq, int vol, int vflux) {
   if (dim < 1 || dim > 3 || N < 2 || N > HOST_NMAX) return false;
   if (eq == 0) return vol == 0 || (vol == 1 && vflux == 2);  // advection: weak form, central flux differencing
+  if (eq == 2) {  // ideal GLM-MHD: polydeg <= 4; FD with flux_hindenlang_gassner / flux_central, SC with the former
+    if (N > 5) return false;
+    return (vol == 1 && (vflux == 4 || vflux == 2)) || (vol == 2 && vflux == 4);
+  }
+  if (vflux == 4) return false;  // flux_hindenlang_gassner is the MHD flux
   if (vol == 0) return true;
   if (vol == 1 || vol == 2) return vflux == 1 || vflux == 2;  // flux_ranocha, flux_central
   return false;
@@ -14,6 +19,15 @@ bool fused_supported(int dim, int N, int eq, int vol, int vflux) {
 cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed, const FusedHost &h,
                          cudaStream_t s) {
   if (!fused_supported(dim, N, eq, vol, vflux)) return cudaErrorNotSupported;
+  if (eq == 2) {  // ideal GLM-MHD (periodic meshes, no source terms)
+    if (h.bc_kind >= 0 || h.src_kind != 0) return cudaErrorNotSupported;
+    switch (dim) {
+      case 1: return mixed ? launch_fused_1d_f32_mhd(N, eq, vol, vflux, h, s) : launch_fused_1d_f64_mhd(N, eq, vol, vflux, h, s);
+      case 2: return mixed ? launch_fused_2d_f32_mhd(N, eq, vol, vflux, h, s) : launch_fused_2d_f64_mhd(N, eq, vol, vflux, h, s);
+      case 3: return mixed ? launch_fused_3d_f32_mhd(N, eq, vol, vflux, h, s) : launch_fused_3d_f64_mhd(N, eq, vol, vflux, h, s);
+    }
+    return cudaErrorNotSupported;
+  }
   if (h.bc_kind >= 0 || h.src_kind != 0) {  // the instantiations with boundary states and sources
     switch (dim) {
       case 1:

@@ -198,6 +198,13 @@ template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX, int BND = 0>
 struct FusedKernel {
   using P = Physics<DIM, EQ, R>;
   static constexpr int NV = P::NV;
+  // nonconservative terms (ideal GLM-MHD in 2D/3D: Powell + GLM transport)
+  static constexpr bool NC = (EQ == EQ_MHD && DIM > 1);
+  // FV subcell fluxes per interface: one, or with nonconservative terms one
+  // per side (fstar_L / fstar_R of src/solvers/dg_2d_kernel.jl:609-707)
+  static constexpr int FV_RECS = NC ? 2 : 1;
+  // largest block: 16 warps, 8 for the register-heavy MHD kernels
+  static constexpr int MAX_WARPS = (EQ == EQ_MHD) ? 8 : 16;
   static constexpr int NN = ipow(N, DIM);
   static constexpr int NF = ipow(N, DIM - 1);
   static constexpr int NP = N * (N - 1) / 2;
@@ -216,7 +223,7 @@ struct FusedKernel {
   static constexpr int n_cons(int epg) { return round_up4(epg * NN * NV); }
   static constexpr int n_vol(int epg) { return round_up4(epg * DIM * VOL_PER_DIR * NV); }
   static constexpr int n_surf(int epg) { return round_up4(epg * SURF_PER_EL * NV); }
-  static constexpr int n_fv(int epg) { return round_up4(epg * DIM * FV_PER_DIR * NV); }
+  static constexpr int n_fv(int epg) { return round_up4(epg * DIM * FV_PER_DIR * FV_RECS * NV); }
   static constexpr int n_trace(int epg) { return round_up4(epg * TRACE_PER_EL); }
   static constexpr int n_el(int epg) { return round_up4(epg); }
   static constexpr int N_OPS = round_up4(2 * N * N + N);  // D_split, D_hat, 1/w
@@ -315,9 +322,9 @@ struct FusedKernel {
     __device__ __forceinline__ R *surf(int el, int face, int t) const {
       return fsurf + ((el * 2 * DIM + face) * NF + t) * NV;
     }
-    // [el][dir][t][a][v]
-    __device__ __forceinline__ R *fv(int el, int d, int t, int a) const {
-      return ffv + (((el * DIM + d) * NF + t) * (N - 1) + a) * NV;
+    // [el][dir][t][a][side][v]: side 0 seen from node a (left), 1 from node a+1
+    __device__ __forceinline__ R *fv(int el, int d, int t, int a, int side = 0) const {
+      return ffv + ((((el * DIM + d) * NF + t) * (N - 1) + a) * FV_RECS + side) * NV;
     }
   };
 
@@ -373,6 +380,9 @@ struct FusedKernel {
         two_point_flux<DIM, EQ, R, O>(p.surface_flux, un, wn, uo, wo, f, p.pp);
       else
         two_point_flux<DIM, EQ, R, O>(p.surface_flux, uo, wo, un, wn, f, p.pp);
+      // nonconservative terms: each side adds 0.5 Phi(own, other)
+      // (interface_flux_kernel!, src/solvers/dg_2d_kernel.jl:1009-1035)
+      if constexpr (NC) P::template add_noncons<O>(wo, wn, R(0.5), f);
     }
     sts_rec<NV>(s.surf(el, face, t), f);
   }
@@ -387,6 +397,14 @@ struct FusedKernel {
     lds_rec<NV>(s.c(el, nr), ur);
     lds_rec<NV>(s.w(el, nr), wr);
     two_point_flux<DIM, EQ, R, O>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
+    if constexpr (NC) {
+      R g[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) g[v] = f[v];
+      P::template add_noncons<O>(wl, wr, R(0.5), f);  // fstar_L: node a's side
+      P::template add_noncons<O>(wr, wl, R(0.5), g);  // fstar_R: node a+1's side
+      sts_rec<NV>(s.fv(el, O, t, a, 1), g);
+    }
     sts_rec<NV>(s.fv(el, O, t, a), f);
   }
 
@@ -589,6 +607,33 @@ struct FusedKernel {
         }
       }
     }
+    if constexpr (NC) {
+      // nonconservative volume term 0.5 sum_d sum_m D_split[i_d, m] Phi_d(u_i, u_m)
+      // (src/solvers/dg_2d_kernel.jl:269-292).  Phi_d(u_i, u_m) is linear in
+      // u_m's (B_d, psi), so the sum is Phi_d(u_i, .) of sum_m D_split[i_d, m] (B_d, psi)_m.
+      R wo[NV];
+      lds_rec<NV>(s.w(el, node), wo);
+      constexpr int strides[3] = {1, N, N * N};
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        const int ci = coord[d];
+        const int n0 = node - ci * strides[d];
+        R g[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) g[v] = R(0);
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          if (m == ci) continue;
+          const R dm = s.dsplit[ci * N + m];
+          const R *wm = s.w(el, n0 + m * strides[d]);
+          g[5 + d] += dm * wm[5 + d];
+          g[8] += dm * wm[8];
+        }
+        if (d == 0) P::template add_noncons<0>(wo, g, R(0.5), acc);
+        if constexpr (DIM > 1) if (d == 1) P::template add_noncons<1>(wo, g, R(0.5), acc);
+        if constexpr (DIM > 2) if (d == 2) P::template add_noncons<2>(wo, g, R(0.5), acc);
+      }
+    }
     if constexpr (VOL == VOL_SC) {
       const R alpha = s.alpha[el];
       if (alpha != R(0)) {
@@ -607,7 +652,7 @@ struct FusedKernel {
           }
           if (ci > 0) {
             R F[NV];
-            lds_rec<NV>(s.fv(el, d, tface[d], ci - 1), F);
+            lds_rec<NV>(s.fv(el, d, tface[d], ci - 1, NC ? 1 : 0), F);
 #pragma unroll
             for (int v = 0; v < NV; ++v) fv[v] -= iw * F[v];
           }
@@ -694,6 +739,20 @@ struct FusedKernel {
 template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX, int BND>
 __global__ void __launch_bounds__(512) dg_fused_kernel(const FusedParams<R> p) {
   FusedKernel<DIM, N, EQ, R, VOL, VFLUX, BND>::run(p);
+}
+
+// the ideal GLM-MHD kernels: blocks of at most 256 threads, so that a thread
+// may hold up to 255 registers (9-variable states)
+template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX, int BND>
+__global__ void __launch_bounds__(256, 1) dg_fused_kernel_wide(const FusedParams<R> p) {
+  FusedKernel<DIM, N, EQ, R, VOL, VFLUX, BND>::run(p);
+}
+
+// the kernel entry of an instantiation
+template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX, int BND>
+constexpr auto fused_entry() {
+  if constexpr (EQ == EQ_MHD) return &dg_fused_kernel_wide<DIM, N, EQ, R, VOL, VFLUX, BND>;
+  else return &dg_fused_kernel<DIM, N, EQ, R, VOL, VFLUX, BND>;
 }
 
 }  // namespace trixi

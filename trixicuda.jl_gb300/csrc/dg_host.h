@@ -30,6 +30,7 @@ struct FusedHost {
   double rk_a = 0, rk_b = 0, dt = 0, atol = 0;
   double gamma = 1.4;
   double adv[3] = {0, 0, 0};
+  double c_h = 0.0;  // GLM cleaning speed (ideal GLM-MHD)
   int N = 0;
   double dsplit[HOST_NMAX * HOST_NMAX] = {};  // row-major, diagonal zeroed
   double dhat[HOST_NMAX * HOST_NMAX] = {};    // row-major
@@ -55,6 +56,7 @@ struct FusedTile {
   int min_wpg = 0;        // warps owning the group's nodes
   int def_wpg = 0, def_gpb = 0;
   size_t group_smem = 0;  // bytes of shared memory per group
+  int max_warps = 16;     // warps per block allowed by the instantiation's launch bounds
 };
 
 // Returns cudaErrorNotSupported when the combination is not compiled.
@@ -74,6 +76,13 @@ cudaError_t launch_fused_3d_f64(int N, int eq, int vol, int vflux, const FusedHo
 cudaError_t launch_fused_1d_f32(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 cudaError_t launch_fused_2d_f32(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 cudaError_t launch_fused_3d_f32(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+// ideal GLM-MHD instantiations (periodic meshes)
+cudaError_t launch_fused_1d_f64_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_1d_f32_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_2d_f64_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_2d_f32_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_3d_f64_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_3d_f32_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 
 // Auxiliary kernels (dg_aux.cu).
 struct MortarHost {
@@ -87,6 +96,7 @@ struct MortarHost {
   int surface_flux = 0;
   bool mixed = false;
   double gamma = 1.4, adv[3] = {0, 0, 0};
+  double c_h = 0.0;
   double fwd_up[HOST_NMAX * HOST_NMAX] = {}, fwd_lo[HOST_NMAX * HOST_NMAX] = {};  // row-major [j][i]
   double rev_up[HOST_NMAX * HOST_NMAX] = {}, rev_lo[HOST_NMAX * HOST_NMAX] = {};  // row-major [k][j]
   int *err = nullptr;
@@ -94,7 +104,7 @@ struct MortarHost {
 cudaError_t launch_mortar_flux(const MortarHost &m, cudaStream_t s);
 
 struct IndicatorHost {
-  int dim = 2, N = 0, nv = 4;
+  int dim = 2, N = 0, nv = 4, eq = 1;
   int64_t nelements = 0;
   const double *u = nullptr;
   double *alpha_raw = nullptr;
@@ -120,6 +130,7 @@ struct StageHost {
   double *mortar_u[4] = {nullptr, nullptr, nullptr, nullptr};
   int surface_flux = 0;
   double gamma = 1.4, adv[3] = {0, 0, 0};
+  double c_h = 0.0;
   double fwd_up[HOST_NMAX * HOST_NMAX] = {}, fwd_lo[HOST_NMAX * HOST_NMAX] = {};
   double rev_up[HOST_NMAX * HOST_NMAX] = {}, rev_lo[HOST_NMAX * HOST_NMAX] = {};
   double lhat_l = 0, lhat_r = 0;

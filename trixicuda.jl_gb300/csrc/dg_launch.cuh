@@ -43,6 +43,7 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   p.pp.gm1 = R(h.gamma - 1.0);
   p.pp.inv_gm1 = R(1.0 / (h.gamma - 1.0));
   for (int d = 0; d < 3; ++d) p.pp.a[d] = R(h.adv[d]);
+  p.pp.c_h = R(h.c_h);
   for (int i = 0; i < NMAXT * NMAXT; ++i) {
     p.dsplit[i] = R(0);
     p.dhat[i] = R(0);
@@ -60,11 +61,12 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
     h.tile_out->def_wpg = K::WPG;
     h.tile_out->def_gpb = K::GPB;
     h.tile_out->group_smem = K::GROUP_SMEM;
+    h.tile_out->max_warps = K::MAX_WARPS;
     return cudaSuccess;
   }
   // tile: the requested one when valid, else the compile-time defaults
   int wpg = K::WPG, gpb = K::GPB;
-  if (h.wpg >= K::warps_for(K::EPG) && h.wpg <= 8 && h.gpb >= 1 && h.gpb <= 15 && h.gpb * h.wpg <= 16 &&
+  if (h.wpg >= K::warps_for(K::EPG) && h.wpg <= 8 && h.gpb >= 1 && h.gpb <= 15 && h.gpb * h.wpg <= K::MAX_WARPS &&
       (size_t)h.gpb * K::GROUP_SMEM <= 200 * 1024) {
     wpg = h.wpg;
     gpb = h.gpb;
@@ -75,7 +77,8 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   const int block = 32 * wpg * gpb;
   const size_t smem = (size_t)gpb * K::GROUP_SMEM;
   // opt in once per instantiation to the large dynamic shared-memory carve-out
-  static const cudaError_t attr = cudaFuncSetAttribute(dg_fused_kernel<DIM, N, EQ, R, VOL, VF, BND>,
+  constexpr auto kernel = fused_entry<DIM, N, EQ, R, VOL, VF, BND>();
+  static const cudaError_t attr = cudaFuncSetAttribute(kernel,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   if (attr != cudaSuccess) return attr;
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
@@ -94,10 +97,10 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, dg_fused_kernel<DIM, N, EQ, R, VOL, VF, BND>, p);
+    return cudaLaunchKernelEx(&cfg, kernel, p);
   }
   p.pdl = 0;
-  dg_fused_kernel<DIM, N, EQ, R, VOL, VF, BND><<<(unsigned)grid, block, smem, s>>>(p);
+  kernel<<<(unsigned)grid, block, smem, s>>>(p);
   return cudaGetLastError();
 }
 
@@ -119,6 +122,29 @@ cudaError_t launch_n(int eq, int vol, int vflux, const FusedHost &h, cudaStream_
     if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_CENTRAL, BND>(h, s);
   }
   return cudaErrorNotSupported;
+}
+
+// ideal GLM-MHD: flux differencing (flux_hindenlang_gassner or flux_central)
+// and shock capturing (flux_hindenlang_gassner), polydeg 1..4
+template <int DIM, int N, typename R>
+cudaError_t launch_n_mhd(int vol, int vflux, const FusedHost &h, cudaStream_t s) {
+  if (vol == VOL_FD) {
+    if (vflux == FLUX_HG) return launch_one<DIM, N, EQ_MHD, R, VOL_FD, FLUX_HG, 0>(h, s);
+    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_MHD, R, VOL_FD, FLUX_CENTRAL, 0>(h, s);
+  }
+  if (vol == VOL_SC && vflux == FLUX_HG) return launch_one<DIM, N, EQ_MHD, R, VOL_SC, FLUX_HG, 0>(h, s);
+  return cudaErrorNotSupported;
+}
+
+template <int DIM, typename R>
+cudaError_t launch_dim_mhd(int N, int vol, int vflux, const FusedHost &h, cudaStream_t s) {
+  switch (N) {
+    case 2: return launch_n_mhd<DIM, 2, R>(vol, vflux, h, s);
+    case 3: return launch_n_mhd<DIM, 3, R>(vol, vflux, h, s);
+    case 4: return launch_n_mhd<DIM, 4, R>(vol, vflux, h, s);
+    case 5: return launch_n_mhd<DIM, 5, R>(vol, vflux, h, s);
+    default: return cudaErrorNotSupported;
+  }
 }
 
 template <int DIM, typename R, int BND>

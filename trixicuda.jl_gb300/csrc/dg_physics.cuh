@@ -24,13 +24,14 @@ __host__ __device__ constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * i
 
 template <int DIM, int EQ>
 struct NVarsOf {
-  static constexpr int value = (EQ == EQ_ADV) ? 1 : DIM + 2;
+  static constexpr int value = (EQ == EQ_ADV) ? 1 : (EQ == EQ_MHD) ? (DIM == 1 ? 8 : 9) : DIM + 2;
 };
 
 template <typename R>
 struct PhysParams {
   R gamma, gm1, inv_gm1;  // gamma, gamma-1, 1/(gamma-1)
   R a[3];                 // advection velocity
+  R c_h;                  // GLM cleaning speed (ideal GLM-MHD)
 };
 
 // Precision-specific elementary operations.  FP64 keeps the library log and
@@ -255,13 +256,191 @@ struct Physics<DIM, EQ_EULER, R> {
   }
 };
 
+// Ideal GLM-MHD (IdealGlmMhdEquations{1,2,3}D).  Conservative variables
+// (rho, rho v1, rho v2, rho v3, E, B1, B2, B3[, psi]), primitive record
+// (rho, v1, v2, v3, p, B1, B2, B3[, psi]); three velocity and field
+// components in every dimension, psi (and the nonconservative terms) in 2D and
+// 3D only.  GLM formulation of Derigs, Winters, Gassner, Walch, Bohm, JCP 364
+// (2018): E = p/(gamma-1) + rho|v|^2/2 + |B|^2/2 + psi^2/2; the conservative
+// flux carries the cleaning terms c_h psi and c_h B_O; v . grad psi and the
+// Powell source are the nonconservative terms.
+template <int DIM, typename R>
+struct Physics<DIM, EQ_MHD, R> {
+  static constexpr int NV = (DIM == 1) ? 8 : 9;
+  static constexpr bool PSI = (DIM > 1);
+  __device__ __forceinline__ static void prim(const R *u, R *w, const PhysParams<R> &pp) {
+    const R rho = u[0];
+    const R inv_rho = dev_rcp(rho);
+    R kin = R(0), mag = R(0);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      w[1 + d] = u[1 + d] * inv_rho;
+      kin += u[1 + d] * w[1 + d];
+      mag += u[5 + d] * u[5 + d];
+      w[5 + d] = u[5 + d];
+    }
+    R e = u[4] - R(0.5) * kin - R(0.5) * mag;
+    if constexpr (PSI) {
+      e -= R(0.5) * u[8] * u[8];
+      w[8] = u[8];
+    }
+    w[0] = rho;
+    w[4] = pp.gm1 * e;
+  }
+  __device__ __forceinline__ static void cons_from_prim(const R *w, R *u, const PhysParams<R> &pp) {
+    R kin = R(0), mag = R(0);
+    u[0] = w[0];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      u[1 + d] = w[0] * w[1 + d];
+      kin += u[1 + d] * w[1 + d];
+      mag += w[5 + d] * w[5 + d];
+      u[5 + d] = w[5 + d];
+    }
+    R e = w[4] * pp.inv_gm1 + R(0.5) * kin + R(0.5) * mag;
+    if constexpr (PSI) {
+      e += R(0.5) * w[8] * w[8];
+      u[8] = w[8];
+    }
+    u[4] = e;
+  }
+  template <int O>
+  __device__ __forceinline__ static void flux(const R *u, const R *w, R *f, const PhysParams<R> &pp) {
+    const R p = w[4];
+    const R mag = R(0.5) * (w[5] * w[5] + w[6] * w[6] + w[7] * w[7]);
+    const R vB = w[1] * w[5] + w[2] * w[6] + w[3] * w[7];
+    const R kin = R(0.5) * (u[1] * w[1] + u[2] * w[2] + u[3] * w[3]);
+    const R BO = w[5 + O];
+    f[0] = u[1 + O];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) f[1 + d] = u[1 + O] * w[1 + d] - BO * w[5 + d] + (d == O ? p + mag : R(0));
+    R fe = (kin + pp.gamma * pp.inv_gm1 * p + R(2) * mag) * w[1 + O] - BO * vB;
+    if constexpr (PSI) fe += pp.c_h * w[8] * BO;
+    f[4] = fe;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (d == O) f[5 + d] = PSI ? pp.c_h * w[8] : R(0);
+      else f[5 + d] = w[1 + O] * w[5 + d] - w[1 + d] * BO;
+    }
+    if constexpr (PSI) f[8] = pp.c_h * BO;
+  }
+  // Hindenlang & Gassner (2019), "A new entropy conservative two-point flux
+  // for ideal MHD equations derived from first principles" (HONOM 2019):
+  // Ismail-Roe logarithmic means of rho and rho/p, arithmetic means of v, p,
+  // psi, product means of the magnetic terms; the energy flux follows from the
+  // entropy-conservation condition with the nonconservative Powell term.
+  template <int O>
+  __device__ __forceinline__ static void hindenlang_gassner(const R *, const R *wl, const R *, const R *wr, R *f,
+                                                            const PhysParams<R> &pp) {
+    const R rl = wl[0], rr = wr[0], pl = wl[4], pr = wr[4];
+    R rho_mean, inv_mean;
+    ranocha_means(rl, rr, rl * pr, rr * pl, rho_mean, inv_mean);
+    const R inv_rho_p_mean = pl * pr * inv_mean;
+    R vavg[3];
+    R v2avg = R(0), b2avg = R(0);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      vavg[d] = R(0.5) * (wl[1 + d] + wr[1 + d]);
+      v2avg += wl[1 + d] * wr[1 + d];
+      b2avg += wl[5 + d] * wr[5 + d];
+    }
+    v2avg *= R(0.5);
+    b2avg *= R(0.5);
+    const R pavg = R(0.5) * (pl + pr);
+    const R BOl = wl[5 + O], BOr = wr[5 + O];
+    const R f0 = rho_mean * vavg[O];
+    f[0] = f0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      f[1 + d] = f0 * vavg[d] + (d == O ? pavg + b2avg : R(0)) - R(0.5) * (BOl * wr[5 + d] + BOr * wl[5 + d]);
+    const R vOl = wl[1 + O], vOr = wr[1 + O];
+    R e = pl * vOr + pr * vOl;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (d == O) continue;
+      e += (vOl + vOr) * wl[5 + d] * wr[5 + d];
+      e -= wl[1 + d] * BOl * wr[5 + d] + wr[1 + d] * BOr * wl[5 + d];
+      f[5 + d] = R(0.5) * (vOl * wl[5 + d] - wl[1 + d] * BOl + vOr * wr[5 + d] - wr[1 + d] * BOr);
+    }
+    if constexpr (PSI) {
+      e += pp.c_h * (BOl * wr[8] + BOr * wl[8]);
+      f[5 + O] = pp.c_h * R(0.5) * (wl[8] + wr[8]);
+      f[8] = pp.c_h * R(0.5) * (BOl + BOr);
+    } else {
+      f[5 + O] = R(0);
+    }
+    f[4] = f0 * (v2avg + inv_rho_p_mean * pp.inv_gm1) + R(0.5) * e;
+  }
+  template <int O>
+  __device__ __forceinline__ static void ec(const R *ul, const R *wl, const R *ur, const R *wr, R *f,
+                                            const PhysParams<R> &pp) {
+    hindenlang_gassner<O>(ul, wl, ur, wr, f, pp);
+  }
+  template <int O>
+  __device__ __forceinline__ static void central(const R *ul, const R *wl, const R *ur, const R *wr, R *f,
+                                                 const PhysParams<R> &pp) {
+    R fl[NV], fr[NV];
+    flux<O>(ul, wl, fl, pp);
+    flux<O>(ur, wr, fr, pp);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) f[v] = R(0.5) * (fl[v] + fr[v]);
+  }
+  // fast magnetosonic speed along O:
+  // c_f^2 = (a^2 + b^2)/2 + sqrt((a^2 + b^2)^2 - 4 a^2 b_O^2)/2, a^2 = gamma p/rho, b = B/sqrt(rho)
+  template <int O>
+  __device__ __forceinline__ static R fast_speed(const R *w, const PhysParams<R> &pp) {
+    const R inv_rho = dev_rcp(w[0]);
+    const R a2 = pp.gamma * w[4] * inv_rho;
+    const R b2 = (w[5] * w[5] + w[6] * w[6] + w[7] * w[7]) * inv_rho;
+    const R bo2 = w[5 + O] * w[5 + O] * inv_rho;
+    const R s = a2 + b2;
+    return dev_sqrt(R(0.5) * (s + dev_sqrt(s * s - R(4) * a2 * bo2)));
+  }
+  template <int O>
+  __device__ __forceinline__ static R max_speed(const R *, const R *wl, const R *, const R *wr, bool naive,
+                                                const PhysParams<R> &pp) {
+    const R cl = fast_speed<O>(wl, pp), cr = fast_speed<O>(wr, pp);
+    if (naive) return dev_fmax(dev_fabs(wl[1 + O]), dev_fabs(wr[1 + O])) + dev_fmax(cl, cr);
+    return dev_fmax(dev_fabs(wl[1 + O]) + cl, dev_fabs(wr[1 + O]) + cr);
+  }
+  // f += s * Phi_O(u_own, u_other): the Powell term phi_P(own) B_O(other) and
+  // the GLM transport term v_O(own) phi_GLM(own) psi(other), phi_P = (0, B,
+  // v.B, v, 0), phi_GLM = (0, 0, 0, 0, psi, 0, 0, 0, 1) (Derigs et al. 2018;
+  // Bohm et al., JCP 422 (2020)).  2D/3D only.
+  template <int O>
+  __device__ __forceinline__ static void add_noncons(const R *wown, const R *wother, R s, R *f) {
+    if constexpr (PSI) {
+      const R b = s * wother[5 + O], q = s * wother[8];
+      const R vB = wown[1] * wown[5] + wown[2] * wown[6] + wown[3] * wown[7];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        f[1 + d] += wown[5 + d] * b;
+        f[5 + d] += wown[1 + d] * b;
+      }
+      f[4] += vB * b + wown[1 + O] * wown[8] * q;
+      f[8] += wown[1 + O] * q;
+    }
+  }
+};
+
+// The entropy-conservative two-point flux of each system: flux_ranocha for
+// Euler, the central flux for linear advection, flux_hindenlang_gassner for
+// ideal GLM-MHD (the same kernel path serves FLUX_RANOCHA and FLUX_HG).
+template <int DIM, int EQ, typename R, int O>
+__device__ __forceinline__ void ec_flux(const R *ul, const R *wl, const R *ur, const R *wr, R *f,
+                                        const PhysParams<R> &pp) {
+  using P = Physics<DIM, EQ, R>;
+  if constexpr (EQ == EQ_MHD) P::template ec<O>(ul, wl, ur, wr, f, pp);
+  else P::template ranocha<O>(ul, wl, ur, wr, f, pp);
+}
+
 // Two-point flux dispatch (kind is warp-uniform).
 template <int DIM, int EQ, typename R, int O>
 __device__ __forceinline__ void two_point_flux(int kind, const R *ul, const R *wl, const R *ur, const R *wr, R *f,
                                                const PhysParams<R> &pp) {
   using P = Physics<DIM, EQ, R>;
-  if (kind == FLUX_RANOCHA) {
-    P::template ranocha<O>(ul, wl, ur, wr, f, pp);
+  if (kind == FLUX_RANOCHA || kind == FLUX_HG) {
+    ec_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
   } else if (kind == FLUX_CENTRAL) {
     P::template central<O>(ul, wl, ur, wr, f, pp);
   } else {
@@ -277,8 +456,8 @@ template <int DIM, int EQ, typename R, int O, int KIND>
 __device__ __forceinline__ void two_point_flux_t(const R *ul, const R *wl, const R *ur, const R *wr, R *f,
                                                  const PhysParams<R> &pp) {
   using P = Physics<DIM, EQ, R>;
-  if constexpr (KIND == FLUX_RANOCHA) {
-    P::template ranocha<O>(ul, wl, ur, wr, f, pp);
+  if constexpr (KIND == FLUX_RANOCHA || KIND == FLUX_HG) {
+    ec_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
   } else if constexpr (KIND == FLUX_CENTRAL) {
     P::template central<O>(ul, wl, ur, wr, f, pp);
   } else {

@@ -74,6 +74,7 @@ struct trixi_handle {
   int eq = 0, vol = 0, vflux = 0, sflux = 0, fvflux = 0;
   bool mixed = false;
   double gamma = 1.4, adv[3] = {0, 0, 0};
+  double c_h = 0.0;  // GLM cleaning speed (ideal GLM-MHD)
   double alpha_max = 0.5, alpha_min = 0.001;
   int alpha_smooth = 1;
   int64_t E = 0, I = 0, M = 0, B = 0;
@@ -219,15 +220,36 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   if (d->ndims < 1 || d->ndims > 3) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "ndims %d", d->ndims);
   if (d->polydeg < 1 || d->polydeg + 1 > HOST_NMAX)
     return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "polydeg %d (supported 1..%d)", d->polydeg, HOST_NMAX - 1);
-  if (d->equation != TRIXI_EQ_LINEAR_ADVECTION && d->equation != TRIXI_EQ_COMPRESSIBLE_EULER)
+  if (d->equation != TRIXI_EQ_LINEAR_ADVECTION && d->equation != TRIXI_EQ_COMPRESSIBLE_EULER &&
+      d->equation != TRIXI_EQ_IDEAL_GLM_MHD)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "equation %d", d->equation);
-  const int nv_expect = d->equation == TRIXI_EQ_LINEAR_ADVECTION ? 1 : d->ndims + 2;
+  const bool mhd = d->equation == TRIXI_EQ_IDEAL_GLM_MHD;
+  const int nv_expect = d->equation == TRIXI_EQ_LINEAR_ADVECTION ? 1 : mhd ? (d->ndims == 1 ? 8 : 9) : d->ndims + 2;
   if (d->nvars != nv_expect)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "nvars %d, equation needs %d", d->nvars, nv_expect);
   if (d->volume_integral < 0 || d->volume_integral > 2)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "volume_integral %d", d->volume_integral);
   for (int f : {d->volume_flux, d->surface_flux, d->volume_flux_fv})
-    if (f < 0 || f > 3) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux enum %d", f);
+    if (f < 0 || f > 4) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux enum %d", f);
+  for (int f : {d->volume_flux, d->surface_flux, d->volume_flux_fv}) {
+    // flux_hindenlang_gassner is the MHD flux, flux_ranocha the Euler one
+    if (f == TRIXI_FLUX_HINDENLANG_GASSNER && !mhd)
+      return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux_hindenlang_gassner needs ideal GLM-MHD");
+    if (f == TRIXI_FLUX_RANOCHA && mhd)
+      return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux_ranocha is not defined for ideal GLM-MHD");
+  }
+  {
+    // ideal GLM-MHD in 2D/3D pairs every flux with flux_nonconservative_powell
+    // (have_nonconservative_terms); every other system takes plain fluxes
+    const int need = (mhd && d->ndims > 1) ? TRIXI_NONCONSERVATIVE_POWELL : TRIXI_NONCONSERVATIVE_NONE;
+    if (d->nonconservative_flux != need)
+      return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "nonconservative_flux %d, the equations need %d",
+                  d->nonconservative_flux, need);
+  }
+  if (mhd && (d->nboundaries > 0 || d->source_terms != TRIXI_SOURCE_NONE))
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: periodic meshes without source terms");
+  if (mhd && d->volume_integral == TRIXI_VOLUME_WEAK_FORM)
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: flux differencing or shock capturing");
   if (d->precision != TRIXI_PRECISION_FP64 && d->precision != TRIXI_PRECISION_MIXED)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "precision %d", d->precision);
   if (d->nelements <= 0 || d->nelements > INT32_MAX)
@@ -254,7 +276,7 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   if (d->nmortars < 0 || (d->nmortars > 0 && (!d->mortar_neighbor_ids || !d->mortar_large_sides || !d->mortar_orientations)))
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "mortar tables");
   if (d->nmortars > 0 && d->ndims == 1) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "mortars in 1D");
-  if (d->equation == TRIXI_EQ_COMPRESSIBLE_EULER && !(d->gamma > 1.0))
+  if (d->equation != TRIXI_EQ_LINEAR_ADVECTION && !(d->gamma > 1.0))
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "gamma %g", d->gamma);
 
   trixi_handle *h = new trixi_handle();
@@ -264,7 +286,8 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   h->NF = (int)ipow64(h->N, h->dim - 1);
   h->NN = h->NF * h->N;
   h->nchild = 1 << (h->dim - 1);
-  h->eq = d->equation == TRIXI_EQ_LINEAR_ADVECTION ? EQ_ADV : EQ_EULER;
+  h->eq = d->equation == TRIXI_EQ_LINEAR_ADVECTION ? EQ_ADV : mhd ? EQ_MHD : EQ_EULER;
+  h->c_h = d->glm_speed;
   h->vol = d->volume_integral;
   h->vflux = d->volume_flux;
   h->sflux = d->surface_flux;
@@ -428,6 +451,7 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   f.atol = std::max(100 * eps, std::pow(eps, 0.75));  // src/solvers/dg_2d.jl:173
   f.gamma = h->gamma;
   for (int i = 0; i < 3; ++i) f.adv[i] = h->adv[i];
+  f.c_h = h->c_h;
   f.N = h->N;
   to_row_major(h->basis.dsplit, h->N, f.dsplit);
   for (int i = 0; i < h->N; ++i) f.dsplit[i * h->N + i] = 0.0;  // zeroed diagonal (dg_2d_kernel.jl:189-190)
@@ -476,6 +500,7 @@ void fill_mortar(const trixi_handle *h, MortarHost &mh, const double *u) {
   mh.surface_flux = h->sflux;
   mh.mixed = h->mixed;
   mh.gamma = h->gamma;
+  mh.c_h = h->c_h;
   for (int i = 0; i < 3; ++i) mh.adv[i] = h->adv[i];
   to_row_major(h->basis.fwd_up, h->N, mh.fwd_up);
   to_row_major(h->basis.fwd_lo, h->N, mh.fwd_lo);
@@ -489,6 +514,7 @@ int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStrea
   ih.dim = h->dim;
   ih.N = h->N;
   ih.nv = h->nv;
+  ih.eq = h->eq;
   ih.nelements = h->E;
   ih.u = u;
   ih.alpha_raw = h->d_alpha_raw;
@@ -553,7 +579,7 @@ int tune_tiles(trixi_handle *h, const double *u, cudaStream_t s) {
   std::vector<Cand> cand;
   for (int w = t.min_wpg; w <= 8; ++w)
     for (int g : {1, 2, 4, 8})
-      if (g * w <= 16 && (size_t)g * t.group_smem <= 200 * 1024) cand.push_back({w, g});
+      if (g * w <= t.max_warps && (size_t)g * t.group_smem <= 200 * 1024) cand.push_back({w, g});
   const size_t bytes = sizeof(double) * (size_t)(h->E * h->NN * h->nv);
   double *out = nullptr, *k = nullptr;
   TRIXI_CUDA(h, cudaMalloc(&out, bytes), "tuner buffers");
@@ -628,6 +654,7 @@ StageHost stage_of(trixi_handle *h) {
   for (int c = 0; c < 4; ++c) sh.mortar_u[c] = h->d_mortar_u[c];
   sh.surface_flux = h->sflux;
   sh.gamma = h->gamma;
+  sh.c_h = h->c_h;
   for (int i = 0; i < 3; ++i) sh.adv[i] = h->adv[i];
   to_row_major(h->basis.fwd_up, h->N, sh.fwd_up);
   to_row_major(h->basis.fwd_lo, h->N, sh.fwd_lo);
@@ -841,7 +868,7 @@ int trixi_container(trixi_handle *h, int which, void **dev_ptr, int64_t *count) 
 
 int trixi_indicator(trixi_handle *h, const double *u, double *alpha, void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
-  if (h->eq != EQ_EULER) return fail(h, TRIXI_ERR_UNSUPPORTED, "indicator on density_pressure needs Euler");
+  if (h->eq == EQ_ADV) return fail(h, TRIXI_ERR_UNSUPPORTED, "indicator on density_pressure needs Euler or MHD");
   if (int st = check_u_args(h, u, "u")) return st;
   if (int st = check_u_args(h, alpha, "alpha")) return st;
   if (!h->d_alpha_raw) {
@@ -899,12 +926,21 @@ int trixi_set_tile(trixi_handle *h, int wpg, int gpb) {
   }
   FusedTile t;
   if (int st = fused_tile(h, t)) return st;
-  if (wpg < t.min_wpg || wpg > 8 || gpb < 1 || gpb > 15 || gpb * wpg > 16 || (size_t)gpb * t.group_smem > 200 * 1024)
+  if (wpg < t.min_wpg || wpg > 8 || gpb < 1 || gpb > 15 || gpb * wpg > t.max_warps ||
+      (size_t)gpb * t.group_smem > 200 * 1024)
     return fail(h, TRIXI_ERR_INVALID_ARGUMENT,
-                "tile (%d warps per group, %d groups per block) outside [%d..8] warps, <= 16 warps per block", wpg,
-                gpb, t.min_wpg);
+                "tile (%d warps per group, %d groups per block) outside [%d..8] warps, <= %d warps per block", wpg,
+                gpb, t.min_wpg, t.max_warps);
   h->fused.wpg = wpg;
   h->fused.gpb = gpb;
+  return TRIXI_OK;
+}
+
+int trixi_set_glm_speed(trixi_handle *h, double c_h) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (h->eq != EQ_MHD) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "the GLM speed belongs to ideal GLM-MHD");
+  h->c_h = c_h;
+  h->fused.c_h = c_h;
   return TRIXI_OK;
 }
 
@@ -983,6 +1019,7 @@ extern "C" {
 int trixi_compute_coefficients(trixi_handle *h, int ic_kind, const double *params, int64_t nparams, double t,
                                double *u, void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: not available in this function");
   if (int st = check_u_args(h, u, "u")) return st;
   if (int st = check_ic(h, ic_kind, nparams, params)) return st;
   if (!h->d_coords) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "desc.node_coordinates was not given");
@@ -1002,6 +1039,7 @@ int trixi_compute_coefficients(trixi_handle *h, int ic_kind, const double *param
 
 int trixi_max_dt(trixi_handle *h, const double *u, double *dt_dev, void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: not available in this function");
   if (int st = check_u_args(h, u, "u")) return st;
   if (int st = check_u_args(h, dt_dev, "dt")) return st;
   if (int st = ensure_reduction(h, 1)) return st;
@@ -1023,6 +1061,7 @@ int trixi_max_dt(trixi_handle *h, const double *u, double *dt_dev, void *stream)
 int trixi_integrate(trixi_handle *h, const double *u, const double *du, int which, double *out_host, int64_t count,
                     void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: not available in this function");
   if (int st = check_u_args(h, u, "u")) return st;
   if (which < 0 || which > 3) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "integral kind %d", which);
   if ((which == 2 || which == 3) && !aligned8(du)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "du is required");
@@ -1053,6 +1092,7 @@ int trixi_integrate(trixi_handle *h, const double *u, const double *du, int whic
 int trixi_calc_error_norms(trixi_handle *h, const double *u, const double *u_ref, int ic_kind, const double *params,
                            int64_t nparams, double t, double *l2_host, double *linf_host, void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: not available in this function");
   if (int st = check_u_args(h, u, "u")) return st;
   if (!l2_host || !linf_host) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "null output");
   if (!u_ref) {
@@ -1382,6 +1422,10 @@ int trixi_batch_create(const trixi_problem_desc *const *descs, int64_t n, trixi_
       delete b;
       return batch_fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "batch: instance " + std::to_string(i) + " descriptor");
     }
+    if (d->equation == TRIXI_EQ_IDEAL_GLM_MHD) {
+      delete b;
+      return batch_fail(nullptr, TRIXI_ERR_UNSUPPORTED, "batch: ideal GLM-MHD instances are not batched");
+    }
     const KindKey k = key_of(d);
     size_t gi = 0;
     while (gi < keys.size() && !(keys[gi] == k)) ++gi;
@@ -1642,6 +1686,7 @@ AdjointHost adjoint_host(const trixi_handle *h) {
 }
 
 int check_adjoint_supported(trixi_handle *h) {
+  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "adjoint: ideal GLM-MHD is not differentiated");
   if (h->mixed) return fail(h, TRIXI_ERR_UNSUPPORTED, "the adjoint runs in FP64 (precision = FP64)");
   if (h->B > 0 || h->src_kind != 0)
     return fail(h, TRIXI_ERR_UNSUPPORTED, "adjoint: periodic meshes without source terms only");

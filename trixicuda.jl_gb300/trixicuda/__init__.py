@@ -12,13 +12,18 @@ from .equations import (
     CompressibleEulerEquations1D,
     CompressibleEulerEquations2D,
     CompressibleEulerEquations3D,
+    IdealGlmMhdEquations1D,
+    IdealGlmMhdEquations2D,
+    IdealGlmMhdEquations3D,
     LinearScalarAdvectionEquation1D,
     LinearScalarAdvectionEquation2D,
     LinearScalarAdvectionEquation3D,
     flux,
     flux_central,
+    flux_hindenlang_gassner,
     flux_lax_friedrichs,
     flux_lax_friedrichs_naive,
+    flux_nonconservative_powell,
     flux_ranocha,
     initial_condition_constant,
     initial_condition_convergence_test,
@@ -35,6 +40,7 @@ from .semidiscretization import (
     SemidiscretizationHyperbolicGPU,
     autotune,
     set_tile,
+    set_glm_speed,
     calc_error_norms,
     compute_coefficients_gpu,
     integrate,

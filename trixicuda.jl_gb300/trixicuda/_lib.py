@@ -24,9 +24,11 @@ STATUS_NAMES = {
     7: "TRIXI_ERR_BAD_CONNECTIVITY",
 }
 
-EQ_LINEAR_ADVECTION, EQ_COMPRESSIBLE_EULER = 0, 1
+EQ_LINEAR_ADVECTION, EQ_COMPRESSIBLE_EULER, EQ_IDEAL_GLM_MHD = 0, 1, 2
 VOLUME_WEAK_FORM, VOLUME_FLUX_DIFFERENCING, VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
 FLUX_LAX_FRIEDRICHS, FLUX_RANOCHA, FLUX_CENTRAL, FLUX_LAX_FRIEDRICHS_NAIVE = 0, 1, 2, 3
+FLUX_HINDENLANG_GASSNER = 4
+NONCONSERVATIVE_NONE, NONCONSERVATIVE_POWELL = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 IC_CONSTANT, IC_CONVERGENCE_TEST, IC_WEAK_BLAST_WAVE = 0, 1, 2
@@ -100,6 +102,9 @@ class ProblemDesc(C.Structure):
         ("nsource_params", C.c_int32),
         ("boundary_params", C.c_double * 8),
         ("source_params", C.c_double * 3),
+        ("nonconservative_flux", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("glm_speed", C.c_double),
     ]
 
 
@@ -155,6 +160,7 @@ SIGNATURES = {
     "trixi_calc_error_norms": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _D,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double), _VP]),
     "trixi_probe_convert": (C.c_int, [_VP, _VP, _VP, _VP, _I64, _VP]),
+    "trixi_set_glm_speed": (C.c_int, [_VP, _D]),
 }
 
 _lib = None

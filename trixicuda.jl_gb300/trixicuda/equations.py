@@ -31,6 +31,31 @@ flux_ranocha = NumericalFlux("flux_ranocha", _lib.FLUX_RANOCHA)
 flux_central = NumericalFlux("flux_central", _lib.FLUX_CENTRAL)
 flux_lax_friedrichs_naive = NumericalFlux("flux_lax_friedrichs_naive", _lib.FLUX_LAX_FRIEDRICHS_NAIVE)
 flux = NumericalFlux("flux", -1)  # physical flux (weak form)
+flux_hindenlang_gassner = NumericalFlux("flux_hindenlang_gassner", _lib.FLUX_HINDENLANG_GASSNER)
+
+
+@dataclass(frozen=True)
+class NonconservativeFlux:
+    """The nonconservative half of a `(flux, nonconservative_flux)` pair, as
+    Trixi's equations with nonconservative terms take them."""
+    name: str
+    code: int
+
+    def __repr__(self) -> str:
+        return self.name
+
+
+flux_nonconservative_powell = NonconservativeFlux("flux_nonconservative_powell", _lib.NONCONSERVATIVE_POWELL)
+
+
+def split_flux(f):
+    """(symmetric flux, nonconservative flux or None) of a flux or a
+    `(flux, nonconservative_flux)` tuple."""
+    if isinstance(f, tuple):
+        if len(f) != 2 or not isinstance(f[0], NumericalFlux) or not isinstance(f[1], NonconservativeFlux):
+            raise ValueError(f"expected (flux, nonconservative_flux), got {f!r}")
+        return f[0], f[1]
+    return f, None
 
 
 # --- equations ------------------------------------------------------------------
@@ -110,6 +135,67 @@ class CompressibleEulerEquations3D(_CompressibleEuler):
     ndims = 3
 
 
+class _IdealGlmMhd(AbstractEquations):
+    """Ideal GLM-MHD (Trixi's IdealGlmMhdEquations{1,2,3}D): conservative
+    variables (rho, rho v1, rho v2, rho v3, E, B1, B2, B3[, psi]) -- three
+    velocity and field components in every dimension, the divergence-cleaning
+    field psi in 2D and 3D, which have the nonconservative Powell terms.
+    `c_h` is the GLM cleaning speed (a GlmSpeedCallback sets it during a run);
+    it starts as NaN, as Trixi's `initial_c_h` default does."""
+    code = _lib.EQ_IDEAL_GLM_MHD
+
+    def __init__(self, gamma: float = 1.4, initial_c_h: float = float("nan")):
+        self.gamma = float(gamma)
+        self.c_h = float(initial_c_h)
+        self.nvariables = 8 if self.ndims == 1 else 9
+        self.advection_velocity = np.zeros(self.ndims)
+
+    @property
+    def have_nonconservative_terms(self) -> bool:
+        return self.ndims > 1
+
+    def __repr__(self):
+        return f"IdealGlmMhdEquations{self.ndims}D({self.gamma}, c_h={self.c_h})"
+
+    def prim2cons(self, rho, v, p, B=None, psi=None):
+        """rho (n,), v (3, n), p (n,), B (3, n), psi (n,) -> u (nvars, n)."""
+        rho = np.asarray(rho, dtype=np.float64)
+        n = rho.shape
+        v = np.asarray(v, dtype=np.float64).reshape((3,) + n)
+        B = np.zeros((3,) + n) if B is None else np.asarray(B, dtype=np.float64).reshape((3,) + n)
+        psi = np.zeros(n) if psi is None else np.asarray(psi, dtype=np.float64).reshape(n)
+        u = np.empty((self.nvariables,) + n)
+        u[0] = rho
+        u[1:4] = rho * v
+        u[4] = (p / (self.gamma - 1) + 0.5 * rho * np.sum(v * v, axis=0) + 0.5 * np.sum(B * B, axis=0))
+        u[5:8] = B
+        if self.nvariables == 9:
+            u[4] += 0.5 * psi * psi
+            u[8] = psi
+        return u
+
+    def cons2prim(self, u):
+        """(rho, v (3, n), p): p = (gamma-1)(E - rho|v|^2/2 - |B|^2/2 - psi^2/2)."""
+        rho = u[0]
+        v = u[1:4] / rho
+        psi2 = u[8] * u[8] if self.nvariables == 9 else 0.0
+        p = (self.gamma - 1) * (u[4] - 0.5 * np.sum(u[1:4] * v, axis=0) - 0.5 * np.sum(u[5:8] * u[5:8], axis=0)
+                                - 0.5 * psi2)
+        return rho, v, p
+
+
+class IdealGlmMhdEquations1D(_IdealGlmMhd):
+    ndims = 1
+
+
+class IdealGlmMhdEquations2D(_IdealGlmMhd):
+    ndims = 2
+
+
+class IdealGlmMhdEquations3D(_IdealGlmMhd):
+    ndims = 3
+
+
 # --- initial conditions (x: (ndims, n) array) -----------------------------------
 def initial_condition_convergence_test(x, t, equations):
     """Advection: c + A sin(omega (sum(x) - t*sum(a)))... per dimension as in
@@ -121,6 +207,8 @@ def initial_condition_convergence_test(x, t, equations):
         omega = 2 * np.pi / L
         xt = x - equations.advection_velocity[:, None] * t
         return (c + A * np.sin(omega * np.sum(xt, axis=0)))[None, :]
+    if isinstance(equations, _IdealGlmMhd):
+        return _mhd_alfven_wave(x, t, equations)
     # Euler manufactured solution (source terms are not part of the hot path)
     c, A, L = 2.0, 0.1, 2.0
     omega = 2 * np.pi / L
@@ -135,11 +223,46 @@ def initial_condition_convergence_test(x, t, equations):
     return u
 
 
+def _mhd_alfven_wave(x, t, eq):
+    """Smooth circularly polarised Alfven waves, the convergence tests of
+    ideal MHD.  1D and 2D: Derigs et al., "A novel high-order,
+    entropy stable, 3D AMR MHD solver with guaranteed positive pressure",
+    JCP 317 (2016) -- rho = 1, p = 0.1, unit background field along the
+    propagation direction (the x axis in 1D; alpha = pi/4 in 2D on
+    [0, sqrt 2]^2), perturbation amplitude 0.1, speed 1 (gamma = 5/3).
+    3D: Altmann's thesis (2012) set-up on [-1, 1]^3 -- propagation along
+    (1, 0, 2)/sqrt 5, amplitude 0.2, wave number 2 pi / 2 on the box."""
+    n = x.shape[1]
+    if eq.ndims == 1:
+        arg = 2 * np.pi * (x[0] + t)
+        v = np.stack([np.zeros(n), 0.1 * np.sin(arg), 0.1 * np.cos(arg)])
+        B = np.stack([np.ones(n), v[1], v[2]])
+        return eq.prim2cons(np.ones(n), v, np.full(n, 0.1), B)
+    if eq.ndims == 2:
+        alpha = 0.25 * np.pi
+        x_perp = x[0] * np.cos(alpha) + x[1] * np.sin(alpha)
+        b_perp = 0.1 * np.sin(2 * np.pi * (x_perp + t))
+        v = np.stack([-b_perp * np.sin(alpha), b_perp * np.cos(alpha), 0.1 * np.cos(2 * np.pi * (x_perp + t))])
+        B = np.stack([np.cos(alpha) + v[0], np.sin(alpha) + v[1], v[2]])
+        return eq.prim2cons(np.ones(n), v, np.full(n, 0.1), B, np.zeros(n))
+    omega, r, e = 2 * np.pi, 2.0, 0.2
+    nx, ny = 1 / np.sqrt(r * r + 1), r / np.sqrt(r * r + 1)
+    va = omega / ny
+    ph = omega / ny * (nx * (x[0] - 0.5 * r) + ny * (x[2] - 0.5 * r)) - va * t
+    v = np.stack([-e * ny * np.cos(ph), e * np.sin(ph), e * nx * np.cos(ph)])
+    B = np.stack([nx - v[0], -v[1], ny - v[2]])
+    return eq.prim2cons(np.ones(n), v, np.ones(n), B, np.zeros(n))
+
+
 def initial_condition_constant(x, t, equations, rho=1.0, v=None, p=1.0):
     x = np.atleast_2d(x)
     n = x.shape[1]
     if isinstance(equations, _LinearScalarAdvection):
         return np.full((1, n), 1.0)
+    if isinstance(equations, _IdealGlmMhd):
+        v = np.zeros(3) if v is None else np.resize(np.asarray(v, dtype=np.float64), 3)
+        return equations.prim2cons(np.full(n, rho), np.repeat(v[:, None], n, axis=1), np.full(n, p),
+                                   np.ones((3, n)), np.zeros(n))
     v = np.zeros(equations.ndims) if v is None else np.asarray(v, dtype=np.float64)
     return equations.prim2cons(np.full(n, rho), np.repeat(v[:, None], n, axis=1), np.full(n, p))
 
@@ -165,6 +288,11 @@ def initial_condition_weak_blast_wave(x, t, equations):
         v[0] = np.where(r > 0.5, 0.0, 0.1882 * np.cos(phi) * np.sin(theta))
         v[1] = np.where(r > 0.5, 0.0, 0.1882 * np.sin(phi) * np.sin(theta))
         v[2] = np.where(r > 0.5, 0.0, 0.1882 * np.cos(theta))
+    if isinstance(equations, _IdealGlmMhd):
+        # the MHD variant: the same jump, in a uniform field B = (1, 1, 1)
+        v3 = np.zeros((3,) + r.shape)
+        v3[:d] = v
+        return equations.prim2cons(rho, v3, p, np.ones((3,) + r.shape), np.zeros(r.shape))
     return equations.prim2cons(rho, v, p)
 
 

@@ -72,6 +72,34 @@ def _boundary_spec(boundary_conditions, cont, equations):
     return code, params
 
 
+def flux_codes(solver: DGSEMGPU, equations: AbstractEquations) -> dict:
+    """Enum codes of the solver's fluxes.  Equations with nonconservative
+    terms (ideal GLM-MHD in 2D/3D) take every flux as a `(flux,
+    nonconservative_flux)` pair with one common nonconservative flux, as
+    Trixi's do; the others take plain fluxes."""
+    from .equations import split_flux
+
+    vi = solver.volume_integral
+    pairs = {"surface_flux": solver.surface_flux}
+    if isinstance(vi, VolumeIntegralFluxDifferencing):
+        pairs["volume_flux"] = vi.volume_flux
+    if isinstance(vi, VolumeIntegralShockCapturingHG):
+        pairs["volume_flux"] = vi.volume_flux_dg
+        pairs["volume_flux_fv"] = vi.volume_flux_fv
+    out = {"volume_flux": _lib.FLUX_CENTRAL, "volume_flux_fv": _lib.FLUX_LAX_FRIEDRICHS}
+    nc = set()
+    for k, f in pairs.items():
+        sym, ncf = split_flux(f)
+        out[k] = sym.code
+        nc.add(ncf.code if ncf is not None else _lib.NONCONSERVATIVE_NONE)
+    need = bool(getattr(equations, "have_nonconservative_terms", False))
+    if len(nc) != 1 or (need and _lib.NONCONSERVATIVE_NONE in nc) or (not need and nc != {_lib.NONCONSERVATIVE_NONE}):
+        raise ValueError(f"{equations!r} takes {'(flux, nonconservative_flux) pairs' if need else 'plain fluxes'} "
+                         "for every volume and surface flux")
+    out["nonconservative_flux"] = nc.pop()
+    return out
+
+
 def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver: DGSEMGPU,
                        precision: str = "fp64", boundary_conditions="periodic", source_terms=None):
     """trixi_problem_desc for a mesh (or prebuilt containers).  Returns the
@@ -88,18 +116,15 @@ def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver:
     d.equation = equations.code
     vi = solver.volume_integral
     d.volume_integral = vi.code
-    d.volume_flux = _lib.FLUX_CENTRAL
-    d.volume_flux_fv = _lib.FLUX_LAX_FRIEDRICHS
+    codes = flux_codes(solver, equations)
+    d.volume_flux, d.surface_flux, d.volume_flux_fv = codes["volume_flux"], codes["surface_flux"], codes["volume_flux_fv"]
+    d.nonconservative_flux = codes["nonconservative_flux"]
+    d.glm_speed = float(getattr(equations, "c_h", 0.0))
     d.alpha_max, d.alpha_min, d.alpha_smooth = 0.5, 0.001, 1
-    if isinstance(vi, VolumeIntegralFluxDifferencing):
-        d.volume_flux = vi.volume_flux.code
     if isinstance(vi, VolumeIntegralShockCapturingHG):
-        d.volume_flux = vi.volume_flux_dg.code
-        d.volume_flux_fv = vi.volume_flux_fv.code
         d.alpha_max = vi.indicator.alpha_max
         d.alpha_min = vi.indicator.alpha_min
         d.alpha_smooth = int(bool(vi.indicator.alpha_smooth))
-    d.surface_flux = solver.surface_flux.code
     if precision not in ("fp64", "mixed"):
         raise ValueError("precision must be 'fp64' or 'mixed'")
     d.precision = _lib.PRECISION_MIXED if precision == "mixed" else _lib.PRECISION_FP64
@@ -245,6 +270,14 @@ class SemidiscretizationHyperbolicGPU:
             return torch.empty(0, dtype=torch.float64, device=self.device)
         # wrap the device pointer through a DLPack-free route: cupy-less torch view
         return _device_view(ptr.value, cnt.value, self.device)
+
+
+def set_glm_speed(semi, c_h: float) -> None:
+    """Set the GLM cleaning speed c_h of an ideal GLM-MHD semidiscretization
+    (what Trixi's GlmSpeedCallback does to `equations.c_h` between steps)."""
+    c_h = float(c_h)
+    _lib.check(semi._lib.trixi_set_glm_speed(semi._handle, c_h), semi._handle)
+    semi.equations.c_h = c_h
 
 
 def _device_view(ptr: int, count: int, device):
