@@ -19,12 +19,16 @@ const libtrixi = get(ENV, "TRIXI_B200_LIB", joinpath(@__DIR__, "..", "_build", "
 # enum values of include/trixi_b200.h
 const EQ_LINEAR_ADVECTION = Int32(0)
 const EQ_COMPRESSIBLE_EULER = Int32(1)
+const EQ_IDEAL_GLM_MHD = Int32(2)
 const VOLUME_WEAK_FORM = Int32(0)
 const VOLUME_FLUX_DIFFERENCING = Int32(1)
 const VOLUME_SHOCK_CAPTURING_HG = Int32(2)
 const FLUX_LAX_FRIEDRICHS = Int32(0)
 const FLUX_RANOCHA = Int32(1)
 const FLUX_CENTRAL = Int32(2)
+const FLUX_HINDENLANG_GASSNER = Int32(4)
+const NONCONSERVATIVE_NONE = Int32(0)
+const NONCONSERVATIVE_POWELL = Int32(1)
 
 # mirror of trixi_problem_desc (field order and types must match the C struct)
 mutable struct ProblemDesc
@@ -73,11 +77,19 @@ mutable struct ProblemDesc
     nsource_params::Int32
     boundary_params::NTuple{8, Float64}
     source_params::NTuple{3, Float64}
+    nonconservative_flux::Int32
+    reserved0::Int32
+    glm_speed::Float64
 end
 
 flux_code(::typeof(Trixi.flux_ranocha)) = FLUX_RANOCHA
 flux_code(::typeof(Trixi.flux_central)) = FLUX_CENTRAL
 flux_code(::Trixi.FluxLaxFriedrichs) = FLUX_LAX_FRIEDRICHS
+flux_code(::typeof(Trixi.flux_hindenlang_gassner)) = FLUX_HINDENLANG_GASSNER
+# equations with nonconservative terms pass (flux, nonconservative_flux) tuples
+flux_code(f::Tuple) = flux_code(first(f))
+noncons_code(::Any) = NONCONSERVATIVE_NONE
+noncons_code(f::Tuple) = last(f) === Trixi.flux_nonconservative_powell ? NONCONSERVATIVE_POWELL : Int32(-1)
 
 function check(status)
     status == 0 && return nothing
@@ -106,9 +118,14 @@ function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
         vol, vflux, fvflux = VOLUME_SHOCK_CAPTURING_HG, flux_code(vi.volume_flux_dg), flux_code(vi.volume_flux_fv)
         amax, amin, asmooth = vi.indicator.alpha_max, vi.indicator.alpha_min, Int32(vi.indicator.alpha_smooth)
     end
-    eq = equations isa Trixi.AbstractCompressibleEulerEquations ? EQ_COMPRESSIBLE_EULER : EQ_LINEAR_ADVECTION
+    eq = equations isa Trixi.AbstractCompressibleEulerEquations ? EQ_COMPRESSIBLE_EULER :
+         equations isa Trixi.AbstractIdealGlmMhdEquations ? EQ_IDEAL_GLM_MHD : EQ_LINEAR_ADVECTION
     adv = eq == EQ_LINEAR_ADVECTION ? (Float64.(equations.advection_velocity)..., 0.0, 0.0, 0.0)[1:3] : (0.0, 0.0, 0.0)
-    gamma = eq == EQ_COMPRESSIBLE_EULER ? Float64(equations.gamma) : 1.4
+    gamma = eq == EQ_LINEAR_ADVECTION ? 1.4 : Float64(equations.gamma)
+    # ideal GLM-MHD: the nonconservative flux of the surface pair and c_h
+    # (equations.c_h; a GlmSpeedCallback updates it through trixi_set_glm_speed)
+    noncons = noncons_code(solver.surface_integral.surface_flux)
+    c_h = eq == EQ_IDEAL_GLM_MHD && ndims(mesh) > 1 ? Float64(equations.c_h) : 0.0
     # keep the host arrays alive for the duration of the call
     dsplit = Matrix{Float64}(Array(basis.derivative_split))
     dhat = Matrix{Float64}(Array(basis.derivative_dhat))
@@ -125,7 +142,7 @@ function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
                        pointer(mortars.orientations), pointer(weights), pointer(dsplit), pointer(dhat),
                        C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, pointer(elements.node_coordinates), 0,
                        C_NULL, C_NULL, C_NULL, Int32(-1), Int32(0), Int32(0), Int32(0),
-                       ntuple(_ -> 0.0, 8), ntuple(_ -> 0.0, 3))
+                       ntuple(_ -> 0.0, 8), ntuple(_ -> 0.0, 3), noncons, Int32(0), c_h)
     desc.struct_size = Int32(sizeof(ProblemDesc))
     handle = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve elements interfaces mortars dsplit dhat weights desc begin
@@ -166,6 +183,10 @@ cuda_surface_integral!(du, handle) =
 cuda_jacobian!(du, handle) =
     check(ccall((:trixi_jacobian, libtrixi), Cint, (Ptr{Cvoid}, CuPtr{Float64}, Ptr{Cvoid}),
                 handle, pointer(du), stream_ptr()))
+
+# GlmSpeedCallback: equations.c_h changed between steps
+set_glm_speed!(handle, c_h) =
+    check(ccall((:trixi_set_glm_speed, libtrixi), Cint, (Ptr{Cvoid}, Float64), handle, Float64(c_h)))
 
 destroy!(handle) = ccall((:trixi_destroy, libtrixi), Cint, (Ptr{Cvoid},), handle)
 
