@@ -242,3 +242,51 @@ def test_mhd_rejections(cuda):
             polydeg=5, surface_flux=(T.flux_lax_friedrichs, T.flux_nonconservative_powell),
             volume_integral=T.VolumeIntegralFluxDifferencing((T.flux_hindenlang_gassner,
                                                               T.flux_nonconservative_powell))))
+
+
+def _np_prim(eq, u):
+    uu = u.reshape(-1, eq.nvariables).T
+    rho, v, p = eq.cons2prim(uu)
+    return uu, rho, v, p
+
+
+def test_mhd_max_dt(cuda):
+    """max_dt with |v_d| + the fast magnetosonic speed (StepsizeCallback)."""
+    for d in (1, 2, 3):
+        semi, _ = _semi("alfven", d, 3 if d < 3 else 2, 3, False)
+        u_host, u = _u(semi, cuda)
+        eq = semi.equations
+        uu, rho, v, p = _np_prim(eq, u_host)
+        a2, b2 = eq.gamma * p / rho, np.sum(uu[5:8] ** 2, axis=0) / rho
+        E, NN = semi.nelements, semi.nnodes ** d
+        lam = []
+        for k in range(d):
+            cf = np.sqrt(0.5 * (a2 + b2 + np.sqrt((a2 + b2) ** 2 - 4 * a2 * uu[5 + k] ** 2 / rho)))
+            lam.append(np.max((np.abs(v[k]) + cf).reshape(E, NN), axis=1))
+        m = np.max(semi.containers.inverse_jacobian * np.sum(lam, axis=0))
+        ref = 2.0 / (semi.nnodes * m)
+        assert abs(T.max_dt(u, semi) - ref) <= 1e-13 * ref
+
+
+def test_mhd_integrals(cuda):
+    """State and entropy integrals, and the entropy production of the
+    entropy-conservative set-up (flux_hindenlang_gassner + Powell terms on a
+    periodic mesh): zero to round-off, on the GPU's own rhs."""
+    semi, _ = _semi("ec", 2, 3, 3, False)
+    u_host, u = _u(semi, cuda)
+    eq = semi.equations
+    du = cuda.empty_like(u)
+    T.rhs_gpu(du, u, semi, 0.0)
+    w1 = semi.solver.basis.weights
+    wn = np.multiply.outer(w1, w1).T.reshape(-1)
+    J = (1.0 / semi.containers.inverse_jacobian) ** 2
+    state = T.integrate(u, semi, "state")
+    ref = np.einsum("e,n,env->v", J, wn, u_host.reshape(semi.nelements, -1, eq.nvariables))
+    assert_rel(state, ref, 1e-13, "state integral")
+    uu, rho, v, p = _np_prim(eq, u_host)
+    s = np.log(p) - eq.gamma * np.log(rho)
+    S = (-rho * s / (eq.gamma - 1)).reshape(semi.nelements, -1)
+    assert_rel(T.integrate(u, semi, "entropy"), [np.einsum("e,n,en->", J, wn, S)], 1e-13, "entropy integral")
+    prod = T.integrate(u, semi, "entropy_production", du=du)[0]
+    scale = float(np.einsum("e,n,en->", J, wn, np.abs(S)))
+    assert abs(prod) < 1e-11 * scale, (prod, scale)

@@ -46,6 +46,28 @@ __global__ void max_speed_kernel(int N, int64_t E, const double *__restrict__ u,
     lam[0] = fabs(a0);
     lam[1] = fabs(a1);
     lam[2] = fabs(a2);
+  } else if (EQ == EQ_MHD) {
+    // ideal GLM-MHD: |v_d| + the fast magnetosonic speed along d
+    for (int n = lane; n < NN; n += 32) {
+      const double *un = u + (e * NN + n) * NV;
+      const double rho = un[0];
+      double kin = 0.0, mag = 0.0, v[3];
+      for (int d = 0; d < 3; ++d) {
+        v[d] = un[1 + d] / rho;
+        kin += un[1 + d] * v[d];
+        mag += un[5 + d] * un[5 + d];
+      }
+      const double psi2 = (NV == 9) ? un[NV - 1] * un[NV - 1] : 0.0;
+      const double p = (gamma - 1.0) * (un[4] - 0.5 * kin - 0.5 * mag - 0.5 * psi2);
+      const double a2 = gamma * p / rho, b2 = mag / rho;
+      for (int d = 0; d < DIM; ++d) {
+        const double bd2 = un[5 + d] * un[5 + d] / rho;
+        const double cf = sqrt(0.5 * (a2 + b2 + sqrt((a2 + b2) * (a2 + b2) - 4.0 * a2 * bd2)));
+        lam[d] = fmax(lam[d], fabs(v[d]) + cf);
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1)
+      for (int d = 0; d < DIM; ++d) lam[d] = fmax(lam[d], __shfl_xor_sync(0xffffffffu, lam[d], off));
   } else {
     for (int n = lane; n < NN; n += 32) {
       const double *un = u + (e * NN + n) * NV;
@@ -94,6 +116,32 @@ __device__ void quantity(int which, const double *un, const double *dun, double 
   if (EQ == EQ_ADV) {
     if (which == 1) q[0] = 0.5 * un[0] * un[0];  // entropy 1/2 u^2
     else q[0] = un[0] * dun[0];                  // entropy variable u times du
+    return;
+  }
+  if (EQ == EQ_MHD) {
+    // ideal GLM-MHD: S = -rho s/(gamma-1) with the MHD pressure; entropy
+    // variables ((gamma-s)/(gamma-1) - beta|v|^2, 2 beta v, -2 beta, 2 beta B,
+    // 2 beta psi), beta = rho/(2p) (Derigs et al., JCP 364 (2018))
+    const double rho = un[0];
+    double kin = 0.0, mag = 0.0, v[3];
+    for (int d = 0; d < 3; ++d) {
+      v[d] = un[1 + d] / rho;
+      kin += un[1 + d] * v[d];
+      mag += un[5 + d] * un[5 + d];
+    }
+    const double psi = (NV == 9) ? un[NV - 1] : 0.0;
+    const double p = (gamma - 1.0) * (un[4] - 0.5 * kin - 0.5 * mag - 0.5 * psi * psi);
+    const double s = log(p) - gamma * log(rho);
+    if (which == 1) {
+      q[0] = -rho * s / (gamma - 1.0);
+      return;
+    }
+    const double rho_p = rho / p;  // 2 beta
+    double acc = ((gamma - s) / (gamma - 1.0) - 0.5 * rho_p * kin / rho) * dun[0];
+    for (int d = 0; d < 3; ++d) acc += rho_p * (v[d] * dun[1 + d] + un[5 + d] * dun[5 + d]);
+    acc += -rho_p * dun[4];
+    if (NV == 9) acc += rho_p * psi * dun[NV - 1];
+    q[0] = acc;
     return;
   }
   const double rho = un[0];
@@ -380,12 +428,24 @@ cudaError_t launch_error_norms(const ErrorNormHost &h, cudaStream_t s) {
     }                                                                 \
   } while (0)
 
+// the same with ideal GLM-MHD (max_dt and the integrals)
+#define TRIXI_DISPATCH_MHD(dim, eq, call)                                                   \
+  do {                                                                                      \
+    if ((eq) == EQ_MHD) {                                                                   \
+      if ((dim) == 1) { constexpr int D_ = 1, Q_ = EQ_MHD; call; }                          \
+      else if ((dim) == 2) { constexpr int D_ = 2, Q_ = EQ_MHD; call; }                     \
+      else { constexpr int D_ = 3, Q_ = EQ_MHD; call; }                                     \
+    } else {                                                                                \
+      TRIXI_DISPATCH(dim, eq, call);                                                        \
+    }                                                                                       \
+  } while (0)
+
 cudaError_t launch_max_dt(const MaxDtHost &h, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(h.acc, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   const int per_block = 8;  // one warp per element
   const unsigned grid = (unsigned)((h.E + per_block - 1) / per_block);
-  TRIXI_DISPATCH(h.dim, h.eq,
+  TRIXI_DISPATCH_MHD(h.dim, h.eq,
                  (max_speed_kernel<D_, Q_><<<grid, 32 * per_block, 0, s>>>(h.N, h.E, h.u, h.inv_jac, h.gamma, h.a[0],
                                                                            h.a[1], h.a[2], h.acc)));
   e = cudaGetLastError();
@@ -397,7 +457,7 @@ cudaError_t launch_max_dt(const MaxDtHost &h, cudaStream_t s) {
 cudaError_t launch_integrate(const IntegrateHost &h, cudaStream_t s) {
   const int per_block = 8;
   const unsigned grid = (unsigned)((h.E + per_block - 1) / per_block);
-  TRIXI_DISPATCH(h.dim, h.eq,
+  TRIXI_DISPATCH_MHD(h.dim, h.eq,
                  (integrate_kernel<D_, Q_><<<grid, 32 * per_block, 0, s>>>(h.N, h.E, h.u, h.du, h.inv_jac, h.w, h.which,
                                                                            h.nq, h.gamma, h.partial)));
   cudaError_t e = cudaGetLastError();

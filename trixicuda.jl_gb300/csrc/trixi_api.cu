@@ -1039,7 +1039,6 @@ int trixi_compute_coefficients(trixi_handle *h, int ic_kind, const double *param
 
 int trixi_max_dt(trixi_handle *h, const double *u, double *dt_dev, void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
-  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: not available in this function");
   if (int st = check_u_args(h, u, "u")) return st;
   if (int st = check_u_args(h, dt_dev, "dt")) return st;
   if (int st = ensure_reduction(h, 1)) return st;
@@ -1061,7 +1060,6 @@ int trixi_max_dt(trixi_handle *h, const double *u, double *dt_dev, void *stream)
 int trixi_integrate(trixi_handle *h, const double *u, const double *du, int which, double *out_host, int64_t count,
                     void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
-  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: not available in this function");
   if (int st = check_u_args(h, u, "u")) return st;
   if (which < 0 || which > 3) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "integral kind %d", which);
   if ((which == 2 || which == 3) && !aligned8(du)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "du is required");

@@ -470,7 +470,7 @@ def integrate(u, semi, which="state", du=None, stream=None) -> np.ndarray:
     _check_state(semi, u)
     if du is not None:
         _check_state(semi, du)
-    out = np.zeros(8)
+    out = np.zeros(max(8, semi.equations.nvariables))
     _lib.check(semi._lib.trixi_integrate(semi._handle, C.c_void_p(u.data_ptr()),
                                          C.c_void_p(du.data_ptr()) if du is not None else None, codes[which],
                                          out.ctypes.data_as(C.POINTER(C.c_double)), out.size,
