@@ -57,12 +57,30 @@ def build_problem(precision: str):
     return mesh, eq, ic, solver
 
 
-def stable_dt(semi) -> float:
+C3_LEVEL = 5
+C3_WORKLOAD = ("3D compressible Euler, TreeMesh [-2,2]^3 periodic level 5 (32768 elements), polydeg 3, "
+               "Hennemann-Gassner shock capturing (density_pressure, alpha_max 0.5, alpha_min 0.001, smoothing), "
+               "flux_ranocha volume, flux_lax_friedrichs surface and FV, weak blast wave, CarpenterKennedy2N54 step")
+
+
+def build_problem_c3(precision: str):
+    """The 3D shock-capturing configuration (test/tree_dgsem_3d/euler_shock.jl set-up, level 5)."""
+    import trixicuda as T
+
+    eq = T.CompressibleEulerEquations3D(1.4)
+    ind = T.IndicatorHennemannGassner(eq, None, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True)
+    vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=T.flux_ranocha, volume_flux_fv=T.flux_lax_friedrichs)
+    solver = T.DGSEMGPU(polydeg=POLYDEG, surface_flux=T.flux_lax_friedrichs, volume_integral=vi)
+    mesh = T.TreeMesh((-2.0,) * 3, (2.0,) * 3, initial_refinement_level=C3_LEVEL)
+    return mesh, eq, T.initial_condition_weak_blast_wave, solver
+
+
+def stable_dt(semi, level=LEVEL) -> float:
     """CFL 0.5 time step from the initial state (max |v| + c)."""
     u = semi.compute_coefficients_host().reshape(-1, semi.equations.nvariables).T
     rho, v, p = semi.equations.cons2prim(u)
     lam = np.max(np.sqrt(np.sum(v * v, axis=0)) + np.sqrt(semi.equations.gamma * p / rho))
-    h = 4.0 / 2**LEVEL
+    h = 4.0 / 2**level
     return 0.5 * h / (POLYDEG + 1) / lam
 
 
@@ -129,18 +147,19 @@ def _tile_report(semi):
             "tuner_us_per_launch": {f"{w}x{g}": round(ms * 1e3, 2) for (w, g), ms in sorted(table.items())}}
 
 
-def time_gpu_path(precision, steps, warmup, device, flush, tile=None):
+def time_gpu_path(precision, steps, warmup, device, flush, tile=None, c3=False):
     """Device-timed CK2N54 steps through trixi_rk_stage (ping-pong buffers).
-    Returns per-step ms (back-to-back launches), per-launch ms of the fused
-    kernel (a second loop with events around every launch), the semi, final u."""
+    Returns per-step ms (back-to-back launches), per-launch ms of the stage
+    (a second loop with events around every stage: the fused kernel, plus the
+    indicator for shock capturing), the semi, final u."""
     import torch
 
     import trixicuda as T
     from trixicuda.time_integration import CK2N54_A, CK2N54_B
 
-    mesh, eq, ic, solver = build_problem(precision)
+    mesh, eq, ic, solver = (build_problem_c3 if c3 else build_problem)(precision)
     semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, precision=precision)
-    dt = stable_dt(semi)
+    dt = stable_dt(semi, C3_LEVEL if c3 else LEVEL)
     u0 = semi.compute_coefficients()
     if tile:  # a fixed tile (profiling: a tuner run under a profiler would time other things)
         T.set_tile(semi, *tile)
@@ -412,7 +431,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "batched-mixed", "batched-fp64", "adjoint"], default=None,
+    ap.add_argument("--no-c3", action="store_true", help="skip the 3D shock-capturing configuration")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "batched-mixed", "batched-fp64", "adjoint", "c3-mixed",
+                                          "c3-fp64"], default=None,
                     help="run only the device-timed loop of one precision (for ncu captures)")
     ap.add_argument("--tile", default=None,
                     help="with --profile mixed/fp64: fixed tile WPGxGPB (e.g. 2x4) instead of the tuner")
@@ -459,7 +480,9 @@ def main():
         return 0
     if args.profile:
         tile = tuple(int(x) for x in args.tile.split("x")) if args.tile else None
-        step_ms, launch_ms, semi, _, _ = time_gpu_path(args.profile, args.steps, args.warmup, device, flush, tile)
+        c3 = args.profile.startswith("c3-")
+        step_ms, launch_ms, semi, _, _ = time_gpu_path(args.profile.split("-")[-1], args.steps, args.warmup, device,
+                                                       flush, tile, c3=c3)
         print(json.dumps({"profile": args.profile, "ms_per_step": statistics.mean(step_ms),
                           "mean_launch_ms": statistics.mean(launch_ms), "fp64_fma_peak_tflops": fp64_peak.value / 1e12,
                           "fp32_fma_peak_tflops": fp32_peak.value / 1e12}))
@@ -498,6 +521,7 @@ def main():
         for r in batched.values():
             r["hbm_frac"] = r["achieved_gbs"] / hbm_peak
     adjoint = None if args.no_adjoint else adjoint_path(device)
+    c3 = None if args.no_c3 else c3_path(max(3, args.steps // 4), 3, device, flush, hbm_peak)
     cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline()
     traffic = None
     prof = ROOT / "profiles" / "traffic_fused_rk_stage_euler2d_l7.json"
@@ -523,6 +547,7 @@ def main():
                 "d2h_bytes_per_step": nbytes, "api": "trixicuda.rk_steps (C ABI trixi_rk_steps)"},
         "batched": batched,
         "adjoint": adjoint,
+        "shock_capturing_3d": c3,
         "cpu_baseline": cpu,
         "gpu_launches": 5 * args.steps,
         "clocks": clocks,
@@ -532,6 +557,28 @@ def main():
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def c3_path(steps, warmup, device, flush, hbm_peak):
+    """The 3D shock-capturing configuration (level 5, 32768 elements, 2.1 M
+    DOFs, 84 MB FP64 state), FP32-mixed and FP64, tuned tiles.  Each RK stage
+    is the indicator (two small kernels) and the fused stage kernel."""
+    out = {"workload": C3_WORKLOAD}
+    for prec in ("mixed", "fp64"):
+        step_ms, stage_ms, semi, _, _ = time_gpu_path(prec, steps, warmup, device, flush, c3=True)
+        dofs, nv, E = semi.ndofs(), semi.equations.nvariables, semi.nelements
+        nval = dofs * nv
+        # algorithmic bytes of one stage: the fused kernel reads u, k and writes u_out, k
+        # (stage 1 does not read k), plus J^{-1}, alpha and the face table; the
+        # indicator reads u once more
+        stage_bytes = statistics.mean([nval * 8 * (3 if st == 0 else 4) + E * (8 + 8 + 6 * 4) + nval * 8
+                                       for st in range(5)])
+        ms = statistics.mean(step_ms)
+        ach = stage_bytes / (statistics.mean(stage_ms) * 1e-3) / 1e9
+        out[prec] = {"value": 5 * dofs / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms,
+                     "mean_stage_ms": statistics.mean(stage_ms), "algorithmic_bytes_per_stage": stage_bytes,
+                     "achieved_gbs": ach, "hbm_frac": ach / hbm_peak, "tile": _tile_report(semi)}
+    return out
 
 
 def l2_mixed_vs_fp64(semi_mixed, semi64, dt, nsteps):

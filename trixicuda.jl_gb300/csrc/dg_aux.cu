@@ -7,6 +7,7 @@
 
 #include "dg_host.h"
 #include "dg_ic.cuh"
+#include "dg_convert.cuh"
 #include "dg_physics.cuh"
 
 namespace trixi {
@@ -219,71 +220,158 @@ struct IvdmMat {
   double m[HOST_NMAX * HOST_NMAX];
 };
 
-template <int DIM>
-__global__ void indicator_raw_kernel(int N, int64_t E, int epb, const double *__restrict__ u, double *__restrict__ alpha_raw,
-                                     double gamma, double amax, double amin, double threshold, double param_s,
-                                     IvdmMat ivdm, int mhd) {
-  const int NV = mhd ? (DIM == 1 ? 8 : 9) : DIM + 2;
-  extern __shared__ __align__(16) double sm[];
-  int NN = N;
-  for (int d = 1; d < DIM; ++d) NN *= N;
-  double *s_a = sm;                // [epb][NN]
-  double *s_b = sm + epb * NN;     // [epb][NN]
-  const int64_t e0 = (int64_t)blockIdx.x * epb;
-  const int ne = (int)min((int64_t)epb, E - e0);
-  for (int i = threadIdx.x; i < ne * NN; i += blockDim.x) {
-    const int el = i / NN, n = i - el * NN;
-    const double *un = u + ((e0 + el) * NN + n) * NV;
-    const double rho = un[0];
-    double kin = 0.0, p;
-    if (mhd) {  // p = (gamma-1)(E - rho|v|^2/2 - |B|^2/2 - psi^2/2)
-      double mag = 0.0;
-      for (int d = 0; d < 3; ++d) {
-        kin += un[1 + d] * (un[1 + d] / rho);
-        mag += un[5 + d] * un[5 + d];
-      }
-      if (NV == 9) mag += un[8] * un[8];
-      p = (gamma - 1.0) * (un[4] - 0.5 * kin - 0.5 * mag);
-    } else {
-      for (int d = 0; d < DIM; ++d) kin += un[1 + d] * (un[1 + d] / rho);
-      p = (gamma - 1.0) * (un[DIM + 1] - 0.5 * kin);
-    }
-    s_a[i] = rho * p;
-  }
+// Eight elements per block, N a compile-time constant, compute type R
+// (double; float in the FP32-mixed rhs, states narrowed on the integer pipe).
+// Each warp computes rho*p and the modal transform of one element.  Then warp 0
+// accumulates the three energy sums of all eight elements at once -- three
+// lanes per element, each a sequential fold in node order, the oracle's
+// order, so the FP64 result matches it bit for bit.  An FP64 warp instruction
+// occupies GB300's narrow FP64 pipe for the whole warp however few lanes are
+// active, so a sequential fold per element on a single lane cost ~0.4 ms per
+// call on the 3D level-5 mesh; folding 24 sums in one instruction stream
+// divides that by eight.
+template <typename R>
+__device__ __forceinline__ R ind_load(const double *p) { return R(*p); }
+template <>
+__device__ __forceinline__ float ind_load<float>(const double *p) { return from_double<float>(*p); }
+__device__ __forceinline__ double ind_div(double a, double b) { return a / b; }
+__device__ __forceinline__ float ind_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double ind_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float ind_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double ind_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float ind_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double ind_exp(double x) { return exp(x); }
+__device__ __forceinline__ float ind_exp(float x) { return __expf(x); }
+
+template <int DIM, int N, typename R>
+__global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const double *__restrict__ u,
+                                                            double *__restrict__ alpha_raw, double gamma_, double amax,
+                                                            double amin, double threshold_, double param_s_,
+                                                            IvdmMat ivdm, int mhd, int nv) {
+  constexpr int NN = (DIM == 1) ? N : (DIM == 2 ? N * N : N * N * N);
+  constexpr int WPB = 8;  // warps (elements) per block
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  R *s_iv = reinterpret_cast<R *>(sm_raw);  // [N][N] inverse Vandermonde (lanes read it at different indices)
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) s_iv[i] = R(ivdm.m[i]);
   __syncthreads();
-  double *src = s_a, *dst = s_b;
-  int stride = 1;
-  for (int d = 0; d < DIM; ++d) {
-    for (int i = threadIdx.x; i < ne * NN; i += blockDim.x) {
-      const int el = i / NN, n = i - el * NN;
-      const int c = (n / stride) % N;
-      const int nb = n - c * stride;
-      double s = 0.0;
-      for (int m = 0; m < N; ++m) s += ivdm.m[c * N + m] * src[el * NN + nb + m * stride];
-      dst[i] = s;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e0 = (int64_t)blockIdx.x * WPB;
+  const int64_t e = e0 + warp;
+  R *a = s_iv + N * N + warp * 2 * NN, *b = a + NN;
+  R *coef = a;  // where this warp's modal coefficients end up
+  if (e < E) {
+    const R half = R(0.5), gm1 = R(gamma_ - 1.0);
+    for (int n = lane; n < NN; n += 32) {
+      const double *un = u + (e * NN + n) * nv;
+      const R rho = ind_load<R>(un);
+      const R inv = ind_div(R(1), rho);  // one reciprocal, not a division per component
+      R kin = R(0), p;
+      if (mhd) {  // p = (gamma-1)(E - rho|v|^2/2 - |B|^2/2 - psi^2/2)
+        R mag = R(0);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const R m = ind_load<R>(un + 1 + d), B = ind_load<R>(un + 5 + d);
+          kin += m * (m * inv);
+          mag += B * B;
+        }
+        if (nv == 9) {
+          const R psi = ind_load<R>(un + 8);
+          mag += psi * psi;
+        }
+        p = gm1 * (ind_load<R>(un + 4) - half * kin - half * mag);
+      } else {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const R m = ind_load<R>(un + 1 + d);
+          kin += m * (m * inv);
+        }
+        p = gm1 * (ind_load<R>(un + DIM + 1) - half * kin);
+      }
+      a[n] = rho * p;
     }
-    __syncthreads();
-    double *t = src; src = dst; dst = t;
-    stride *= N;
+    __syncwarp();
+    R *src = a, *dst = b;
+    int stride = 1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      for (int n = lane; n < NN; n += 32) {
+        const int c = (n / stride) % N;
+        const int nb = n - c * stride;
+        R acc = R(0);
+#pragma unroll
+        for (int m = 0; m < N; ++m) acc += s_iv[c * N + m] * src[nb + m * stride];
+        dst[n] = acc;
+      }
+      __syncwarp();
+      R *t = src;
+      src = dst;
+      dst = t;
+      stride *= N;
+    }
+    coef = src;
   }
-  for (int el = threadIdx.x; el < ne; el += blockDim.x) {
-    double total = 0.0, clip1 = 0.0, clip2 = 0.0;
+  // coefficient arrays alternate between a and b per dimension: after DIM
+  // passes they sit in a when DIM is even, in b when it is odd
+  (void)coef;
+  __syncthreads();
+  if (warp != 0) return;
+  const int el = lane / 3, which = lane - 3 * (lane / 3);  // which: 0 all modes, 1 without the highest, 2 without two
+  const bool active = lane < 3 * WPB && e0 + el < E;
+  R sum = R(0);
+  if (active) {
+    const R *c = s_iv + N * N + el * 2 * NN + ((DIM & 1) ? NN : 0);
     for (int n = 0; n < NN; ++n) {
-      int maxc = 0, r = n;
-      for (int d = 0; d < DIM; ++d) { maxc = max(maxc, r % N); r /= N; }
-      const double m2 = src[el * NN + n] * src[el * NN + n];
-      total += m2;
-      if (maxc < N - 1) clip1 += m2;
-      if (maxc < N - 2) clip2 += m2;
+      int maxc = n % N;
+      if (DIM > 1) maxc = max(maxc, (n / N) % N);
+      if (DIM > 2) maxc = max(maxc, n / (N * N));
+      const bool take = (which == 0) || (which == 1 && maxc < N - 1) || (which == 2 && maxc < N - 2);
+      if (take) sum = ind_add(sum, ind_mul(c[n], c[n]));  // no contraction: the oracle's roundings
     }
-    const double f1 = (total != 0.0) ? (total - clip1) / total : 0.0;
-    const double f2 = (clip1 != 0.0) ? (clip1 - clip2) / clip1 : 0.0;
-    const double energy = fmax(f1, f2);
-    double a = 1.0 / (1.0 + exp(-param_s / threshold * (energy - threshold)));
-    if (a < amin) a = 0.0;
-    if (a > 1.0 - amin) a = 1.0;
-    alpha_raw[e0 + el] = fmin(amax, a);
   }
+  const R clip1 = __shfl_down_sync(0xffffffffu, sum, 1), clip2 = __shfl_down_sync(0xffffffffu, sum, 2);
+  if (active && which == 0) {
+    const R total = sum;
+    const R f1 = (total != R(0)) ? (total - clip1) / total : R(0);
+    const R f2 = (clip1 != R(0)) ? (clip1 - clip2) / clip1 : R(0);
+    const R energy = f1 > f2 ? f1 : f2;
+    const R threshold = R(threshold_);
+    double al = double(R(1) / (R(1) + ind_exp(-R(param_s_) / threshold * (energy - threshold))));
+    if (al < amin) al = 0.0;
+    if (al > 1.0 - amin) al = 1.0;
+    alpha_raw[e0 + el] = fmin(amax, al);
+  }
+}
+
+template <int DIM, int N>
+static cudaError_t launch_indicator_raw(const IndicatorHost &ih, cudaStream_t s) {
+  constexpr int NN = (DIM == 1) ? N : (DIM == 2 ? N * N : N * N * N);
+  const int64_t grid = (ih.nelements + 7) / 8;
+  IvdmMat iv;
+  std::copy(ih.ivdm, ih.ivdm + HOST_NMAX * HOST_NMAX, iv.m);
+  if (ih.mixed) {
+    const size_t smem = sizeof(float) * (size_t)(N * N + 8 * 2 * NN);
+    indicator_raw_kernel<DIM, N, float><<<(unsigned)grid, 256, smem, s>>>(
+        ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
+        ih.eq == EQ_MHD ? 1 : 0, ih.nv);
+  } else {
+    const size_t smem = sizeof(double) * (size_t)(N * N + 8 * 2 * NN);
+    indicator_raw_kernel<DIM, N, double><<<(unsigned)grid, 256, smem, s>>>(
+        ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
+        ih.eq == EQ_MHD ? 1 : 0, ih.nv);
+  }
+  return cudaGetLastError();
+}
+
+template <int DIM>
+static cudaError_t launch_indicator_dim(const IndicatorHost &ih, cudaStream_t s) {
+  switch (ih.N) {
+    case 2: return launch_indicator_raw<DIM, 2>(ih, s);
+    case 3: return launch_indicator_raw<DIM, 3>(ih, s);
+    case 4: return launch_indicator_raw<DIM, 4>(ih, s);
+    case 5: return launch_indicator_raw<DIM, 5>(ih, s);
+    case 6: return launch_indicator_raw<DIM, 6>(ih, s);
+  }
+  return cudaErrorNotSupported;
 }
 
 // alpha[e] = max(alpha_raw[e], 0.5 * alpha_raw[face neighbours]) -- the result
@@ -313,27 +401,8 @@ __global__ void indicator_smooth_kernel(int dim, int64_t E, const double *__rest
 
 cudaError_t launch_indicator(const IndicatorHost &ih, cudaStream_t s) {
   if (ih.nelements <= 0) return cudaSuccess;
-  int NN = ih.N;
-  for (int d = 1; d < ih.dim; ++d) NN *= ih.N;
-  const int epb = std::max(1, 256 / NN);
-  const int block = std::min(256, std::max(32, ((epb * NN + 31) / 32) * 32));
-  const size_t smem = sizeof(double) * 2 * (size_t)epb * NN;
-  const int64_t grid = (ih.nelements + epb - 1) / epb;
-  IvdmMat iv;
-  std::copy(ih.ivdm, ih.ivdm + HOST_NMAX * HOST_NMAX, iv.m);
-  if (ih.dim == 1)
-    indicator_raw_kernel<1><<<(unsigned)grid, block, smem, s>>>(ih.N, ih.nelements, epb, ih.u, ih.alpha_raw, ih.gamma,
-                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
-                                                              ih.eq == EQ_MHD ? 1 : 0);
-  else if (ih.dim == 2)
-    indicator_raw_kernel<2><<<(unsigned)grid, block, smem, s>>>(ih.N, ih.nelements, epb, ih.u, ih.alpha_raw, ih.gamma,
-                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
-                                                              ih.eq == EQ_MHD ? 1 : 0);
-  else
-    indicator_raw_kernel<3><<<(unsigned)grid, block, smem, s>>>(ih.N, ih.nelements, epb, ih.u, ih.alpha_raw, ih.gamma,
-                                                              ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
-                                                              ih.eq == EQ_MHD ? 1 : 0);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = (ih.dim == 1) ? launch_indicator_dim<1>(ih, s)
+                  : (ih.dim == 2) ? launch_indicator_dim<2>(ih, s) : launch_indicator_dim<3>(ih, s);
   if (e != cudaSuccess) return e;
   indicator_smooth_kernel<<<(unsigned)((ih.nelements + 255) / 256), 256, 0, s>>>(
       ih.dim, ih.nelements, ih.alpha_raw, ih.alpha, ih.face_table, ih.slot_neighbors, ih.smooth);

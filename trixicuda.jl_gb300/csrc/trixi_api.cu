@@ -509,12 +509,15 @@ void fill_mortar(const trixi_handle *h, MortarHost &mh, const double *u) {
   mh.err = h->d_err;
 }
 
-int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStream_t s) {
+// fp32: the indicator inside an FP32-mixed rhs; the stage entry point
+// trixi_indicator always computes in FP64
+int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStream_t s, bool fp32 = false) {
   IndicatorHost ih;
   ih.dim = h->dim;
   ih.N = h->N;
   ih.nv = h->nv;
   ih.eq = h->eq;
+  ih.mixed = fp32;
   ih.nelements = h->E;
   ih.u = u;
   ih.alpha_raw = h->d_alpha_raw;
@@ -537,7 +540,7 @@ int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStrea
 int run_rhs(trixi_handle *h, int mode, const double *u_in, double *out, double *k, double a, double b, double dt,
             cudaStream_t s, double t = 0.0) {
   if (h->vol == TRIXI_VOLUME_SHOCK_CAPTURING_HG) {
-    int st = run_indicator(h, u_in, h->d_alpha, s);
+    int st = run_indicator(h, u_in, h->d_alpha, s, h->mixed && mode != MODE_VOLUME);
     if (st) return st;
   }
   if (h->M > 0 && mode != MODE_VOLUME) {
