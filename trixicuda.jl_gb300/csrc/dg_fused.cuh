@@ -691,7 +691,9 @@ struct FusedKernel {
       }
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        const double du = double(acc[v]) * sc + src[v];
+        double du;
+        if constexpr (BND) du = double(acc[v]) * sc + src[v];
+        else du = double(acc[v]) * sc;
         if (mode == MODE_RHS) {
           o[v] = du;
         } else {
@@ -718,7 +720,9 @@ struct FusedKernel {
       }
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        const double dd = to_double(acc[v] * sc) + src[v];
+        // (x + 0.0 is not x for x = -0: without sources the FP64 add is not emitted)
+        double dd = to_double(acc[v] * sc);
+        if constexpr (BND) dd += src[v];
         if (mode == MODE_RHS) {
           o[v] = dd;
         } else {
