@@ -463,8 +463,59 @@ static void flux_llf(const phys_t *P, const double *ul, const double *ur, int o,
   for (int v = 0; v < P->nv; ++v) f[v] += -0.5 * lam * (ur[v] - ul[v]);
 }
 
+/* Shima, Kuya, Tamaki, Kawai (2021), JCP 427: kinetic-energy and pressure-
+ * equilibrium preserving flux (Euler). */
+static void flux_shima(const phys_t *P, const double *ul, const double *ur, int o, double *f) {
+  const int dim = P->dim;
+  double rl, rr, vl[3], vr[3], pl, pr;
+  cons2prim(P, ul, &rl, vl, &pl);
+  cons2prim(P, ur, &rr, vr, &pr);
+  const double rho_avg = 0.5 * (rl + rr), p_avg = 0.5 * (pl + pr);
+  double vavg[3], kin = 0;
+  for (int d = 0; d < dim; ++d) { vavg[d] = 0.5 * (vl[d] + vr[d]); kin += vl[d] * vr[d]; }
+  kin *= 0.5;
+  const double f0 = rho_avg * vavg[o];
+  f[0] = f0;
+  for (int d = 0; d < dim; ++d) f[1 + d] = f0 * vavg[d] + (d == o ? p_avg : 0.0);
+  f[dim + 1] = p_avg * vavg[o] / (P->gamma - 1) + f0 * kin + 0.5 * (pl * vr[o] + pr * vl[o]);
+}
+
+/* HLL (Harten, Lax, van Leer 1983) with the naive signal-speed estimates
+ * min(v_l - c_l, v_r - c_r), max(v_l + c_l, v_r + c_r) (fast magnetosonic c
+ * for MHD, the advection speed for linear advection). */
+static void flux_hll(const phys_t *P, const double *ul, const double *ur, int o, double *f) {
+  double lmin, lmax;
+  if (P->eq == ORC_EQ_ADVECTION) {
+    lmin = lmax = P->a[o];
+  } else if (P->eq == ORC_EQ_MHD) {
+    double wl[9], wr[9];
+    mhd_prim(P, ul, wl);
+    mhd_prim(P, ur, wr);
+    const double cl = mhd_fast_speed(P, wl, o), cr = mhd_fast_speed(P, wr, o);
+    lmin = fmin(wl[1 + o] - cl, wr[1 + o] - cr);
+    lmax = fmax(wl[1 + o] + cl, wr[1 + o] + cr);
+  } else {
+    double rl, rr, vl[3], vr[3], pl, pr;
+    cons2prim(P, ul, &rl, vl, &pl);
+    cons2prim(P, ur, &rr, vr, &pr);
+    const double cl = sqrt(P->gamma * pl / rl), cr = sqrt(P->gamma * pr / rr);
+    lmin = fmin(vl[o] - cl, vr[o] - cr);
+    lmax = fmax(vl[o] + cl, vr[o] + cr);
+  }
+  double fl[NVMAX], fr[NVMAX];
+  flux_phys(P, ul, o, fl);
+  flux_phys(P, ur, o, fr);
+  for (int v = 0; v < P->nv; ++v) {
+    if (lmin >= 0) f[v] = fl[v];
+    else if (lmax <= 0) f[v] = fr[v];
+    else f[v] = (lmax * fl[v] - lmin * fr[v] + lmin * lmax * (ur[v] - ul[v])) / (lmax - lmin);
+  }
+}
+
 static void two_point_flux(const phys_t *P, int kind, const double *ul, const double *ur, int o, double *f) {
   switch (kind) {
+    case ORC_FLUX_SHIMA_ETAL: flux_shima(P, ul, ur, o, f); break;
+    case ORC_FLUX_HLL: flux_hll(P, ul, ur, o, f); break;
     case ORC_FLUX_RANOCHA: flux_ranocha(P, ul, ur, o, f); break;
     case ORC_FLUX_HINDENLANG_GASSNER: mhd_flux_hindenlang_gassner(P, ul, ur, o, f); break;
     case ORC_FLUX_CENTRAL: flux_central(P, ul, ur, o, f); break;

@@ -12,7 +12,7 @@ bool fused_supported(int dim, int N, int eq, int vol, int vflux) {
   }
   if (vflux == 4) return false;  // flux_hindenlang_gassner is the MHD flux
   if (vol == 0) return true;
-  if (vol == 1 || vol == 2) return vflux == 1 || vflux == 2;  // flux_ranocha, flux_central
+  if (vol == 1 || vol == 2) return vflux == 1 || vflux == 2 || vflux == 5;  // flux_ranocha, flux_central, flux_shima_etal
   return false;
 }
 
@@ -29,6 +29,7 @@ cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed,
     return cudaErrorNotSupported;
   }
   if (h.bc_kind >= 0 || h.src_kind != 0) {  // the instantiations with boundary states and sources
+    if (vflux == 5) return cudaErrorNotSupported;  // flux_shima_etal: periodic kernels only
     switch (dim) {
       case 1:
         return mixed ? launch_fused_1d_f32_bnd(N, eq, vol, vflux, h, s) : launch_fused_1d_f64_bnd(N, eq, vol, vflux, h, s);

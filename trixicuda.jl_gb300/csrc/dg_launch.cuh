@@ -115,11 +115,15 @@ cudaError_t launch_n(int eq, int vol, int vflux, const FusedHost &h, cudaStream_
   if (vol == VOL_FD) {
     if (vflux == FLUX_RANOCHA) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_RANOCHA, BND>(h, s);
     if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_CENTRAL, BND>(h, s);
+    if constexpr (!BND)
+      if (vflux == FLUX_SHIMA) return launch_one<DIM, N, EQ_EULER, R, VOL_FD, FLUX_SHIMA, BND>(h, s);
     return cudaErrorNotSupported;
   }
   if (vol == VOL_SC) {
     if (vflux == FLUX_RANOCHA) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_RANOCHA, BND>(h, s);
     if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_CENTRAL, BND>(h, s);
+    if constexpr (!BND)
+      if (vflux == FLUX_SHIMA) return launch_one<DIM, N, EQ_EULER, R, VOL_SC, FLUX_SHIMA, BND>(h, s);
   }
   return cudaErrorNotSupported;
 }

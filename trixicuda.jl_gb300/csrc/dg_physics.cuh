@@ -178,6 +178,12 @@ struct Physics<DIM, EQ_ADV, R> {
                                                 const PhysParams<R> &pp) {
     return dev_fabs(pp.a[O]);
   }
+  template <int O>
+  __device__ __forceinline__ static void min_max_speed(const R *, const R *, R &lmin, R &lmax,
+                                                       const PhysParams<R> &pp) {
+    lmin = pp.a[O];
+    lmax = pp.a[O];
+  }
 };
 
 template <int DIM, typename R>
@@ -237,6 +243,31 @@ struct Physics<DIM, EQ_EULER, R> {
     for (int d = 0; d < DIM; ++d) f[1 + d] = f0 * vavg[d] + (d == O ? pavg : R(0));
     f[DIM + 1] = f0 * (v2avg + inv_rho_p_mean * pp.inv_gm1) + R(0.5) * (pl * wr[1 + O] + pr * wl[1 + O]);
   }
+  // Shima, Kuya, Tamaki, Kawai (2021), "Preventing spurious pressure
+  // oscillations in split convective form discretization for compressible
+  // flows", JCP 427: the kinetic-energy and pressure-equilibrium preserving
+  // flux (arithmetic means; product mean of the kinetic energy; internal
+  // energy {{p}}{{v}}/(gamma-1); pressure work (p_l v_r + p_r v_l)/2).
+  template <int O>
+  __device__ __forceinline__ static void shima(const R *, const R *wl, const R *, const R *wr, R *f,
+                                               const PhysParams<R> &pp) {
+    const R rho_avg = R(0.5) * (wl[0] + wr[0]);
+    const R pl = wl[DIM + 1], pr = wr[DIM + 1];
+    const R p_avg = R(0.5) * (pl + pr);
+    R vavg[DIM];
+    R kin = R(0);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      vavg[d] = R(0.5) * (wl[1 + d] + wr[1 + d]);
+      kin += wl[1 + d] * wr[1 + d];
+    }
+    kin *= R(0.5);
+    const R f0 = rho_avg * vavg[O];
+    f[0] = f0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) f[1 + d] = f0 * vavg[d] + (d == O ? p_avg : R(0));
+    f[DIM + 1] = p_avg * vavg[O] * pp.inv_gm1 + f0 * kin + R(0.5) * (pl * wr[1 + O] + pr * wl[1 + O]);
+  }
   template <int O>
   __device__ __forceinline__ static void central(const R *ul, const R *wl, const R *ur, const R *wr, R *f,
                                                  const PhysParams<R> &pp) {
@@ -254,6 +285,16 @@ struct Physics<DIM, EQ_EULER, R> {
     if (naive) return dev_fmax(dev_fabs(wl[1 + O]), dev_fabs(wr[1 + O])) + dev_fmax(cl, cr);
     return dev_fmax(dev_fabs(wl[1 + O]) + cl, dev_fabs(wr[1 + O]) + cr);
   }
+  // naive signal-speed estimates of HLL: min(v_l - c_l, v_r - c_r), max(v_l + c_l, v_r + c_r)
+  template <int O>
+  __device__ __forceinline__ static void min_max_speed(const R *wl, const R *wr, R &lmin, R &lmax,
+                                                       const PhysParams<R> &pp) {
+    const R cl = dev_sqrt(dev_div(pp.gamma * wl[DIM + 1], wl[0]));
+    const R cr = dev_sqrt(dev_div(pp.gamma * wr[DIM + 1], wr[0]));
+    lmin = fminf_(wl[1 + O] - cl, wr[1 + O] - cr);
+    lmax = dev_fmax(wl[1 + O] + cl, wr[1 + O] + cr);
+  }
+  __device__ __forceinline__ static R fminf_(R a, R b) { return a < b ? a : b; }
 };
 
 // Ideal GLM-MHD (IdealGlmMhdEquations{1,2,3}D).  Conservative variables
@@ -397,6 +438,14 @@ struct Physics<DIM, EQ_MHD, R> {
     return dev_sqrt(R(0.5) * (s + dev_sqrt(s * s - R(4) * a2 * bo2)));
   }
   template <int O>
+  __device__ __forceinline__ static void min_max_speed(const R *wl, const R *wr, R &lmin, R &lmax,
+                                                       const PhysParams<R> &pp) {
+    const R cl = fast_speed<O>(wl, pp), cr = fast_speed<O>(wr, pp);
+    const R a = wl[1 + O] - cl, b = wr[1 + O] - cr;
+    lmin = a < b ? a : b;
+    lmax = dev_fmax(wl[1 + O] + cl, wr[1 + O] + cr);
+  }
+  template <int O>
   __device__ __forceinline__ static R max_speed(const R *, const R *wl, const R *, const R *wr, bool naive,
                                                 const PhysParams<R> &pp) {
     const R cl = fast_speed<O>(wl, pp), cr = fast_speed<O>(wr, pp);
@@ -434,6 +483,31 @@ __device__ __forceinline__ void ec_flux(const R *ul, const R *wl, const R *ur, c
   else P::template ranocha<O>(ul, wl, ur, wr, f, pp);
 }
 
+// HLL (Harten, Lax, van Leer 1983) with the naive signal-speed estimates:
+// f_l when lmin >= 0, f_r when lmax <= 0, else
+// (lmax f_l - lmin f_r + lmin lmax (u_r - u_l)) / (lmax - lmin).
+template <int DIM, int EQ, typename R, int O>
+__device__ __forceinline__ void hll_flux(const R *ul, const R *wl, const R *ur, const R *wr, R *f,
+                                         const PhysParams<R> &pp) {
+  using P = Physics<DIM, EQ, R>;
+  R lmin, lmax;
+  P::template min_max_speed<O>(wl, wr, lmin, lmax, pp);
+  R fl[P::NV], fr[P::NV];
+  P::template flux<O>(ul, wl, fl, pp);
+  P::template flux<O>(ur, wr, fr, pp);
+  if (lmin >= R(0)) {
+#pragma unroll
+    for (int v = 0; v < P::NV; ++v) f[v] = fl[v];
+  } else if (lmax <= R(0)) {
+#pragma unroll
+    for (int v = 0; v < P::NV; ++v) f[v] = fr[v];
+  } else {
+    const R inv = dev_rcp(lmax - lmin);
+#pragma unroll
+    for (int v = 0; v < P::NV; ++v) f[v] = (lmax * fl[v] - lmin * fr[v] + lmin * lmax * (ur[v] - ul[v])) * inv;
+  }
+}
+
 // Two-point flux dispatch (kind is warp-uniform).
 template <int DIM, int EQ, typename R, int O>
 __device__ __forceinline__ void two_point_flux(int kind, const R *ul, const R *wl, const R *ur, const R *wr, R *f,
@@ -441,6 +515,8 @@ __device__ __forceinline__ void two_point_flux(int kind, const R *ul, const R *w
   using P = Physics<DIM, EQ, R>;
   if (kind == FLUX_RANOCHA || kind == FLUX_HG) {
     ec_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
+  } else if (kind == FLUX_HLL) {
+    hll_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
   } else if (kind == FLUX_CENTRAL) {
     P::template central<O>(ul, wl, ur, wr, f, pp);
   } else {
@@ -458,6 +534,8 @@ __device__ __forceinline__ void two_point_flux_t(const R *ul, const R *wl, const
   using P = Physics<DIM, EQ, R>;
   if constexpr (KIND == FLUX_RANOCHA || KIND == FLUX_HG) {
     ec_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
+  } else if constexpr (KIND == FLUX_SHIMA && EQ == EQ_EULER) {
+    P::template shima<O>(ul, wl, ur, wr, f, pp);
   } else if constexpr (KIND == FLUX_CENTRAL) {
     P::template central<O>(ul, wl, ur, wr, f, pp);
   } else {

@@ -27,6 +27,8 @@ const FLUX_LAX_FRIEDRICHS = Int32(0)
 const FLUX_RANOCHA = Int32(1)
 const FLUX_CENTRAL = Int32(2)
 const FLUX_HINDENLANG_GASSNER = Int32(4)
+const FLUX_SHIMA_ETAL = Int32(5)
+const FLUX_HLL = Int32(6)
 const NONCONSERVATIVE_NONE = Int32(0)
 const NONCONSERVATIVE_POWELL = Int32(1)
 
@@ -86,6 +88,8 @@ flux_code(::typeof(Trixi.flux_ranocha)) = FLUX_RANOCHA
 flux_code(::typeof(Trixi.flux_central)) = FLUX_CENTRAL
 flux_code(::Trixi.FluxLaxFriedrichs) = FLUX_LAX_FRIEDRICHS
 flux_code(::typeof(Trixi.flux_hindenlang_gassner)) = FLUX_HINDENLANG_GASSNER
+flux_code(::typeof(Trixi.flux_shima_etal)) = FLUX_SHIMA_ETAL
+flux_code(::Trixi.FluxHLL) = FLUX_HLL
 # equations with nonconservative terms pass (flux, nonconservative_flux) tuples
 flux_code(f::Tuple) = flux_code(first(f))
 noncons_code(::Any) = NONCONSERVATIVE_NONE

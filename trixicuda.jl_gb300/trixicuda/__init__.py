@@ -21,10 +21,12 @@ from .equations import (
     flux,
     flux_central,
     flux_hindenlang_gassner,
+    flux_hll,
     flux_lax_friedrichs,
     flux_lax_friedrichs_naive,
     flux_nonconservative_powell,
     flux_ranocha,
+    flux_shima_etal,
     initial_condition_constant,
     initial_condition_convergence_test,
     initial_condition_fourier_advection,

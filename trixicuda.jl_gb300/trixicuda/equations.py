@@ -32,6 +32,8 @@ flux_central = NumericalFlux("flux_central", _lib.FLUX_CENTRAL)
 flux_lax_friedrichs_naive = NumericalFlux("flux_lax_friedrichs_naive", _lib.FLUX_LAX_FRIEDRICHS_NAIVE)
 flux = NumericalFlux("flux", -1)  # physical flux (weak form)
 flux_hindenlang_gassner = NumericalFlux("flux_hindenlang_gassner", _lib.FLUX_HINDENLANG_GASSNER)
+flux_shima_etal = NumericalFlux("flux_shima_etal", _lib.FLUX_SHIMA_ETAL)
+flux_hll = NumericalFlux("flux_hll", _lib.FLUX_HLL)
 
 
 @dataclass(frozen=True)
