@@ -258,7 +258,6 @@ __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const dou
   const int64_t e0 = (int64_t)blockIdx.x * WPB;
   const int64_t e = e0 + warp;
   R *a = s_iv + N * N + warp * 2 * NN, *b = a + NN;
-  R *coef = a;  // where this warp's modal coefficients end up
   if (e < E) {
     const R half = R(0.5), gm1 = R(gamma_ - 1.0);
     for (int n = lane; n < NN; n += 32) {
@@ -308,11 +307,9 @@ __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const dou
       dst = t;
       stride *= N;
     }
-    coef = src;
   }
-  // coefficient arrays alternate between a and b per dimension: after DIM
-  // passes they sit in a when DIM is even, in b when it is odd
-  (void)coef;
+  // the transform alternates between a and b per dimension: after DIM passes
+  // the coefficients sit in a when DIM is even, in b when it is odd
   __syncthreads();
   if (warp != 0) return;
   const int el = lane / 3, which = lane - 3 * (lane / 3);  // which: 0 all modes, 1 without the highest, 2 without two
