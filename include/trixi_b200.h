@@ -115,7 +115,7 @@ typedef struct trixi_problem_desc {
   double advection_velocity[3]; /* advection */
   double alpha_max, alpha_min;  /* IndicatorHennemannGassner */
   int32_t alpha_smooth;
-  int32_t indicator_variable;   /* 0 = density_pressure */
+  int32_t indicator_variable;   /* 0 = density_pressure, 1 = pressure */
   int64_t nelements;
   const double *inverse_jacobian;        /* [nelements] */
   int64_t ninterfaces;

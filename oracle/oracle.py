@@ -40,6 +40,7 @@ class OracleDesc(C.Structure):
         ("boundary_params", C.c_double * 8), ("source_params", C.c_double * 3),
         ("node_coordinates", C.POINTER(C.c_double)),
         ("nonconservative_flux", C.c_int32), ("glm_speed", C.c_double),
+        ("indicator_variable", C.c_int32),
     ]
 
 
@@ -109,7 +110,7 @@ class Oracle:
                  volume_integral=VOL_WEAK, volume_flux=FLUX_CENTRAL, surface_flux=FLUX_LLF,
                  volume_flux_fv=FLUX_LLF, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
                  boundary_function=-1, boundary_params=None, source_terms=0, source_params=None,
-                 nonconservative_flux=NONCONS_NONE, glm_speed=0.0):
+                 nonconservative_flux=NONCONS_NONE, glm_speed=0.0, indicator_variable=0):
         lib = load()
         self._keep = dict(
             inv=np.ascontiguousarray(containers.inverse_jacobian, dtype=np.float64),
@@ -150,6 +151,7 @@ class Oracle:
             d.source_params[i] = float(v)
         d.node_coordinates = _pd(k["coords"])
         d.nonconservative_flux, d.glm_speed = int(nonconservative_flux), float(glm_speed)
+        d.indicator_variable = int(indicator_variable)
         self._desc = d
         self._h = lib.oracle_create(C.byref(d))
         if not self._h:
@@ -173,7 +175,7 @@ class Oracle:
                   glm_speed=float(getattr(eq, "c_h", 0.0)))
         if isinstance(vi, VolumeIntegralShockCapturingHG):
             kw.update(alpha_max=vi.indicator.alpha_max, alpha_min=vi.indicator.alpha_min,
-                      alpha_smooth=vi.indicator.alpha_smooth)
+                      alpha_smooth=vi.indicator.alpha_smooth, indicator_variable=vi.indicator.variable_code)
         av = tuple(getattr(eq, "advection_velocity", np.zeros(eq.ndims)))
         # boundary function and source terms, with the library's parameters
         d = getattr(semi, "_desc", None)

@@ -934,7 +934,7 @@ void oracle_indicator_hg(oracle_handle *h, const double *u, double *alpha) {
       const double *un = u + NV * (n + (int64_t)NN * e);
       double rho, v[3], p;
       cons2prim(&h->P, un, &rho, v, &p);
-      ind[n] = rho * p;
+      ind[n] = h->d.indicator_variable ? p : rho * p;
     }
     /* modal coefficients: inverse Vandermonde applied dimension by dimension */
     for (int d = 0; d < DIM; ++d) {

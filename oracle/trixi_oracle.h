@@ -70,6 +70,7 @@ typedef struct {
    * fluxes (flux_nonconservative_powell) and the GLM cleaning speed c_h */
   int32_t nonconservative_flux;             /* ORC_NONCONS_* */
   double glm_speed;
+  int32_t indicator_variable;               /* 0: density_pressure (rho p), 1: pressure */
 } oracle_desc;
 
 typedef struct oracle_handle oracle_handle;

@@ -59,3 +59,22 @@ def test_coordinates_and_jacobian():
     e0 = c.node_coordinates[0]
     assert np.allclose(e0[0, :, 0], -2 + 0.25 * (b.nodes + 1))
     assert np.allclose(e0[:, 0, 1], -2 + 0.25 * (b.nodes + 1))
+
+
+def test_repeated_patches_are_balanced():
+    """Two identical refinement boxes (test/tree_dgsem_2d/euler_blob_mortar.jl):
+    the second level of refinement forces the coarse neighbours of the box
+    up one level, so faces differ by at most one level."""
+    import collections
+
+    mesh = T.TreeMesh((-32.0, -32.0), (32.0, 32.0), initial_refinement_level=4,
+                      refinement_patches=[dict(type="box", coordinates_min=(-40.0, -5.0),
+                                               coordinates_max=(40.0, 5.0))] * 2)
+    levels = collections.Counter(c[0] for c in mesh.elements)
+    # 32 level-4 cells in the box -> 128 level 5 -> 512 level 6; the 32 level-4
+    # rows next to it are refined once to keep the 2:1 balance
+    assert levels == {4: 192, 5: 128, 6: 512}
+    mesh._check_balance()
+    cont = mesh.build_containers(np.array([-1.0, 1.0]))
+    area = np.sum((1.0 / cont.inverse_jacobian) ** 2 * 4.0)  # J = h/2 per dimension, reference square of area 4
+    assert np.isclose(area, 64.0 * 64.0)

@@ -247,7 +247,7 @@ template <int DIM, int N, typename R>
 __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const double *__restrict__ u,
                                                             double *__restrict__ alpha_raw, double gamma_, double amax,
                                                             double amin, double threshold_, double param_s_,
-                                                            IvdmMat ivdm, int mhd, int nv) {
+                                                            IvdmMat ivdm, int mhd, int nv, int variable) {
   constexpr int NN = (DIM == 1) ? N : (DIM == 2 ? N * N : N * N * N);
   constexpr int WPB = 8;  // warps (elements) per block
   extern __shared__ __align__(16) unsigned char sm_raw[];
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const dou
         }
         p = gm1 * (ind_load<R>(un + DIM + 1) - half * kin);
       }
-      a[n] = rho * p;
+      a[n] = variable ? p : rho * p;  // pressure or density_pressure
     }
     __syncwarp();
     R *src = a, *dst = b;
@@ -349,12 +349,12 @@ static cudaError_t launch_indicator_raw(const IndicatorHost &ih, cudaStream_t s)
     const size_t smem = sizeof(float) * (size_t)(N * N + 8 * 2 * NN);
     indicator_raw_kernel<DIM, N, float><<<(unsigned)grid, 256, smem, s>>>(
         ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
-        ih.eq == EQ_MHD ? 1 : 0, ih.nv);
+        ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable);
   } else {
     const size_t smem = sizeof(double) * (size_t)(N * N + 8 * 2 * NN);
     indicator_raw_kernel<DIM, N, double><<<(unsigned)grid, 256, smem, s>>>(
         ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
-        ih.eq == EQ_MHD ? 1 : 0, ih.nv);
+        ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable);
   }
   return cudaGetLastError();
 }

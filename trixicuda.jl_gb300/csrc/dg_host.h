@@ -106,6 +106,7 @@ cudaError_t launch_mortar_flux(const MortarHost &m, cudaStream_t s);
 struct IndicatorHost {
   int dim = 2, N = 0, nv = 4, eq = 1;
   bool mixed = false;  // FP32 arithmetic (the FP32-mixed rhs), else FP64
+  int variable = 0;    // 0: density_pressure, 1: pressure
   int64_t nelements = 0;
   const double *u = nullptr;
   double *alpha_raw = nullptr;

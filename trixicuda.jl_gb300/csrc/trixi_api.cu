@@ -77,6 +77,7 @@ struct trixi_handle {
   double c_h = 0.0;  // GLM cleaning speed (ideal GLM-MHD)
   double alpha_max = 0.5, alpha_min = 0.001;
   int alpha_smooth = 1;
+  int ind_var = 0;  // indicator variable: 0 density_pressure, 1 pressure
   int64_t E = 0, I = 0, M = 0, B = 0;
   Basis basis;
   // non-periodic meshes and source terms
@@ -260,6 +261,8 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
     return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: periodic meshes without source terms");
   if (mhd && d->volume_integral == TRIXI_VOLUME_WEAK_FORM)
     return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: flux differencing or shock capturing");
+  if (d->volume_integral == TRIXI_VOLUME_SHOCK_CAPTURING_HG && d->indicator_variable != 0 && d->indicator_variable != 1)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "indicator_variable %d", d->indicator_variable);
   if (d->precision != TRIXI_PRECISION_FP64 && d->precision != TRIXI_PRECISION_MIXED)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "precision %d", d->precision);
   if (d->nelements <= 0 || d->nelements > INT32_MAX)
@@ -310,6 +313,7 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   h->alpha_max = d->alpha_max;
   h->alpha_min = d->alpha_min;
   h->alpha_smooth = d->alpha_smooth;
+  h->ind_var = d->volume_integral == TRIXI_VOLUME_SHOCK_CAPTURING_HG ? d->indicator_variable : 0;
   h->E = d->nelements;
   h->I = d->ninterfaces;
   h->M = d->nmortars;
@@ -528,6 +532,7 @@ int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStrea
   ih.nv = h->nv;
   ih.eq = h->eq;
   ih.mixed = fp32;
+  ih.variable = h->ind_var;
   ih.nelements = h->E;
   ih.u = u;
   ih.alpha_raw = h->d_alpha_raw;
@@ -1218,18 +1223,20 @@ int batch_fail(trixi_batch *b, int status, const std::string &msg) {
 struct KindKey {
   int32_t ndims, polydeg, eq, vol, vflux, sflux, fvflux, precision;
   double gamma, a0, a1, a2, amax, amin;
-  int32_t smooth;
+  int32_t smooth, ind_var;
   bool operator==(const KindKey &o) const {
     return ndims == o.ndims && polydeg == o.polydeg && eq == o.eq && vol == o.vol && vflux == o.vflux &&
            sflux == o.sflux && fvflux == o.fvflux && precision == o.precision && gamma == o.gamma && a0 == o.a0 &&
-           a1 == o.a1 && a2 == o.a2 && amax == o.amax && amin == o.amin && smooth == o.smooth;
+           a1 == o.a1 && a2 == o.a2 && amax == o.amax && amin == o.amin && smooth == o.smooth &&
+           ind_var == o.ind_var;
   }
 };
 
 KindKey key_of(const trixi_problem_desc *d) {
   return KindKey{d->ndims, d->polydeg, d->equation, d->volume_integral, d->volume_flux, d->surface_flux,
                  d->volume_flux_fv, d->precision, d->gamma, d->advection_velocity[0], d->advection_velocity[1],
-                 d->advection_velocity[2], d->alpha_max, d->alpha_min, d->alpha_smooth};
+                 d->advection_velocity[2], d->alpha_max, d->alpha_min, d->alpha_smooth,
+                 d->volume_integral == TRIXI_VOLUME_SHOCK_CAPTURING_HG ? d->indicator_variable : 0};
 }
 
 void destroy_graphs(trixi_batch *b) {

@@ -115,12 +115,13 @@ function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
     basis = solver.basis
     vi = solver.volume_integral
     vol, vflux, fvflux = VOLUME_WEAK_FORM, FLUX_CENTRAL, FLUX_LAX_FRIEDRICHS
-    amax, amin, asmooth = 0.5, 0.001, Int32(1)
+    amax, amin, asmooth, indvar = 0.5, 0.001, Int32(1), Int32(0)
     if vi isa Trixi.VolumeIntegralFluxDifferencing
         vol, vflux = VOLUME_FLUX_DIFFERENCING, flux_code(vi.volume_flux)
     elseif vi isa Trixi.VolumeIntegralShockCapturingHG
         vol, vflux, fvflux = VOLUME_SHOCK_CAPTURING_HG, flux_code(vi.volume_flux_dg), flux_code(vi.volume_flux_fv)
         amax, amin, asmooth = vi.indicator.alpha_max, vi.indicator.alpha_min, Int32(vi.indicator.alpha_smooth)
+        indvar = vi.indicator.variable === Trixi.pressure ? Int32(1) : Int32(0)
     end
     eq = equations isa Trixi.AbstractCompressibleEulerEquations ? EQ_COMPRESSIBLE_EULER :
          equations isa Trixi.AbstractIdealGlmMhdEquations ? EQ_IDEAL_GLM_MHD : EQ_LINEAR_ADVECTION
@@ -139,7 +140,7 @@ function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
     # neighbor_sides and orientations and the Dirichlet function's kind
     desc = ProblemDesc(0, ndims(mesh), Trixi.polydeg(basis), nvariables(equations), eq, vol, vflux,
                        flux_code(solver.surface_integral.surface_flux), fvflux, Int32(precision), gamma, adv,
-                       amax, amin, asmooth, Int32(0),
+                       amax, amin, asmooth, indvar,
                        nelements(elements), pointer(elements.inverse_jacobian),
                        ninterfaces(interfaces), pointer(interfaces.neighbor_ids), pointer(interfaces.orientations),
                        0, Trixi.nmortars(mortars), pointer(mortars.neighbor_ids), pointer(mortars.large_sides),

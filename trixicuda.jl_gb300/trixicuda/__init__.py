@@ -74,6 +74,7 @@ from .solver import (
     VolumeIntegralShockCapturingHG,
     VolumeIntegralWeakForm,
     density_pressure,
+    pressure,
 )
 from .time_integration import CarpenterKennedy2N54, solve
 

@@ -8,8 +8,10 @@ GPU (src/solvers/cache.jl:60-88, containers_{1,2,3}d.jl):
   depth-first order with children in Morton order (x bit fastest), which for
   uniform refinement is the order of Trixi's cell ids;
 * `refinement_patches` of type "box" refine every leaf whose centre lies in
-  the box (one extra level per patch, the mesh stays 2:1 balanced for the
-  patches used here);
+  the box (one extra level per patch); after each patch, coarser leaves are
+  refined until every face neighbour differs by at most one level (2:1
+  balance across faces, periodic wrap included), as Trixi's `refine!` keeps
+  its trees;
 * interfaces between equal-size neighbours: neighbor_ids[:, k] = (left,
   right) along orientation k (1-based), one interface per +direction face;
 * L2 mortars where a leaf faces a refined neighbour: neighbor_ids = small
@@ -106,6 +108,7 @@ class TreeMesh:
                 c = self.cell_center(leaf)
                 if np.all(c >= bmin) and np.all(c <= bmax):
                     self._refine(leaf)
+            self._balance()
         if n_cells_max is not None and len(self.cells) > n_cells_max:
             raise ValueError(f"mesh needs {len(self.cells)} cells > n_cells_max={n_cells_max}")
         self._check_balance()
@@ -156,6 +159,28 @@ class TreeMesh:
                 return None
             cc[dim] %= n
         return (level, tuple(cc))
+
+    def _unbalanced(self, leaf):
+        """True if a leaf face-neighbour of `leaf` is two or more levels finer."""
+        for d in range(self.ndims):
+            for side in (-1, 1):
+                nb = self._neighbor_cell(leaf, d, side)
+                if nb is not None and nb in self.cells and nb not in self.leaves:
+                    for ch in self._face_children(nb, d, side):
+                        if ch not in self.leaves:
+                            return True
+        return False
+
+    def _balance(self):
+        """Refine leaves until the mesh is 2:1 balanced across faces (the
+        minimal such refinement; the result does not depend on the order)."""
+        changed = True
+        while changed:
+            changed = False
+            for leaf in sorted(self.leaves):
+                if leaf in self.leaves and self._unbalanced(leaf):
+                    self._refine(leaf)
+                    changed = True
 
     def _check_balance(self):
         for leaf in self.leaves:

@@ -125,6 +125,7 @@ def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver:
         d.alpha_max = vi.indicator.alpha_max
         d.alpha_min = vi.indicator.alpha_min
         d.alpha_smooth = int(bool(vi.indicator.alpha_smooth))
+        d.indicator_variable = vi.indicator.variable_code
     if precision not in ("fp64", "mixed"):
         raise ValueError("precision must be 'fp64' or 'mixed'")
     d.precision = _lib.PRECISION_MIXED if precision == "mixed" else _lib.PRECISION_FP64
@@ -133,7 +134,6 @@ def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver:
     av[: equations.ndims] = getattr(equations, "advection_velocity", np.zeros(equations.ndims))
     for i in range(3):
         d.advection_velocity[i] = av[i]
-    d.indicator_variable = 0
     keep = dict(
         inverse_jacobian=np.ascontiguousarray(cont.inverse_jacobian, dtype=np.float64),
         if_nid=np.ascontiguousarray(cont.interface_neighbor_ids, dtype=np.int64),

@@ -34,6 +34,14 @@ def density_pressure(u, equations):
     return rho * p
 
 
+def pressure(u, equations):
+    return equations.cons2prim(u)[2]
+
+
+# indicator variables the library evaluates (trixi_problem_desc.indicator_variable)
+INDICATOR_VARIABLES = {density_pressure: 0, pressure: 1}
+
+
 @dataclass
 class IndicatorHennemannGassner:
     """Hennemann-Gassner shock indicator (Trixi's IndicatorHennemannGassner,
@@ -46,8 +54,12 @@ class IndicatorHennemannGassner:
     variable: object = density_pressure
 
     def __post_init__(self):
-        if self.variable is not density_pressure:
-            raise NotImplementedError("only variable=density_pressure is supported")
+        if self.variable not in INDICATOR_VARIABLES:
+            raise NotImplementedError("indicator variable: density_pressure or pressure")
+
+    @property
+    def variable_code(self) -> int:
+        return INDICATOR_VARIABLES[self.variable]
 
 
 @dataclass
