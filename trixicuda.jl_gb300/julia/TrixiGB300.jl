@@ -13,6 +13,7 @@ module TrixiGB300
 
 using CUDA
 using Trixi
+using ChainRulesCore
 
 const libtrixi = get(ENV, "TRIXI_B200_LIB", joinpath(@__DIR__, "..", "_build", "libtrixi_b200.so"))
 
@@ -188,6 +189,55 @@ cuda_surface_integral!(du, handle) =
 cuda_jacobian!(du, handle) =
     check(ccall((:trixi_jacobian, libtrixi), Cint, (Ptr{Cvoid}, CuPtr{Float64}, Ptr{Cvoid}),
                 handle, pointer(du), stream_ptr()))
+
+# ---- discrete adjoint as ChainRulesCore rules --------------------------------
+# The Julia counterpart of trixicuda/adjoint.py's torch.autograd.Functions:
+# Zygote (or any ChainRules-aware AD) differentiates through the library's
+# hand-written reverse kernels instead of tracing Julia code.
+
+"du = rhs(u): one fused rhs evaluation (t = 0)."
+function rhs(u::CuArray{Float64}, handle::Ptr{Cvoid})
+    du = similar(u)
+    rhs_gpu!(du, u, handle, 0.0)
+    return du
+end
+
+function ChainRulesCore.rrule(::typeof(rhs), u::CuArray{Float64}, handle::Ptr{Cvoid})
+    du = rhs(u, handle)
+    function rhs_pullback(dū)
+        λ = CuArray{Float64}(unthunk(dū))
+        ū = similar(u)
+        check(ccall((:trixi_rhs_vjp, libtrixi), Cint,
+                    (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, CuPtr{Float64}, Ptr{Cvoid}),
+                    handle, pointer(ū), pointer(u), pointer(λ), stream_ptr()))
+        return NoTangent(), ū, NoTangent()
+    end
+    return du, rhs_pullback
+end
+
+"uT = ck2n54(u0, dt, nsteps, nsnapshots, handle): nsteps CarpenterKennedy2N54 steps."
+function ck2n54(u0::CuArray{Float64}, dt, nsteps, nsnapshots, handle::Ptr{Cvoid})
+    uT = similar(u0)
+    check(ccall((:trixi_adjoint_forward, libtrixi), Cint,
+                (Ptr{Cvoid}, CuPtr{Float64}, Float64, Int64, Int64, CuPtr{Float64}, Ptr{Cvoid}),
+                handle, pointer(u0), Float64(dt), Int64(nsteps), Int64(nsnapshots), pointer(uT), stream_ptr()))
+    return uT
+end
+
+# reverse sweep over the stored (binomial) checkpoints, recomputing the rest
+function ChainRulesCore.rrule(::typeof(ck2n54), u0::CuArray{Float64}, dt, nsteps, nsnapshots, handle::Ptr{Cvoid})
+    uT = ck2n54(u0, dt, nsteps, nsnapshots, handle)
+    function ck2n54_pullback(ūT)
+        g = CuArray{Float64}(unthunk(ūT))
+        ū0 = similar(u0)
+        recomputed = Ref{Int64}(0)
+        check(ccall((:trixi_adjoint_backward, libtrixi), Cint,
+                    (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, Ref{Int64}, Ptr{Cvoid}),
+                    handle, pointer(g), pointer(ū0), recomputed, stream_ptr()))
+        return NoTangent(), ū0, NoTangent(), NoTangent(), NoTangent(), NoTangent()
+    end
+    return uT, ck2n54_pullback
+end
 
 # GlmSpeedCallback: equations.c_h changed between steps
 set_glm_speed!(handle, c_h) =
