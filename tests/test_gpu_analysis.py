@@ -149,3 +149,29 @@ def test_error_norms(cuda):
         errinf = max(errinf, np.max(np.abs(ex - ua)))
     assert abs(l2[0] - np.sqrt(err2 / 4.0)) < 1e-12 * l2[0] + 1e-16
     assert abs(linf[0] - errinf) < 1e-12
+
+
+def test_integrals_are_compensated(cuda):
+    """The quadrature sums carry their rounding errors (TwoSum/TwoProduct):
+    with +-1e16 on the two end nodes of every element (equal LGL weights up to
+    their last bit) and O(1) values between, a plain FP64 sum loses the O(1)
+    part entirely; the compensated sum matches the exact rational result."""
+    from fractions import Fraction
+
+    mesh = T.TreeMesh(-1.0, 1.0, initial_refinement_level=4)
+    eq = T.LinearScalarAdvectionEquation1D(1.0)
+    solver = T.DGSEMGPU(polydeg=3, surface_flux=T.flux_lax_friedrichs)
+    semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, T.initial_condition_convergence_test, solver)
+    E = semi.nelements
+    u_host = np.ones((E, 4, 1))
+    u_host[:, 0, 0] = 1.0e16
+    u_host[:, 3, 0] = -1.0e16
+    u = cuda.from_numpy(u_host).to(semi.device)
+    got = T.integrate(u, semi, "state")[0]
+    w = semi.solver.basis.weights
+    J = 1.0 / semi.containers.inverse_jacobian
+    exact = sum(Fraction(J[e]) * sum(Fraction(w[n]) * Fraction(u_host[e, n, 0]) for n in range(4)) for e in range(E))
+    assert abs(Fraction(got) - exact) <= Fraction(1, 10 ** 14) * abs(exact), (got, float(exact))
+    # a plain left-to-right FP64 sum per element is far off
+    plain = sum(J[e] * sum(w[n] * u_host[e, n, 0] for n in range(4)) for e in range(E))
+    assert abs(plain - float(exact)) > 1e-3 * abs(float(exact))

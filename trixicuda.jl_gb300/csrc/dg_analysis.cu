@@ -165,6 +165,49 @@ __device__ void quantity(int which, const double *un, const double *dun, double 
   q[0] = acc;
 }
 
+// Compensated (double-double) accumulation for the quadrature integrals:
+// error-free TwoSum (Knuth) and TwoProduct (by FMA) keep the rounding errors
+// of every product and partial sum in a second word, so conservation and
+// entropy integrals, sums of terms that cancel, come out correct to the last
+// bits instead of to the size of the largest term (Ogita, Rump, Oishi, "Accurate
+// sum and dot product", SIAM J. Sci. Comput. 26 (2005)).
+struct Dd {
+  double hi, lo;
+};
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+  s = __dadd_rn(a, b);
+  const double bp = __dsub_rn(s, a);
+  e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bp)), __dsub_rn(b, bp));
+}
+__device__ __forceinline__ void dd_add(Dd &acc, double x) {  // acc += x
+  double s, e;
+  two_sum(acc.hi, x, s, e);
+  acc.hi = s;
+  acc.lo = __dadd_rn(acc.lo, e);
+}
+__device__ __forceinline__ void dd_add_prod(Dd &acc, double a, double b) {  // acc += a b
+  const double p = __dmul_rn(a, b);
+  const double pe = fma(a, b, -p);  // exact error of the product
+  dd_add(acc, p);
+  acc.lo = __dadd_rn(acc.lo, pe);
+}
+__device__ __forceinline__ void dd_merge(Dd &acc, const Dd &o) {
+  double s, e;
+  two_sum(acc.hi, o.hi, s, e);
+  acc.hi = s;
+  acc.lo = __dadd_rn(__dadd_rn(acc.lo, o.lo), e);
+}
+// a warp-wide compensated sum, the result in every lane
+__device__ __forceinline__ Dd dd_warp_sum(Dd v) {
+  for (int off = 16; off > 0; off >>= 1) {
+    Dd o;
+    o.hi = __shfl_xor_sync(0xffffffffu, v.hi, off);
+    o.lo = __shfl_xor_sync(0xffffffffu, v.lo, off);
+    dd_merge(v, o);
+  }
+  return v;
+}
+
 template <int DIM, int EQ>
 __global__ void integrate_kernel(int N, int64_t E, const double *__restrict__ u, const double *__restrict__ du,
                                  const double *__restrict__ inv_jac, const double *__restrict__ w, int which,
@@ -174,8 +217,8 @@ __global__ void integrate_kernel(int N, int64_t E, const double *__restrict__ u,
   const int lane = threadIdx.x & 31;
   if (e >= E) return;
   const int NN = nodes_per_elem<DIM>(N);
-  double acc[NV];
-  for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+  Dd acc[NV];
+  for (int k = 0; k < NV; ++k) acc[k] = Dd{0.0, 0.0};
   for (int n = lane; n < NN; n += 32) {
     int r = n;
     double wt = 1.0;
@@ -185,14 +228,13 @@ __global__ void integrate_kernel(int N, int64_t E, const double *__restrict__ u,
     }
     double q[NV];
     quantity<DIM, EQ>(which, u + (e * NN + n) * NV, du ? du + (e * NN + n) * NV : nullptr, gamma, q);
-    for (int k = 0; k < nq; ++k) acc[k] += wt * q[k];
+    for (int k = 0; k < nq; ++k) dd_add_prod(acc[k], wt, q[k]);
   }
   double J = 1.0;
   for (int d = 0; d < DIM; ++d) J /= inv_jac[e];
   for (int k = 0; k < nq; ++k) {
-    double v = acc[k];
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    if (lane == 0) partial[e * nq + k] = v * J;
+    const Dd v = dd_warp_sum(acc[k]);
+    if (lane == 0) partial[e * nq + k] = fma(J, v.hi, J * v.lo);
   }
 }
 
@@ -210,8 +252,8 @@ __global__ void integrate_w_kernel(int N, int64_t E, const double *__restrict__ 
   const int lane = threadIdx.x & 31;
   if (e >= E) return;
   const int NN = nodes_per_elem<DIM>(N);
-  double acc[NV];
-  for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+  Dd acc[NV];
+  for (int k = 0; k < NV; ++k) acc[k] = Dd{0.0, 0.0};
   for (int n = lane; n < NN; n += 32) {
     int r = n;
     double wt = 1.0;
@@ -221,34 +263,44 @@ __global__ void integrate_w_kernel(int N, int64_t E, const double *__restrict__ 
     }
     double q[NV];
     quantity<DIM, EQ>(which, u + (e * NN + n) * NV, du ? du + (e * NN + n) * NV : nullptr, gamma, q);
-    for (int k = 0; k < nq; ++k) acc[k] += wt * q[k];
+    for (int k = 0; k < nq; ++k) dd_add_prod(acc[k], wt, q[k]);
   }
   double J = 1.0;
   for (int d = 0; d < DIM; ++d) J /= inv_jac[e];
   for (int k = 0; k < nq; ++k) {
-    double v = acc[k];
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    if (lane == 0) partial[e * nq + k] = v * J;
+    const Dd v = dd_warp_sum(acc[k]);
+    if (lane == 0) partial[e * nq + k] = fma(J, v.hi, J * v.lo);
   }
 }
 
-// one block: deterministic sum (op 0) or max (op 1) of partial[E][nq] per column
+// one block: deterministic compensated sum (op 0) or max (op 1) of
+// partial[E][nq] per column
 __global__ void reduce_columns(int64_t E, int nq, const double *__restrict__ partial, int op, double *__restrict__ out) {
-  __shared__ double sm[1024];
+  __shared__ double sm_hi[1024], sm_lo[1024];
   for (int k = 0; k < nq; ++k) {
-    double v = (op == 0) ? 0.0 : 0.0;
+    Dd v{0.0, 0.0};
     for (int64_t e = threadIdx.x; e < E; e += blockDim.x) {
       const double x = partial[e * nq + k];
-      v = (op == 0) ? v + x : fmax(v, x);
+      if (op == 0) dd_add(v, x);
+      else v.hi = fmax(v.hi, x);
     }
-    sm[threadIdx.x] = v;
+    sm_hi[threadIdx.x] = v.hi;
+    sm_lo[threadIdx.x] = v.lo;
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) sm[threadIdx.x] = (op == 0) ? sm[threadIdx.x] + sm[threadIdx.x + s]
-                                                      : fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+      if (threadIdx.x < s) {
+        if (op == 0) {
+          Dd a{sm_hi[threadIdx.x], sm_lo[threadIdx.x]};
+          dd_merge(a, Dd{sm_hi[threadIdx.x + s], sm_lo[threadIdx.x + s]});
+          sm_hi[threadIdx.x] = a.hi;
+          sm_lo[threadIdx.x] = a.lo;
+        } else {
+          sm_hi[threadIdx.x] = fmax(sm_hi[threadIdx.x], sm_hi[threadIdx.x + s]);
+        }
+      }
       __syncthreads();
     }
-    if (threadIdx.x == 0) out[k] = sm[0];
+    if (threadIdx.x == 0) out[k] = (op == 0) ? sm_hi[0] + sm_lo[0] : sm_hi[0];
     __syncthreads();
   }
 }
