@@ -559,6 +559,7 @@ def main():
             r["hbm_frac"] = r["achieved_gbs"] / hbm_peak
     adjoint = None if args.no_adjoint else adjoint_path(device)
     c3 = None if args.no_c3 else c3_path(max(3, args.steps // 4), 3, device, flush, hbm_peak)
+    c1 = c1_path(device)
     cpu = None if args.no_cpu_baseline or rank != 0 else cpu_baseline()
     traffic = None
     prof = ROOT / "profiles" / "traffic_fused_rk_stage_euler2d_l7.json"
@@ -588,6 +589,7 @@ def main():
         "batched": batched,
         "adjoint": adjoint,
         "shock_capturing_3d": c3,
+        "advection_1d": c1,
         "cpu_baseline": cpu,
         "gpu_launches": 5 * args.steps,
         "clocks": clocks,
@@ -604,8 +606,10 @@ def c3_path(steps, warmup, device, flush, hbm_peak):
     DOFs, 84 MB FP64 state), FP32-mixed and FP64, tuned tiles.  Each RK stage
     is the indicator (two small kernels) and the fused stage kernel."""
     out = {"workload": C3_WORKLOAD}
+    semis = {}
     for prec in ("mixed", "fp64"):
-        step_ms, stage_ms, semi, _, _ = time_gpu_path(prec, steps, warmup, device, flush, c3=True)
+        step_ms, stage_ms, semi, _, dt = time_gpu_path(prec, steps, warmup, device, flush, c3=True)
+        semis[prec] = (semi, dt)
         dofs, nv, E = semi.ndofs(), semi.equations.nvariables, semi.nelements
         nval = dofs * nv
         # algorithmic bytes of one stage: the fused kernel reads u, k and writes u_out, k
@@ -618,6 +622,39 @@ def c3_path(steps, warmup, device, flush, hbm_peak):
         out[prec] = {"value": 5 * dofs / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms,
                      "mean_stage_ms": statistics.mean(stage_ms), "algorithmic_bytes_per_stage": stage_bytes,
                      "achieved_gbs": ach, "hbm_frac": ach / hbm_peak, "tile": _tile_report(semi)}
+    # FP32-mixed against FP64 after 50 steps from the same state
+    out["equal_l2"] = l2_mixed_vs_fp64(semis["mixed"][0], semis["fp64"][0], semis["fp64"][1], nsteps=50)
+    return out
+
+
+def c1_path(device):
+    """The 1D advection configuration (a = 1 on [-1, 1], level 4, polydeg 3,
+    weak form, flux_lax_friedrichs, u0 = 1 + 0.5 sin(pi x), CK2N54 to t = 1 at
+    CFL 1.6): FP32-mixed against FP64 and both against the exact solution."""
+    import torch
+
+    import trixicuda as T
+
+    out = {"workload": "1D linear advection, a = 1, [-1, 1] periodic level 4 (16 elements), polydeg 3, "
+                       "weak form, flux_lax_friedrichs, CarpenterKennedy2N54 to t = 1 at CFL 1.6"}
+    mesh = T.TreeMesh(-1.0, 1.0, initial_refinement_level=4)
+    eq = T.LinearScalarAdvectionEquation1D(1.0)
+    solver = T.DGSEMGPU(polydeg=3, surface_flux=T.flux_lax_friedrichs)
+    semis = {p: T.SemidiscretizationHyperbolicGPU(mesh, eq, T.initial_condition_convergence_test, solver,
+                                                  precision=p) for p in ("fp64", "mixed")}
+    u0 = semis["fp64"].compute_coefficients()
+    dt0 = 1.6 * T.max_dt(u0, semis["fp64"])
+    nsteps = int(np.ceil(1.0 / dt0))
+    dt = 1.0 / nsteps
+    out["equal_l2"] = l2_mixed_vs_fp64(semis["mixed"], semis["fp64"], dt, nsteps)
+    x = semis["fp64"].containers.node_coordinates.reshape(-1, 1).T
+    exact = T.initial_condition_convergence_test(x, 1.0, eq).T.reshape(u0.shape)
+    for p, sm in semis.items():
+        u, k = u0.clone(), torch.zeros_like(u0)
+        T.rk_steps(u, k, 0.0, dt, nsteps, sm)
+        torch.cuda.synchronize()
+        err = u.cpu().numpy() - exact
+        out[f"error_vs_exact_{p}"] = {"l2": float(np.sqrt(np.mean(err ** 2))), "linf": float(np.max(np.abs(err)))}
     return out
 
 
