@@ -202,7 +202,8 @@ int trixi_rk_stage(trixi_handle *h, double *u_out, const double *u_in, double *k
                    double a, double b, double dt, double t, void *stream);
 
 /* nsteps CarpenterKennedy2N54 steps of size dt from time t, in place in u
- * (k is the 2N register).  Ping-pongs with a library-owned buffer. */
+ * (k is the 2N register).  The stages of a step run u -> s1 -> s2 -> s1 -> s2
+ * -> u through two library-owned buffers, so no copy is needed. */
 int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt,
                    int64_t nsteps, void *stream);
 

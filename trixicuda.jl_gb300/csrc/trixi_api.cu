@@ -95,7 +95,7 @@ struct trixi_handle {
   double *d_mortar_flux = nullptr;
   double *d_alpha_raw = nullptr, *d_alpha = nullptr;
   int *d_err = nullptr;
-  double *d_scratch_u = nullptr;
+  double *d_scratch_u = nullptr, *d_scratch_u2 = nullptr;  // RK stage buffers of trixi_rk_steps
   // stage containers (allocated on first use)
   double *d_interfaces_u = nullptr, *d_sfv = nullptr, *d_mortar_u[4] = {nullptr, nullptr, nullptr, nullptr};
   // analysis / initial conditions (allocated on first use)
@@ -167,7 +167,7 @@ void free_all(trixi_handle *h) {
   free_adjoint(h);
   void *ptrs[] = {h->d_face_table, h->d_slot_nbrs, h->d_inv_jac, h->d_if_nid, h->d_if_ori, h->d_mo_nid,
                   h->d_mo_ls, h->d_mo_ori, h->d_mortar_flux, h->d_alpha_raw, h->d_alpha, h->d_err,
-                  h->d_scratch_u, h->d_interfaces_u, h->d_sfv, h->d_mortar_u[0], h->d_mortar_u[1],
+                  h->d_scratch_u, h->d_scratch_u2, h->d_interfaces_u, h->d_sfv, h->d_mortar_u[0], h->d_mortar_u[1],
                   h->d_mortar_u[2], h->d_mortar_u[3], h->d_coords, h->d_acc, h->d_partial, h->d_partial2,
                   h->d_red_out, h->d_vdm, h->d_wa, h->d_w, h->d_bnd_nid, h->d_bnd_side, h->d_bnd_ori,
                   h->d_boundaries_u};
@@ -752,16 +752,17 @@ int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt, i
   cudaStream_t s = (cudaStream_t)stream;
   const size_t bytes = sizeof(double) * (size_t)(h->E * h->NN * h->nv);
   if (!h->d_scratch_u) TRIXI_CUDA(h, cudaMalloc(&h->d_scratch_u, bytes), "alloc RK scratch");
-  double *cur = u, *nxt = h->d_scratch_u;
+  if (!h->d_scratch_u2) TRIXI_CUDA(h, cudaMalloc(&h->d_scratch_u2, bytes), "alloc RK scratch");
+  // the stage inputs and outputs of one step: u -> s1 -> s2 -> s1 -> s2 -> u, so
+  // that every step ends in the caller's buffer (u_out never aliases u_in)
+  double *const seq[6] = {u, h->d_scratch_u, h->d_scratch_u2, h->d_scratch_u, h->d_scratch_u2, u};
   for (int64_t step = 0; step < nsteps; ++step) {
     for (int st = 0; st < 5; ++st) {
-      int r = run_rhs(h, MODE_RK, cur, nxt, k, kCK_A[st], kCK_B[st], dt, s, t + kCK_C[st] * dt);
+      int r = run_rhs(h, MODE_RK, seq[st], seq[st + 1], k, kCK_A[st], kCK_B[st], dt, s, t + kCK_C[st] * dt);
       if (r) return r;
-      std::swap(cur, nxt);
     }
     t += dt;
   }
-  if (cur != u) TRIXI_CUDA(h, cudaMemcpyAsync(u, cur, bytes, cudaMemcpyDeviceToDevice, s), "RK copy back");
   return TRIXI_OK;
 }
 
