@@ -222,7 +222,14 @@ struct FusedKernel {
   static constexpr int NF = ipow(N, DIM - 1);
   static constexpr int NP = N * (N - 1) / 2;
   // staged fluxes per element and direction
-  static constexpr int VOL_PER_DIR = (VOL == VOL_WEAK) ? NN : NF * NP;
+  // Linear advection: its volume fluxes (a_d u, and the central pair flux
+  // a_d {{u}}) cost a multiply, so phase C forms them from the node records
+  // and phase B stages none -- in the weak form, and in flux differencing in
+  // FP32 (measured: 3D N=4 FP32 78 -> 53 us; in FP64 the staged pairs were
+  // 10 % faster).  The other systems stage one flux per node and direction
+  // (weak form) or per pair (flux differencing).
+  static constexpr bool LINEAR = (EQ == EQ_ADV) && (VOL == VOL_WEAK || sizeof(R) == 4);
+  static constexpr int VOL_PER_DIR = LINEAR ? 0 : (VOL == VOL_WEAK) ? NN : NF * NP;
   static constexpr int SURF_PER_EL = 2 * DIM * NF;
   static constexpr int FV_PER_DIR = (VOL == VOL_SC) ? NF * (N - 1) : 0;
   static constexpr int ITEMS_PER_EL = DIM * VOL_PER_DIR + SURF_PER_EL + DIM * FV_PER_DIR;
@@ -593,7 +600,28 @@ struct FusedKernel {
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const int ci = coord[d];
-      if constexpr (VOL == VOL_WEAK) {
+      if constexpr (LINEAR) {
+        // linear advection: sum_m D_hat[i,m] a_d u_m (weak form) or
+        // sum_m D_split[i,m] a_d (u_i + u_m)/2 (flux differencing), with a_d
+        // taken out of the sum: one multiply per direction (FP64 multiplies
+        // occupy GB300's narrow FP64 pipe)
+        constexpr int strides[3] = {1, N, N * N};
+        const int n0 = node - ci * strides[d];
+        R sum = R(0);
+        if constexpr (VOL == VOL_WEAK) {
+#pragma unroll
+          for (int m = 0; m < N; ++m) sum += s.dhat[ci * N + m] * s.c(el, n0 + m * strides[d])[0];
+          acc[0] += p.pp.a[d] * sum;
+        } else {
+          const R ui = s.c(el, node)[0];
+#pragma unroll
+          for (int m = 0; m < N; ++m) {
+            if (m == ci) continue;
+            sum += s.dsplit[ci * N + m] * (ui + s.c(el, n0 + m * strides[d])[0]);
+          }
+          acc[0] += (R(0.5) * p.pp.a[d]) * sum;
+        }
+      } else if constexpr (VOL == VOL_WEAK) {
         constexpr int strides[3] = {1, N, N * N};
         const int n0 = node - ci * strides[d];
 #pragma unroll
