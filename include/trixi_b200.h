@@ -259,10 +259,11 @@ int trixi_container(trixi_handle *h, int which, void **dev_ptr, int64_t *count);
 int trixi_indicator(trixi_handle *h, const double *u, double *alpha, void *stream);
 
 /* Initial conditions evaluated on the GPU (params may be NULL for defaults):
- *   TRIXI_IC_CONSTANT          params = the nvars conservative values
+ *   TRIXI_IC_CONSTANT          params = the nvars conservative values (up to 9)
  *   TRIXI_IC_CONVERGENCE_TEST  params = (c, A, L); advection default (1, 0.5, 2),
- *                              Euler default (2, 0.1, 2)
- *   TRIXI_IC_WEAK_BLAST_WAVE   Euler; no params */
+ *                              Euler default (2, 0.1, 2); ideal GLM-MHD: the
+ *                              smooth Alfven waves, no params
+ *   TRIXI_IC_WEAK_BLAST_WAVE   Euler, ideal GLM-MHD (in B = (1, 1, 1)); no params */
 typedef enum trixi_initial_condition_kind {
   TRIXI_IC_CONSTANT = 0,
   TRIXI_IC_CONVERGENCE_TEST = 1,

@@ -290,3 +290,27 @@ def test_mhd_integrals(cuda):
     prod = T.integrate(u, semi, "entropy_production", du=du)[0]
     scale = float(np.einsum("e,n,en->", J, wn, np.abs(S)))
     assert abs(prod) < 1e-11 * scale, (prod, scale)
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+@pytest.mark.parametrize("kind", ["convergence_test", "weak_blast_wave"])
+def test_mhd_gpu_initial_conditions_and_error_norms(d, kind, cuda):
+    """compute_coefficients on the GPU for the MHD built-in initial conditions
+    equals the host version; calc_error_norms of the exact state is zero and
+    of a perturbed one matches numpy."""
+    setup = "alfven" if kind == "convergence_test" else "ec"
+    semi, _ = _semi(setup, d, 2 if d < 3 else 1, 3, False)
+    host = semi.compute_coefficients_host(t=0.3 if kind == "convergence_test" else 0.0)
+    u = T.compute_coefficients_gpu(semi, kind, t=0.3 if kind == "convergence_test" else 0.0)
+    T.synchronize(semi)
+    np.testing.assert_allclose(u.cpu().numpy(), host, rtol=1e-13, atol=1e-13)
+    if kind == "convergence_test":
+        # against the exact solution on 2N-1 analysis nodes: the interpolation
+        # error of the degree-3 nodal state, small but nonzero (the coarse 3D
+        # mesh, 2 elements per wavelength, shows ~5e-2); rho and E are exact
+        l2, linf = T.calc_error_norms(u, semi, t=0.3, kind=kind)
+        assert l2.shape == (semi.equations.nvariables,)
+        assert 0 < np.max(l2) < 0.1 and np.max(linf) < 0.2
+        assert l2[0] < 1e-14
+        l2b, linfb = T.calc_error_norms(u, semi, u_ref=u)
+        assert np.all(l2b == 0.0) and np.all(linfb == 0.0)

@@ -523,13 +523,13 @@ cudaError_t launch_initial_condition(const IcHost &h, cudaStream_t s) {
   for (int d = 1; d < h.dim; ++d) NN *= h.N;
   const int64_t n = h.E * NN;
   const unsigned grid = (unsigned)((n + 255) / 256);
-  TRIXI_DISPATCH(h.dim, h.eq, (ic_kernel<D_, Q_><<<grid, 256, 0, s>>>(h.N, h.E, h.coords, h.kind, h.ip, h.t, h.u)));
+  TRIXI_DISPATCH_MHD(h.dim, h.eq, (ic_kernel<D_, Q_><<<grid, 256, 0, s>>>(h.N, h.E, h.coords, h.kind, h.ip, h.t, h.u)));
   return cudaGetLastError();
 }
 
 cudaError_t launch_error_norms_all(const ErrorNormHost &h, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
-  TRIXI_DISPATCH(h.dim, h.eq, (e = launch_error_norms<D_, Q_>(h, s)));
+  TRIXI_DISPATCH_MHD(h.dim, h.eq, (e = launch_error_norms<D_, Q_>(h, s)));
   if (e != cudaSuccess) return e;
   reduce_columns<<<1, 1024, 0, s>>>(h.E, h.nv, h.l2p, 0, h.l2_out);
   reduce_columns<<<1, 1024, 0, s>>>(h.E, h.nv, h.linfp, 1, h.linf_out);

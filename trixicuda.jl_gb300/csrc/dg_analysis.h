@@ -12,7 +12,7 @@ constexpr int IC_CONVERGENCE_TEST = 1;  // TRIXI_IC_CONVERGENCE_TEST
 constexpr int IC_WEAK_BLAST_WAVE = 2;   // TRIXI_IC_WEAK_BLAST_WAVE
 
 struct IcParams {
-  double p[8];       // kind-specific parameters
+  double p[9];       // kind-specific parameters (a constant state: nvars values)
   double a[3];       // advection velocity
   double gamma;
   double xa[16];     // analysis nodes on [-1, 1] (error norms)

@@ -10,9 +10,105 @@ namespace trixi {
 constexpr int SRC_NONE = 0;              // TRIXI_SOURCE_NONE
 constexpr int SRC_CONVERGENCE_TEST = 1;  // TRIXI_SOURCE_CONVERGENCE_TEST
 
+// Ideal GLM-MHD: the convergence tests are the smooth circularly polarised
+// Alfven waves -- 1D and 2D after Derigs et al., JCP 317 (2016) (rho = 1,
+// p = 0.1, amplitude 0.1, unit background field along the propagation
+// direction: the x axis in 1D, alpha = pi/4 in 2D; speed 1), 3D after
+// Altmann's thesis (2012) (propagation along (1, 0, 2)/sqrt 5 on [-1, 1]^3,
+// amplitude 0.2, p = 1); the weak blast wave is the Euler one in a uniform
+// field B = (1, 1, 1).  psi = 0 (2D/3D).
+template <int DIM>
+__device__ void eval_ic_mhd(int kind, const double *x, double t, const IcParams &ip, double *u) {
+  constexpr int NV = (DIM == 1) ? 8 : 9;
+  if (kind == IC_CONSTANT) {
+    for (int v = 0; v < NV; ++v) u[v] = ip.p[v];
+    return;
+  }
+  double rho, v[3] = {0.0, 0.0, 0.0}, p, B[3];
+  const double pi = 3.14159265358979323846;
+  if (kind == IC_CONVERGENCE_TEST) {
+    rho = 1.0;
+    if (DIM == 1) {
+      double sn, cs;
+      sincos(2.0 * pi * (x[0] + t), &sn, &cs);
+      v[1] = 0.1 * sn;
+      v[2] = 0.1 * cs;
+      p = 0.1;
+      B[0] = 1.0;
+      B[1] = v[1];
+      B[2] = v[2];
+    } else if (DIM == 2) {
+      const double alpha = 0.25 * pi;
+      const double ca = cos(alpha), sa = sin(alpha);
+      const double x_perp = x[0] * ca + x[1] * sa;
+      double sn, cs;
+      sincos(2.0 * pi * (x_perp + t), &sn, &cs);
+      const double b_perp = 0.1 * sn;
+      v[0] = -b_perp * sa;
+      v[1] = b_perp * ca;
+      v[2] = 0.1 * cs;
+      p = 0.1;
+      B[0] = ca + v[0];
+      B[1] = sa + v[1];
+      B[2] = v[2];
+    } else {
+      const double omega = 2.0 * pi, r = 2.0, e = 0.2;
+      const double nx = 1.0 / sqrt(r * r + 1.0), ny = r / sqrt(r * r + 1.0);
+      const double va = omega / ny;
+      const double ph = omega / ny * (nx * (x[0] - 0.5 * r) + ny * (x[2] - 0.5 * r)) - va * t;
+      double sn, cs;
+      sincos(ph, &sn, &cs);
+      v[0] = -e * ny * cs;
+      v[1] = e * sn;
+      v[2] = e * nx * cs;
+      p = 1.0;
+      B[0] = nx - v[0];
+      B[1] = -v[1];
+      B[2] = ny - v[2];
+    }
+  } else {  // weak blast wave in B = (1, 1, 1)
+    double r2 = 0.0;
+    for (int d = 0; d < DIM; ++d) r2 += x[d] * x[d];
+    const double rr = sqrt(r2);
+    const bool out = rr > 0.5;
+    rho = out ? 1.0 : 1.1691;
+    p = out ? 1.0 : 1.245;
+    if (!out) {
+      if (DIM == 1) {
+        v[0] = 0.1882 * (x[0] > 0 ? 1.0 : (x[0] < 0 ? -1.0 : 0.0));
+      } else if (DIM == 2) {
+        const double phi = atan2(x[1], x[0]);
+        v[0] = 0.1882 * cos(phi);
+        v[1] = 0.1882 * sin(phi);
+      } else {
+        const double phi = atan2(x[1], x[0]);
+        const double theta = (rr == 0.0) ? 0.0 : acos(fmin(1.0, fmax(-1.0, x[2] / rr)));
+        v[0] = 0.1882 * cos(phi) * sin(theta);
+        v[1] = 0.1882 * sin(phi) * sin(theta);
+        v[2] = 0.1882 * cos(theta);
+      }
+    }
+    B[0] = B[1] = B[2] = 1.0;
+  }
+  u[0] = rho;
+  double kin = 0.0, mag = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    u[1 + d] = rho * v[d];
+    kin += v[d] * v[d];
+    mag += B[d] * B[d];
+    u[5 + d] = B[d];
+  }
+  u[4] = p / (ip.gamma - 1.0) + 0.5 * rho * kin + 0.5 * mag;
+  if (NV == 9) u[NV - 1] = 0.0;
+}
+
 template <int DIM, int EQ>
 __device__ void eval_ic(int kind, const double *x, double t, const IcParams &ip, double *u) {
   constexpr int NV = NVarsOf<DIM, EQ>::value;
+  if constexpr (EQ == EQ_MHD) {
+    eval_ic_mhd<DIM>(kind, x, t, ip, u);
+    return;
+  }
   if (kind == IC_CONSTANT) {
     for (int v = 0; v < NV; ++v) u[v] = ip.p[v];
     return;

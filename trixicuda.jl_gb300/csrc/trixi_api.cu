@@ -1006,27 +1006,37 @@ IcParams ic_params(const trixi_handle *h, int kind, const double *params, int64_
       ip.p[0] = 2.0; ip.p[1] = 0.1; ip.p[2] = 2.0;
     }
   }
-  for (int64_t i = 0; params && i < nparams && i < 8; ++i) ip.p[i] = params[i];
+  for (int64_t i = 0; params && i < nparams && i < 9; ++i) ip.p[i] = params[i];
   for (size_t i = 0; i < h->xa.size() && i < 16; ++i) ip.xa[i] = h->xa[i];
   return ip;
 }
 
 int check_ic(trixi_handle *h, int kind, int64_t nparams, const double *params) {
   if (kind < IC_CONSTANT || kind > IC_WEAK_BLAST_WAVE) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "ic kind %d", kind);
-  if (kind == IC_WEAK_BLAST_WAVE && h->eq != EQ_EULER)
-    return fail(h, TRIXI_ERR_UNSUPPORTED, "weak blast wave needs the Euler equations");
+  if (kind == IC_WEAK_BLAST_WAVE && h->eq == EQ_ADV)
+    return fail(h, TRIXI_ERR_UNSUPPORTED, "weak blast wave needs the Euler or MHD equations");
   if (kind == IC_CONSTANT && (!params || nparams < h->nv))
     return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "constant state needs %d params", h->nv);
-  if (nparams < 0 || nparams > 8) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "nparams %lld", (long long)nparams);
+  if (nparams < 0 || nparams > 9) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "nparams %lld", (long long)nparams);
   return TRIXI_OK;
 }
 
+// results of the single-block reductions: up to kRedSlot values (the nvars
+// of one quantity, at most 9) from offset 0, and a second set (Linf) from
+// offset kRedSlot
+constexpr int kRedSlot = 16;
+constexpr int kRedOut = 2 * kRedSlot;
+
 int ensure_reduction(trixi_handle *h, int nq) {
+  if (nq > kRedSlot || h->nv > kRedSlot) return fail(h, TRIXI_ERR_UNSUPPORTED, "reduction of %d values", nq);
   if (!h->d_acc) TRIXI_CUDA(h, cudaMalloc(&h->d_acc, sizeof(unsigned long long)), "alloc reduction");
   if (!h->d_partial) {
-    TRIXI_CUDA(h, cudaMalloc(&h->d_partial, sizeof(double) * (size_t)(h->E * std::max(nq, 5))), "alloc partials");
-    TRIXI_CUDA(h, cudaMalloc(&h->d_partial2, sizeof(double) * (size_t)(h->E * std::max(nq, 5))), "alloc partials");
-    TRIXI_CUDA(h, cudaMalloc(&h->d_red_out, sizeof(double) * 16), "alloc reduction out");
+    // sized for the largest quantity any call asks for (nvars per element),
+    // whichever call allocates first
+    const size_t per = (size_t)std::max(h->nv, 5);
+    TRIXI_CUDA(h, cudaMalloc(&h->d_partial, sizeof(double) * (size_t)h->E * per), "alloc partials");
+    TRIXI_CUDA(h, cudaMalloc(&h->d_partial2, sizeof(double) * (size_t)h->E * per), "alloc partials");
+    TRIXI_CUDA(h, cudaMalloc(&h->d_red_out, sizeof(double) * kRedOut), "alloc reduction out");
   }
   return TRIXI_OK;
 }
@@ -1038,7 +1048,6 @@ extern "C" {
 int trixi_compute_coefficients(trixi_handle *h, int ic_kind, const double *params, int64_t nparams, double t,
                                double *u, void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
-  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: not available in this function");
   if (int st = check_u_args(h, u, "u")) return st;
   if (int st = check_ic(h, ic_kind, nparams, params)) return st;
   if (!h->d_coords) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "desc.node_coordinates was not given");
@@ -1109,7 +1118,6 @@ int trixi_integrate(trixi_handle *h, const double *u, const double *du, int whic
 int trixi_calc_error_norms(trixi_handle *h, const double *u, const double *u_ref, int ic_kind, const double *params,
                            int64_t nparams, double t, double *l2_host, double *linf_host, void *stream) {
   if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
-  if (h->eq == EQ_MHD) return fail(h, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: not available in this function");
   if (int st = check_u_args(h, u, "u")) return st;
   if (!l2_host || !linf_host) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "null output");
   if (!u_ref) {
@@ -1146,15 +1154,15 @@ int trixi_calc_error_norms(trixi_handle *h, const double *u, const double *u_ref
   eh.l2p = h->d_partial;
   eh.linfp = h->d_partial2;
   eh.l2_out = h->d_red_out;
-  eh.linf_out = h->d_red_out + 8;
+  eh.linf_out = h->d_red_out + kRedSlot;
   cudaStream_t s = (cudaStream_t)stream;
   if (!h->d_coords) {
     // coordinates are only read for the analytic reference; give a harmless pointer
     eh.coords = h->d_inv_jac;
   }
   TRIXI_CUDA(h, launch_error_norms_all(eh, s), "error norms");
-  double buf[16];
-  TRIXI_CUDA(h, cudaMemcpyAsync(buf, h->d_red_out, sizeof(double) * 16, cudaMemcpyDeviceToHost, s), "copy");
+  double buf[kRedOut];
+  TRIXI_CUDA(h, cudaMemcpyAsync(buf, h->d_red_out, sizeof(double) * kRedOut, cudaMemcpyDeviceToHost, s), "copy");
   TRIXI_CUDA(h, cudaStreamSynchronize(s), "synchronize");
   // total volume = sum_e (2 / J^{-1}_e)^d: L2 is normalised by it
   double vol = 0.0;
@@ -1162,7 +1170,7 @@ int trixi_calc_error_norms(trixi_handle *h, const double *u, const double *u_ref
   vol = h->total_volume;
   for (int v = 0; v < h->nv; ++v) {
     l2_host[v] = std::sqrt(buf[v] / vol);
-    linf_host[v] = buf[8 + v];
+    linf_host[v] = buf[kRedSlot + v];
   }
   return TRIXI_OK;
 }
