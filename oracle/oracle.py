@@ -75,6 +75,9 @@ def load():
             ("oracle_boundary_flux", [C.c_void_p, _PD, C.c_double, _PD]),
             ("oracle_sources", [C.c_void_p, _PD, C.c_double]),
             ("oracle_eval_ic", [C.c_void_p, C.c_int, _PD, _PD, C.c_double, _PD]),
+            ("oracle_physical_flux", [C.c_void_p, _PD, C.c_int, _PD]),
+            ("oracle_two_point_flux", [C.c_void_p, C.c_int, _PD, _PD, C.c_int, _PD]),
+            ("oracle_noncons_flux", [C.c_void_p, _PD, _PD, C.c_int, _PD]),
         ]:
             fn = getattr(lib, name)
             fn.restype = None
@@ -265,6 +268,25 @@ class Oracle:
         du = np.array(du, dtype=np.float64, copy=True)
         self.lib.oracle_jacobian(self._h, _pd(du))
         return du
+
+    # pointwise fluxes (u: nvars values)
+    def physical_flux(self, u, o):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        f = np.zeros(self.nv)
+        self.lib.oracle_physical_flux(self._h, _pd(u), int(o), _pd(f))
+        return f
+
+    def two_point_flux(self, kind, ul, ur, o):
+        ul, ur = (np.ascontiguousarray(x, dtype=np.float64) for x in (ul, ur))
+        f = np.zeros(self.nv)
+        self.lib.oracle_two_point_flux(self._h, int(kind), _pd(ul), _pd(ur), int(o), _pd(f))
+        return f
+
+    def noncons_flux(self, ul, ur, o):
+        ul, ur = (np.ascontiguousarray(x, dtype=np.float64) for x in (ul, ur))
+        f = np.zeros(self.nv)
+        self.lib.oracle_noncons_flux(self._h, _pd(ul), _pd(ur), int(o), _pd(f))
+        return f
 
     def rk_ck2n54(self, u, t, dt, nsteps, k=None):
         u = np.array(u, dtype=np.float64, copy=True)

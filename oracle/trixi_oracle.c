@@ -536,6 +536,7 @@ static void add_half_noncons(const phys_t *P, const double *uown, const double *
 
 /* ------------------------------------------------------------------------ */
 /* Handle                                                                   */
+/* (pointwise fluxes for the tests: oracle_two_point_flux etc. below)       */
 /* ------------------------------------------------------------------------ */
 
 struct oracle_handle {
@@ -1178,4 +1179,14 @@ void oracle_rk_ck2n54(oracle_handle *h, double *u, double *k, double t, double d
     t += dt;
   }
   free(du);
+}
+
+/* Pointwise fluxes of the handle's equations (for the flux pins of the tests). */
+void oracle_physical_flux(oracle_handle *h, const double *u, int o, double *f) { flux_phys(&h->P, u, o, f); }
+void oracle_two_point_flux(oracle_handle *h, int kind, const double *ul, const double *ur, int o, double *f) {
+  two_point_flux(&h->P, kind, ul, ur, o, f);
+}
+void oracle_noncons_flux(oracle_handle *h, const double *ul, const double *ur, int o, double *f) {
+  for (int v = 0; v < h->NV; ++v) f[v] = 0.0;
+  if (h->P.noncons == ORC_NONCONS_POWELL) mhd_noncons_powell(&h->P, ul, ur, o, f);
 }

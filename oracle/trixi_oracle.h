@@ -105,6 +105,13 @@ void oracle_eval_ic(oracle_handle *h, int kind, const double *params, const doub
 void oracle_rhs(oracle_handle *h, double *du, const double *u, double t);
 void oracle_rk_ck2n54(oracle_handle *h, double *u, double *k, double t, double dt, int nsteps);
 
+/* Pointwise fluxes of the problem's equations along orientation o (0-based):
+ * the physical flux, a two-point flux of kind ORC_FLUX_*, and the
+ * nonconservative term Phi(u_l, u_r) (zero without one). */
+void oracle_physical_flux(oracle_handle *h, const double *u, int o, double *f);
+void oracle_two_point_flux(oracle_handle *h, int kind, const double *ul, const double *ur, int o, double *f);
+void oracle_noncons_flux(oracle_handle *h, const double *ul, const double *ur, int o, double *f);
+
 /* Sizes of the internal containers (for callers that want the stage arrays). */
 int64_t oracle_size(oracle_handle *h, int which);
 
