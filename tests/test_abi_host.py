@@ -142,3 +142,75 @@ def test_lgl_basis_entry_point_rejects_bad_input():
     assert lib.trixi_lgl_basis(0, 0, out.ctypes.data_as(C.POINTER(C.c_double)), 4) == 1
     assert lib.trixi_lgl_basis(3, 2, out.ctypes.data_as(C.POINTER(C.c_double)), 4) == 1  # 16 needed
     assert lib.trixi_lgl_basis(3, 0, out.ctypes.data_as(C.POINTER(C.c_double)), 4) == 0
+
+
+def _mhd_desc(d=2):
+    import trixicuda as T
+    from trixicuda.semidiscretization import build_problem_desc
+
+    eq = {1: T.IdealGlmMhdEquations1D, 2: T.IdealGlmMhdEquations2D, 3: T.IdealGlmMhdEquations3D}[d](1.4, 1.0)
+    pair = (lambda f: (f, T.flux_nonconservative_powell)) if d > 1 else (lambda f: f)
+    solver = T.DGSEMGPU(polydeg=3, surface_flux=pair(T.flux_lax_friedrichs),
+                        volume_integral=T.VolumeIntegralFluxDifferencing(pair(T.flux_hindenlang_gassner)))
+    mesh = T.TreeMesh((-2.0,) * d, (2.0,) * d, initial_refinement_level=1)
+    return build_problem_desc(mesh, eq, solver)
+
+
+@pytest.mark.parametrize("field,value,status", [
+    ("nvars", 8, 1),                    # 2D ideal GLM-MHD has 9 variables
+    ("nonconservative_flux", 0, 1),     # and needs flux_nonconservative_powell
+    ("volume_flux", 1, 1),              # flux_ranocha is the Euler flux
+    ("surface_flux", 5, 2),             # flux_shima_etal is a volume flux
+    ("volume_integral", 0, 2),          # weak form with nonconservative terms
+    ("polydeg", 5, 2),                  # the MHD kernels stop at polydeg 4
+    ("source_terms", 1, 2),             # periodic meshes without sources
+])
+def test_create_rejects_bad_mhd_fields(field, value, status):
+    d, keep, _ = _mhd_desc()
+    setattr(d, field, value)
+    st, msg = _create(d)
+    assert st == status, (field, st, msg)
+    assert msg
+
+
+@pytest.mark.parametrize("field,value,status", [
+    ("nonconservative_flux", 1, 1),     # Euler has no nonconservative terms
+    ("volume_flux", 4, 1),              # flux_hindenlang_gassner is the MHD flux
+    ("surface_flux", 5, 2),             # flux_shima_etal as a surface flux
+    ("volume_flux_fv", 5, 2),           # ... or as the FV flux
+    ("surface_flux", 7, 1),             # no such flux
+])
+def test_create_rejects_bad_flux_pairs(field, value, status):
+    d, keep, _ = _desc_from_mesh()
+    setattr(d, field, value)
+    st, msg = _create(d)
+    assert st == status, (field, st, msg)
+
+
+def test_create_rejects_bad_indicator_variable():
+    import trixicuda as T
+    from trixicuda.semidiscretization import build_problem_desc
+
+    eq = T.CompressibleEulerEquations2D(1.4)
+    ind = T.IndicatorHennemannGassner(eq, None)
+    vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=T.flux_ranocha, volume_flux_fv=T.flux_lax_friedrichs)
+    solver = T.DGSEMGPU(polydeg=3, surface_flux=T.flux_lax_friedrichs, volume_integral=vi)
+    d, keep, _ = build_problem_desc(T.TreeMesh((-1.0, -1.0), (1.0, 1.0), initial_refinement_level=1), eq, solver)
+    d.indicator_variable = 2
+    st, msg = _create(d)
+    assert st == 1 and "indicator_variable" in msg
+
+
+def test_flux_pairs_checked_on_the_host():
+    """Plain fluxes for MHD in 2D, or pairs for Euler, are refused before the
+    library is called."""
+    import trixicuda as T
+    from trixicuda.semidiscretization import flux_codes
+
+    eq = T.IdealGlmMhdEquations2D(1.4)
+    with pytest.raises(ValueError):
+        flux_codes(T.DGSEMGPU(polydeg=3, surface_flux=T.flux_lax_friedrichs,
+                              volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_hindenlang_gassner)), eq)
+    with pytest.raises(ValueError):
+        flux_codes(T.DGSEMGPU(polydeg=3, surface_flux=(T.flux_ranocha, T.flux_nonconservative_powell)),
+                   T.CompressibleEulerEquations2D(1.4))
