@@ -993,10 +993,77 @@ void oracle_indicator_hg(oracle_handle *h, const double *u, double *alpha) {
  * (x_d - a_d t)); Euler: rho = rho v_d = c + A sin(omega (sum_d x_d - t)),
  * E = rho^2 -- a manufactured solution of the Euler equations with the
  * source term of oracle_sources); the weak blast wave. */
+/* Ideal GLM-MHD states: the circularly polarised Alfven waves of the MHD
+ * convergence tests (1D/2D after Derigs et al., JCP 317 (2016): rho = 1,
+ * p = 0.1, amplitude 0.1, unit background field along the propagation
+ * direction -- the x axis in 1D, the diagonal alpha = pi/4 in 2D -- speed 1;
+ * 3D after Altmann's thesis (2012): direction (1, 0, 2)/sqrt 5 on [-1, 1]^3,
+ * amplitude 0.2, p = 1), and the weak blast wave in the uniform field
+ * B = (1, 1, 1); psi = 0 where the system carries it. */
+static void eval_ic_mhd(const oracle_handle *h, int kind, const double *x, double t, double *u) {
+  const int DIM = h->DIM, NV = h->NV;
+  double rho = 1.0, v[3] = {0.0, 0.0, 0.0}, p = 1.0, B[3] = {1.0, 1.0, 1.0};
+  if (kind == ORC_IC_CONVERGENCE_TEST) {
+    if (DIM == 1) {
+      const double ph = 2.0 * ORC_PI * (x[0] + t);
+      v[1] = 0.1 * sin(ph);
+      v[2] = 0.1 * cos(ph);
+      p = 0.1;
+      B[0] = 1.0; B[1] = v[1]; B[2] = v[2];
+    } else if (DIM == 2) {
+      const double ca = cos(0.25 * ORC_PI), sa = sin(0.25 * ORC_PI);
+      const double ph = 2.0 * ORC_PI * (x[0] * ca + x[1] * sa + t);
+      const double b_perp = 0.1 * sin(ph);
+      v[0] = -b_perp * sa; v[1] = b_perp * ca; v[2] = 0.1 * cos(ph);
+      p = 0.1;
+      B[0] = ca + v[0]; B[1] = sa + v[1]; B[2] = v[2];
+    } else {
+      const double r = 2.0, amp = 0.2, k = 2.0 * ORC_PI;
+      const double nx = 1.0 / sqrt(r * r + 1.0), nz = r / sqrt(r * r + 1.0);
+      const double ph = k / nz * (nx * (x[0] - 0.5 * r) + nz * (x[2] - 0.5 * r)) - k / nz * t;
+      v[0] = -amp * nz * cos(ph); v[1] = amp * sin(ph); v[2] = amp * nx * cos(ph);
+      B[0] = nx - v[0]; B[1] = -v[1]; B[2] = nz - v[2];
+    }
+  } else { /* weak blast wave: the Euler states below in B = (1, 1, 1) */
+    double r2 = 0.0;
+    for (int d = 0; d < DIM; ++d) r2 += x[d] * x[d];
+    const double r = sqrt(r2);
+    if (r <= 0.5) {
+      rho = 1.1691; p = 1.245;
+      if (DIM == 1) {
+        v[0] = x[0] > 0.0 ? 0.1882 : (x[0] < 0.0 ? -0.1882 : 0.0);
+      } else if (DIM == 2) {
+        const double phi = atan2(x[1], x[0]);
+        v[0] = 0.1882 * cos(phi); v[1] = 0.1882 * sin(phi);
+      } else {
+        const double phi = atan2(x[1], x[0]);
+        double c = r > 0.0 ? x[2] / r : 1.0;
+        c = c > 1.0 ? 1.0 : (c < -1.0 ? -1.0 : c);
+        const double theta = r > 0.0 ? acos(c) : 0.0;
+        v[0] = 0.1882 * cos(phi) * sin(theta); v[1] = 0.1882 * sin(phi) * sin(theta); v[2] = 0.1882 * cos(theta);
+      }
+    }
+  }
+  double kin = 0.0, mag = 0.0;
+  u[0] = rho;
+  for (int d = 0; d < 3; ++d) {
+    u[1 + d] = rho * v[d];
+    u[5 + d] = B[d];
+    kin += v[d] * v[d];
+    mag += B[d] * B[d];
+  }
+  u[4] = p / (h->P.gamma - 1.0) + 0.5 * rho * kin + 0.5 * mag;
+  if (NV == 9) u[8] = 0.0;
+}
+
 void oracle_eval_ic(oracle_handle *h, int kind, const double *params, const double *x, double t, double *u) {
   const int DIM = h->DIM, NV = h->NV;
   if (kind == ORC_IC_CONSTANT) {
     for (int v = 0; v < NV; ++v) u[v] = params[v];
+    return;
+  }
+  if (h->P.eq == ORC_EQ_MHD) {
+    eval_ic_mhd(h, kind, x, t, u);
     return;
   }
   if (kind == ORC_IC_CONVERGENCE_TEST) {
@@ -1074,7 +1141,11 @@ void oracle_prolong2boundaries(oracle_handle *h, const double *u, double *bu) {
 
 /* Dirichlet boundaries: the numerical flux between the inner trace and the
  * boundary function's state at the face node, the inner state on the left
- * for a boundary on the element's upper face (directions 2, 4, 6). */
+ * for a boundary on the element's upper face (directions 2, 4, 6)
+ * (boundary_flux_kernel!, dg_2d_kernel.jl:1067-1110). The reference's
+ * boundary condition evaluates the nonconservative part inside Trixi.jl,
+ * outside the repository; the element's side of an interface is taken:
+ * 0.5 Phi(u_inner, u_boundary). */
 void oracle_boundary_flux(oracle_handle *h, const double *bu, double t, double *sfv) {
   const int N = h->N, NF = h->NF, NV = h->NV, DIM = h->DIM;
   const int64_t B = h->d.nboundaries;
@@ -1092,6 +1163,9 @@ void oracle_boundary_flux(oracle_handle *h, const double *bu, double t, double *
         two_point_flux(&h->P, h->d.surface_flux, ui, ub, o, fs);
       else
         two_point_flux(&h->P, h->d.surface_flux, ub, ui, o, fs);
+      /* nonconservative terms as on the element's side of an interface:
+       * 0.5 Phi(u_inner, u_boundary) */
+      add_half_noncons(&h->P, ui, ub, o, fs);
       for (int v = 0; v < NV; ++v) sfv[v + NV * (f + (int64_t)NF * (dir + 2 * DIM * e))] = fs[v];
     }
   }

@@ -163,7 +163,7 @@ def _mhd_desc(d=2):
     ("surface_flux", 5, 2),             # flux_shima_etal is a volume flux
     ("volume_integral", 0, 2),          # weak form with nonconservative terms
     ("polydeg", 5, 2),                  # the MHD kernels stop at polydeg 4
-    ("source_terms", 1, 2),             # periodic meshes without sources
+    ("source_terms", 1, 2),             # no source terms for MHD
 ])
 def test_create_rejects_bad_mhd_fields(field, value, status):
     d, keep, _ = _mhd_desc()
@@ -185,6 +185,32 @@ def test_create_rejects_bad_flux_pairs(field, value, status):
     setattr(d, field, value)
     st, msg = _create(d)
     assert st == status, (field, st, msg)
+
+
+def test_mhd_boundary_rules():
+    """Ideal GLM-MHD takes Dirichlet boundaries; a constant state of 9
+    variables does not fit the descriptor's 8 boundary parameters and is
+    refused, in Python before the call and by the library."""
+    import trixicuda as T
+    from trixicuda.semidiscretization import build_problem_desc
+
+    eq = T.IdealGlmMhdEquations2D(1.4, 1.0)
+    pair = lambda f: (f, T.flux_nonconservative_powell)  # noqa: E731
+    solver = T.DGSEMGPU(polydeg=3, surface_flux=pair(T.flux_lax_friedrichs),
+                        volume_integral=T.VolumeIntegralFluxDifferencing(pair(T.flux_hindenlang_gassner)))
+    mesh = T.TreeMesh((0.0, 0.0), (2.0, 2.0), initial_refinement_level=1, periodicity=False)
+    with pytest.raises(NotImplementedError):
+        build_problem_desc(mesh, eq, solver,
+                           boundary_conditions=T.BoundaryConditionDirichlet(T.initial_condition_constant))
+    d, keep, _ = build_problem_desc(mesh, eq, solver,
+                                    boundary_conditions=T.BoundaryConditionDirichlet(T.initial_condition_weak_blast_wave))
+    assert d.nboundaries > 0 and d.boundary_function == 2
+    d.boundary_function = 0
+    st, msg = _create(d)
+    assert st == 2 and "8 parameters" in msg
+    d.boundary_function, d.source_terms = 2, 1
+    st, msg = _create(d)
+    assert st == 2 and "source" in msg
 
 
 def test_create_rejects_bad_indicator_variable():

@@ -314,3 +314,138 @@ def test_mhd_gpu_initial_conditions_and_error_norms(d, kind, cuda):
         assert l2[0] < 1e-14
         l2b, linfb = T.calc_error_norms(u, semi, u_ref=u)
         assert np.all(l2b == 0.0) and np.all(linfb == 0.0)
+
+
+# ---------------------------------------------------------------------------
+# Dirichlet boundaries: BoundaryConditionDirichlet on every side of a
+# non-periodic TreeMesh with the MHD boundary functions; each boundary face
+# adds 0.5 Phi(u_inner, u_boundary) on the element's side, as an interface
+# face does on each of its sides.
+
+def _bnd_semi(setup, d, level, polydeg=3, refined=False, precision="fp64", c_h=0.8):
+    if setup == "alfven":
+        gamma, ic = 5.0 / 3.0, T.initial_condition_convergence_test
+        lo, hi = {1: (0.0, 1.0), 2: (0.0, np.sqrt(2.0)), 3: (-1.0, 1.0)}[d]
+    else:
+        gamma, ic = 1.4, T.initial_condition_weak_blast_wave
+        lo, hi = (-1.0, 1.0)
+    patches = [dict(type="box", coordinates_min=(lo,) * d,
+                    coordinates_max=(lo + 0.5 * (hi - lo),) * d)] if refined else []
+    mesh = T.TreeMesh((lo,) * d, (hi,) * d, initial_refinement_level=level, refinement_patches=patches,
+                      periodicity=False)
+    eq = EQS[d](gamma, c_h)
+    if setup == "shock":
+        ind = T.IndicatorHennemannGassner(eq, None, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True)
+        sflux = _pair(T.flux_hindenlang_gassner, d)
+        vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=_pair(T.flux_hindenlang_gassner, d),
+                                              volume_flux_fv=sflux)
+    else:
+        vf = T.flux_central if (setup == "alfven" and d == 2) else T.flux_hindenlang_gassner
+        sflux, vi = _pair(T.flux_lax_friedrichs, d), T.VolumeIntegralFluxDifferencing(_pair(vf, d))
+    solver = T.DGSEMGPU(polydeg=polydeg, surface_flux=sflux, volume_integral=vi)
+    bc = T.BoundaryConditionDirichlet(ic)
+    bcs = dict(x_neg=bc, x_pos=bc, y_neg=bc, y_pos=bc, z_neg=bc, z_pos=bc)
+    semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, boundary_conditions=bcs, precision=precision)
+    return semi, Oracle.from_semi(semi)
+
+
+BND_CASES = [
+    ("alfven", 1, 3, 3, False),
+    ("alfven", 2, 3, 3, False),
+    ("alfven", 2, 3, 3, True),      # mortars touching the boundary
+    ("alfven", 3, 2, 3, False),
+    ("blast", 3, 1, 3, True),
+    ("shock", 2, 3, 4, False),
+    ("shock", 3, 2, 3, False),
+    ("blast", 2, 2, 2, False),
+]
+
+
+@pytest.mark.parametrize("case", BND_CASES, ids=[_ids(c) for c in BND_CASES])
+def test_mhd_rhs_with_boundaries_matches_oracle(case, cuda):
+    setup, d, level, p, refined = case
+    semi, orc = _bnd_semi(setup, d, level, p, refined)
+    assert semi.containers.nboundaries > 0
+    u_host, u = _u(semi, cuda)
+    du = cuda.empty_like(u)
+    T.rhs_gpu(du, u, semi, 0.37)
+    T.synchronize(semi)
+    assert_rel(du.cpu().numpy(), orc.rhs(u_host, 0.37), RTOL64, "mhd rhs with boundaries")
+
+
+@pytest.mark.parametrize("case", [BND_CASES[2], BND_CASES[5]], ids=[_ids(c) for c in (BND_CASES[2], BND_CASES[5])])
+def test_mhd_mixed_rhs_with_boundaries_close_to_oracle(case, cuda):
+    setup, d, level, p, refined = case
+    semi, orc = _bnd_semi(setup, d, level, p, refined, precision="mixed")
+    u_host, u = _u(semi, cuda)
+    du = cuda.empty_like(u)
+    T.rhs_gpu(du, u, semi, 0.37)
+    T.synchronize(semi)
+    assert_rel(du.cpu().numpy(), orc.rhs(u_host, 0.37), RTOL_MIXED, "mixed mhd rhs with boundaries")
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_mhd_boundary_stages_match_oracle(d, cuda):
+    """cuda_prolong2boundaries! and cuda_boundary_flux! (with the Powell
+    terms) one by one, then the whole staged rhs."""
+    semi, orc = _bnd_semi("alfven", d, 2, 3, d == 2)
+    u_host, u = _u(semi, cuda)
+    T.cuda_prolong2boundaries(u, semi)
+    T.synchronize(semi)
+    bu = semi.container(T._lib.CONTAINER_BOUNDARIES_U).cpu().numpy()
+    bu_ref = orc.prolong2boundaries(u_host)
+    assert np.array_equal(bu, bu_ref)
+    T.cuda_boundary_flux(0.25, semi)
+    T.synchronize(semi)
+    sfv = semi.container(T._lib.CONTAINER_SURFACE_FLUX_VALUES).cpu().numpy()
+    sfv_ref = orc.boundary_flux(bu_ref, 0.25, np.zeros_like(sfv))
+    nf = (semi.nnodes ** (d - 1)) * semi.equations.nvariables
+    mask = np.zeros(sfv.size // nf, dtype=bool)
+    c = semi.containers
+    for e, side, o in zip(c.boundary_neighbor_ids, c.boundary_neighbor_sides, c.boundary_orientations):
+        mask[(e - 1) * 2 * d + 2 * (o - 1) + (1 if side == 1 else 0)] = True
+    assert_rel(sfv.reshape(-1, nf)[mask], sfv_ref.reshape(-1, nf)[mask], RTOL64, "mhd boundary flux")
+    # the whole rhs stage by stage (volume, interfaces, boundaries, mortars,
+    # surface integral, Jacobian), as rhs_gpu! calls them
+    du = cuda.empty_like(u)
+    T.cuda_volume_integral(du, u, semi)
+    T.cuda_prolong2interfaces(u, semi)
+    T.cuda_interface_flux(semi)
+    T.cuda_prolong2boundaries(u, semi)
+    T.cuda_boundary_flux(0.25, semi)
+    T.cuda_prolong2mortars(u, semi)
+    T.cuda_mortar_flux(semi)
+    T.cuda_surface_integral(du, semi)
+    T.cuda_jacobian(du, semi)
+    T.synchronize(semi)
+    assert_rel(du.cpu().numpy(), orc.rhs(u_host, 0.25), RTOL64, "staged mhd rhs with boundaries")
+
+
+@pytest.mark.parametrize("precision,rtol", [("fp64", RTOL64), ("mixed", RTOL_MIXED)])
+def test_mhd_rk_steps_with_time_dependent_boundaries(precision, rtol, cuda):
+    """The Alfven wave's boundary states follow the RK stage times."""
+    semi, orc = _bnd_semi("alfven", 2, 3, 3, True, precision=precision)
+    u_host, u = _u(semi, cuda)
+    k = cuda.zeros_like(u)
+    T.rk_steps(u, k, 0.1, 1e-3, 3, semi)
+    T.synchronize(semi)
+    uo, _ = orc.rk_ck2n54(u_host, 0.1, 1e-3, 3)
+    assert_rel(u.cpu().numpy() - u_host, uo - u_host, rtol * 10, "mhd rk increment")
+
+
+def test_mhd_gpu_convergence_with_dirichlet_boundaries(cuda):
+    """2D Alfven wave with its exact state on the boundary, FP64: errors at
+    t = 0.1 on levels 2 and 3 fall at about polydeg + 1 = 4th order."""
+    errs = []
+    for level in (2, 3):
+        semi, _ = _bnd_semi("alfven", 2, level, 3)
+        x = semi.containers.node_coordinates.reshape(-1, 2).T
+        u = cuda.from_numpy(np.ascontiguousarray(
+            T.initial_condition_convergence_test(x, 0.0, semi.equations).T.reshape(semi.u_shape()))).to(semi.device)
+        k = cuda.zeros_like(u)
+        h = np.sqrt(2.0) / 2 ** level
+        nsteps = int(np.ceil(0.1 / (0.5 * h / 4 / 2.0)))
+        T.rk_steps(u, k, 0.0, 0.1 / nsteps, nsteps, semi)
+        ue = T.initial_condition_convergence_test(x, 0.1, semi.equations).T.reshape(semi.u_shape())
+        errs.append(float(np.sqrt(np.mean((u.cpu().numpy() - ue) ** 2))))
+    assert np.log2(errs[0] / errs[1]) > 3.0, errs

@@ -174,3 +174,99 @@ def test_mhd_nan_glm_speed_propagates():
     # with c_h = 0 everything is finite
     _, _, orc0 = _oracle(2, 1, c_h=0.0)
     assert np.all(np.isfinite(orc0.rhs(u, 0.0)))
+
+
+# ---------------------------------------------------------------------------
+# Dirichlet boundaries (BoundaryConditionDirichlet on every side of a
+# non-periodic TreeMesh, as the reference's euler_source_terms_nonperiodic.jl
+# set-ups use them), here with the MHD boundary functions and the Powell
+# terms on the element's side of each boundary face.
+
+def _bnd_oracle(d, level, lo, hi, bc, bc_params=None, polydeg=3, periodic=False, gamma=5.0 / 3.0, c_h=0.8,
+                vflux=FLUX_HINDENLANG_GASSNER, sflux=FLUX_LLF):
+    mesh = T.TreeMesh((lo,) * d, (hi,) * d, initial_refinement_level=level, periodicity=periodic)
+    cont = mesh.build_containers(basis(polydeg)["nodes"])
+    eq = MHD[d](gamma, c_h)
+    orc = Oracle(cont, d, polydeg, eq.nvariables, eq.code, gamma=gamma, volume_integral=VOL_FLUXDIFF,
+                 volume_flux=vflux, surface_flux=sflux, volume_flux_fv=sflux,
+                 nonconservative_flux=NONCONS_POWELL if d > 1 else NONCONS_NONE, glm_speed=c_h,
+                 boundary_function=-1 if periodic else bc, boundary_params=bc_params)
+    return eq, cont, orc
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+@pytest.mark.parametrize("kind,ic", [(1, T.initial_condition_convergence_test), (2, T.initial_condition_weak_blast_wave)])
+def test_oracle_mhd_boundary_states_match_host(d, kind, ic):
+    """The oracle's MHD boundary functions (Alfven waves, weak blast wave in
+    B = (1, 1, 1)) equal the host initial conditions the GPU tests use."""
+    lo, hi = {1: (0.0, 1.0), 2: (0.0, np.sqrt(2.0)), 3: (-1.0, 1.0)}[d] if kind == 1 else (-1.0, 1.0)
+    eq, cont, orc = _bnd_oracle(d, 1, lo, hi, kind)
+    x = np.ascontiguousarray(cont.node_coordinates.reshape(-1, d))
+    pd = C.POINTER(C.c_double)
+    for t in (0.0, 0.3):
+        got = np.empty((x.shape[0], eq.nvariables))
+        for i in range(x.shape[0]):
+            orc.lib.oracle_eval_ic(orc._h, kind, None, x[i].ctypes.data_as(pd), t, got[i].ctypes.data_as(pd))
+        np.testing.assert_allclose(got, ic(x.T, t, eq).T, rtol=1e-14, atol=1e-14)
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_mhd_free_stream_with_dirichlet_boundaries(d):
+    """A uniform magnetised state stays put with Dirichlet boundaries that
+    hold it: in 1D a constant boundary state; in 2D/3D the weak blast
+    wave's outer state (rho = p = 1, v = 0, B = (1, 1, 1)) on [1, 3]^d,
+    which lies outside its blast radius."""
+    if d == 1:
+        eq = MHD[1](1.4, 0.8)
+        state = eq.prim2cons(np.array([1.2]), np.array([[0.3], [-0.2], [0.1]]), np.array([0.9]),
+                             np.array([[0.7], [0.4], [-0.5]]), None)[:, 0]
+        eq, cont, orc = _bnd_oracle(1, 3, 0.0, 1.0, 0, state, gamma=1.4)
+    else:
+        eq, cont, orc = _bnd_oracle(d, 2, 1.0, 3.0, 2, gamma=1.4)
+        state = eq.prim2cons(np.array([1.0]), np.zeros((3, 1)), np.array([1.0]), np.ones((3, 1)),
+                             np.zeros(1))[:, 0]
+    u = np.broadcast_to(state, (cont.nelements,) + (4,) * d + (eq.nvariables,)).copy()
+    assert np.max(np.abs(orc.rhs(u, 0.0))) < 1e-12
+
+
+@pytest.mark.parametrize("d", [2, 3])
+def test_mhd_dirichlet_interior_equals_periodic(d):
+    """With the exact Alfven wave as the boundary state, elements away from
+    the boundary see the same neighbours as on the periodic mesh: their rhs
+    is bit-identical.  The LGL nodes include the faces, so the periodic
+    neighbour's trace is the exact state at the face node too: boundary
+    elements differ by rounding only (the coordinates of the periodic image),
+    Powell terms included -- the boundary takes 0.5 Phi(u_inner, u_boundary)
+    as the interface takes 0.5 Phi(u_own, u_other)."""
+    lo, hi = (0.0, np.sqrt(2.0)) if d == 2 else (-1.0, 1.0)
+    level = 3 if d == 2 else 2
+    eq, cont, orc_b = _bnd_oracle(d, level, lo, hi, 1)
+    _, cont_p, orc_p = _bnd_oracle(d, level, lo, hi, 1, periodic=True)
+    assert np.array_equal(cont.node_coordinates, cont_p.node_coordinates)
+    x = cont.node_coordinates.reshape(-1, d).T
+    u = np.ascontiguousarray(T.initial_condition_convergence_test(x, 0.0, eq).T.reshape(
+        (cont.nelements, 4 ** d, eq.nvariables)))
+    du_b, du_p = orc_b.rhs(u, 0.0), orc_p.rhs(u, 0.0)
+    on_bnd = np.zeros(cont.nelements, dtype=bool)
+    on_bnd[cont.boundary_neighbor_ids - 1] = True
+    assert on_bnd.any() and not on_bnd.all()
+    assert np.array_equal(du_b[~on_bnd], du_p[~on_bnd])
+    diff = np.linalg.norm(du_b[on_bnd] - du_p[on_bnd]) / np.linalg.norm(du_p[on_bnd])
+    assert diff < 1e-13, diff
+
+
+def test_mhd_alfven_convergence_with_dirichlet_boundaries():
+    """1D Alfven wave with its exact state on both ends: errors at t = 0.2
+    on levels 3 and 4 fall at about polydeg + 1 = 4th order."""
+    errs = []
+    for level in (3, 4):
+        eq, cont, orc = _bnd_oracle(1, level, 0.0, 1.0, 1, sflux=FLUX_LLF)
+        x = cont.node_coordinates.reshape(-1, 1).T
+        shape = (cont.nelements, 4, eq.nvariables)
+        u = np.ascontiguousarray(T.initial_condition_convergence_test(x, 0.0, eq).T.reshape(shape))
+        h = 1.0 / 2 ** level
+        nsteps = int(np.ceil(0.2 / (0.5 * h / 4 / 2.0)))
+        u, _ = orc.rk_ck2n54(u, 0.0, 0.2 / nsteps, nsteps)
+        ue = T.initial_condition_convergence_test(x, 0.2, eq).T.reshape(shape)
+        errs.append(float(np.sqrt(np.mean((u - ue) ** 2))))
+    assert np.log2(errs[0] / errs[1]) > 3.5, errs

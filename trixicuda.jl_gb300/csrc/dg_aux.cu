@@ -478,6 +478,10 @@ __global__ void boundary_flux_kernel(int N, int64_t B, const double *__restrict_
     flux_dispatch<DIM, EQ, double>(kind, o, ui, wi, ub, wb, fs, pp);
   else
     flux_dispatch<DIM, EQ, double>(kind, o, ub, wb, ui, wi, fs, pp);
+  // nonconservative terms: the element's side, 0.5 Phi(u_inner, u_boundary), as
+  // at interfaces (the argument order Trixi.jl's boundary condition uses for
+  // them is not part of the reference repository)
+  add_noncons_rt<DIM, EQ, double>(o, wi, wb, 0.5, fs);
   const int dir = 2 * o + (sd == 1 ? 1 : 0);
 #pragma unroll
   for (int v = 0; v < NV; ++v) sfv[v + NV * (f + (int64_t)NF * (dir + 2 * DIM * e))] = fs[v];
@@ -757,13 +761,20 @@ static cudaError_t launch_bflux(const StageHost &sh, double t, cudaStream_t s) {
   const int64_t n = sh.nboundaries * NF;
   boundary_flux_kernel<DIM, EQ><<<blocks_for(n, 128), 128, 0, s>>>(
       sh.N, sh.nboundaries, sh.boundaries_u, sh.coords, sh.bnd_neighbor_ids, sh.bnd_sides, sh.bnd_orientations, t,
-      sh.bc_kind, sh.bc, sh.surface_flux, make_pp<double>(sh.gamma, sh.adv), sh.sfv);
+      sh.bc_kind, sh.bc, sh.surface_flux, make_pp<double>(sh.gamma, sh.adv, sh.c_h), sh.sfv);
   return cudaGetLastError();
 }
 
 cudaError_t stage_boundary_flux(const StageHost &sh, double t, cudaStream_t s) {
   if (sh.nboundaries == 0) return cudaSuccess;
-  if (sh.eq == EQ_MHD) return cudaErrorNotSupported;
+  if (sh.eq == EQ_MHD) {
+    switch (sh.dim) {
+      case 1: return launch_bflux<1, EQ_MHD>(sh, t, s);
+      case 2: return launch_bflux<2, EQ_MHD>(sh, t, s);
+      case 3: return launch_bflux<3, EQ_MHD>(sh, t, s);
+    }
+    return cudaErrorNotSupported;
+  }
   const bool adv = sh.eq == EQ_ADV;
   switch (sh.dim) {
     case 1: return adv ? launch_bflux<1, EQ_ADV>(sh, t, s) : launch_bflux<1, EQ_EULER>(sh, t, s);

@@ -19,8 +19,16 @@ bool fused_supported(int dim, int N, int eq, int vol, int vflux) {
 cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed, const FusedHost &h,
                          cudaStream_t s) {
   if (!fused_supported(dim, N, eq, vol, vflux)) return cudaErrorNotSupported;
-  if (eq == 2) {  // ideal GLM-MHD (periodic meshes, no source terms)
-    if (h.bc_kind >= 0 || h.src_kind != 0) return cudaErrorNotSupported;
+  if (eq == 2) {  // ideal GLM-MHD (no source terms)
+    if (h.src_kind != 0) return cudaErrorNotSupported;
+    if (h.bc_kind >= 0) {  // non-periodic: the Dirichlet instantiations
+      switch (dim) {
+        case 1: return mixed ? launch_fused_1d_f32_mhd_bnd(N, eq, vol, vflux, h, s) : launch_fused_1d_f64_mhd_bnd(N, eq, vol, vflux, h, s);
+        case 2: return mixed ? launch_fused_2d_f32_mhd_bnd(N, eq, vol, vflux, h, s) : launch_fused_2d_f64_mhd_bnd(N, eq, vol, vflux, h, s);
+        case 3: return mixed ? launch_fused_3d_f32_mhd_bnd(N, eq, vol, vflux, h, s) : launch_fused_3d_f64_mhd_bnd(N, eq, vol, vflux, h, s);
+      }
+      return cudaErrorNotSupported;
+    }
     switch (dim) {
       case 1: return mixed ? launch_fused_1d_f32_mhd(N, eq, vol, vflux, h, s) : launch_fused_1d_f64_mhd(N, eq, vol, vflux, h, s);
       case 2: return mixed ? launch_fused_2d_f32_mhd(N, eq, vol, vflux, h, s) : launch_fused_2d_f64_mhd(N, eq, vol, vflux, h, s);

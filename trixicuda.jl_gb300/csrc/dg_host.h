@@ -83,6 +83,12 @@ cudaError_t launch_fused_2d_f64_mhd(int N, int eq, int vol, int vflux, const Fus
 cudaError_t launch_fused_2d_f32_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 cudaError_t launch_fused_3d_f64_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 cudaError_t launch_fused_3d_f32_mhd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_1d_f64_mhd_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_1d_f32_mhd_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_2d_f64_mhd_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_2d_f32_mhd_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_3d_f64_mhd_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
+cudaError_t launch_fused_3d_f32_mhd_bnd(int N, int eq, int vol, int vflux, const FusedHost &h, cudaStream_t s);
 
 // Auxiliary kernels (dg_aux.cu).
 struct MortarHost {

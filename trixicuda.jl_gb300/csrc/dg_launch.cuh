@@ -130,23 +130,24 @@ cudaError_t launch_n(int eq, int vol, int vflux, const FusedHost &h, cudaStream_
 
 // ideal GLM-MHD: flux differencing (flux_hindenlang_gassner or flux_central)
 // and shock capturing (flux_hindenlang_gassner), polydeg 1..4
-template <int DIM, int N, typename R>
+template <int DIM, int N, typename R, int BND>
 cudaError_t launch_n_mhd(int vol, int vflux, const FusedHost &h, cudaStream_t s) {
   if (vol == VOL_FD) {
-    if (vflux == FLUX_HG) return launch_one<DIM, N, EQ_MHD, R, VOL_FD, FLUX_HG, 0>(h, s);
-    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_MHD, R, VOL_FD, FLUX_CENTRAL, 0>(h, s);
+    if (vflux == FLUX_HG) return launch_one<DIM, N, EQ_MHD, R, VOL_FD, FLUX_HG, BND>(h, s);
+    if (vflux == FLUX_CENTRAL) return launch_one<DIM, N, EQ_MHD, R, VOL_FD, FLUX_CENTRAL, BND>(h, s);
   }
-  if (vol == VOL_SC && vflux == FLUX_HG) return launch_one<DIM, N, EQ_MHD, R, VOL_SC, FLUX_HG, 0>(h, s);
+  if (vol == VOL_SC && vflux == FLUX_HG) return launch_one<DIM, N, EQ_MHD, R, VOL_SC, FLUX_HG, BND>(h, s);
   return cudaErrorNotSupported;
 }
 
-template <int DIM, typename R>
+// BND = 1: non-periodic meshes (Dirichlet states as the neighbour traces)
+template <int DIM, typename R, int BND = 0>
 cudaError_t launch_dim_mhd(int N, int vol, int vflux, const FusedHost &h, cudaStream_t s) {
   switch (N) {
-    case 2: return launch_n_mhd<DIM, 2, R>(vol, vflux, h, s);
-    case 3: return launch_n_mhd<DIM, 3, R>(vol, vflux, h, s);
-    case 4: return launch_n_mhd<DIM, 4, R>(vol, vflux, h, s);
-    case 5: return launch_n_mhd<DIM, 5, R>(vol, vflux, h, s);
+    case 2: return launch_n_mhd<DIM, 2, R, BND>(vol, vflux, h, s);
+    case 3: return launch_n_mhd<DIM, 3, R, BND>(vol, vflux, h, s);
+    case 4: return launch_n_mhd<DIM, 4, R, BND>(vol, vflux, h, s);
+    case 5: return launch_n_mhd<DIM, 5, R, BND>(vol, vflux, h, s);
     default: return cudaErrorNotSupported;
   }
 }

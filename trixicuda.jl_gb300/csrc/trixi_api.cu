@@ -257,8 +257,10 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
       return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "nonconservative_flux %d, the equations need %d",
                   d->nonconservative_flux, need);
   }
-  if (mhd && (d->nboundaries > 0 || d->source_terms != TRIXI_SOURCE_NONE))
-    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: periodic meshes without source terms");
+  if (mhd && d->source_terms != TRIXI_SOURCE_NONE)
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: no source terms");
+  if (mhd && d->nboundaries > 0 && d->boundary_function == TRIXI_IC_CONSTANT && d->nvars > 8)
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: a constant Dirichlet state needs 9 > 8 parameters");
   if (mhd && d->volume_integral == TRIXI_VOLUME_WEAK_FORM)
     return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "ideal GLM-MHD: flux differencing or shock capturing");
   if (d->volume_integral == TRIXI_VOLUME_SHOCK_CAPTURING_HG && d->indicator_variable != 0 && d->indicator_variable != 1)
@@ -275,8 +277,8 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "boundary tables");
   if (d->nboundaries > 0 && (d->boundary_function < TRIXI_IC_CONSTANT || d->boundary_function > TRIXI_IC_WEAK_BLAST_WAVE))
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "boundary_function %d", d->boundary_function);
-  if (d->nboundaries > 0 && d->boundary_function == TRIXI_IC_WEAK_BLAST_WAVE && d->equation != TRIXI_EQ_COMPRESSIBLE_EULER)
-    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "the weak blast wave needs the Euler equations");
+  if (d->nboundaries > 0 && d->boundary_function == TRIXI_IC_WEAK_BLAST_WAVE && d->equation == TRIXI_EQ_LINEAR_ADVECTION)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "the weak blast wave needs the Euler or MHD equations");
   if (d->nboundary_params < 0 || d->nboundary_params > 8 || d->nsource_params < 0 || d->nsource_params > 3)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "nboundary_params %d / nsource_params %d", d->nboundary_params,
                 d->nsource_params);

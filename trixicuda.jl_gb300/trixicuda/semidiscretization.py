@@ -69,6 +69,9 @@ def _boundary_spec(boundary_conditions, cont, equations):
     if code == _lib.IC_CONSTANT:
         x = np.zeros((equations.ndims, 1))
         params = np.asarray(vals[0].boundary_value_function(x, 0.0, equations))[:, 0]
+        if params.size > 8:
+            raise NotImplementedError(f"a constant Dirichlet state of {params.size} variables: the problem "
+                                      "descriptor holds 8 boundary parameters")
     return code, params
 
 
