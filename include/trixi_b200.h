@@ -152,7 +152,10 @@ typedef struct trixi_problem_desc {
    * boundary_function -- a trixi_initial_condition_kind evaluated at the face
    * node and the time of the rhs, with the first nboundary_params of
    * boundary_params (0: the defaults of trixi_compute_coefficients) -- through
-   * the surface flux, as BoundaryConditionDirichlet does.  source_terms (a
+   * the surface flux, as BoundaryConditionDirichlet does (ideal GLM-MHD adds
+   * 0.5 Phi(u_inner, u_boundary) of the nonconservative flux on the
+   * element's side; a constant state of 9 variables does not fit
+   * boundary_params and is refused with TRIXI_ERR_UNSUPPORTED).  source_terms (a
    * trixi_source_terms_kind) adds a source to du after the Jacobian; its
    * parameters (c, A, L) default to the convergence test's.  Both need
    * node_coordinates. */
