@@ -77,7 +77,8 @@ typedef enum trixi_flux_kind {
   TRIXI_FLUX_LAX_FRIEDRICHS_NAIVE = 3,  /* LLF with max(|v_ll|,|v_rr|) + max(c_ll,c_rr) */
   TRIXI_FLUX_HINDENLANG_GASSNER = 4,    /* flux_hindenlang_gassner (ideal GLM-MHD) */
   TRIXI_FLUX_SHIMA_ETAL = 5,            /* flux_shima_etal (Euler; a volume flux) */
-  TRIXI_FLUX_HLL = 6                    /* flux_hll: HLL with the naive min/max wave-speed estimates */
+  TRIXI_FLUX_HLL = 6,                   /* flux_hll: HLL with the naive min/max wave-speed estimates */
+  TRIXI_FLUX_HLLE = 7                   /* flux_hlle: HLL with Einfeldt's wave speeds (Euler, ideal GLM-MHD) */
 } trixi_flux_kind;
 
 /* The nonconservative half of a (flux, nonconservative_flux) pair.  Ideal

@@ -17,7 +17,7 @@ from . import build as _build_mod
 EQ_ADVECTION, EQ_EULER, EQ_MHD = 0, 1, 2
 VOL_WEAK, VOL_FLUXDIFF, VOL_SHOCK_HG = 0, 1, 2
 FLUX_LLF, FLUX_RANOCHA, FLUX_CENTRAL, FLUX_LLF_NAIVE, FLUX_HINDENLANG_GASSNER = 0, 1, 2, 3, 4
-FLUX_SHIMA_ETAL, FLUX_HLL = 5, 6
+FLUX_SHIMA_ETAL, FLUX_HLL, FLUX_HLLE = 5, 6, 7
 NONCONS_NONE, NONCONS_POWELL = 0, 1
 
 

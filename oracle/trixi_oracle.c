@@ -512,8 +512,85 @@ static void flux_hll(const phys_t *P, const double *ul, const double *ur, int o,
   }
 }
 
+/* Einfeldt's signal speeds for flux_hlle (Trixi.jl's min_max_speed_einfeldt,
+ * outside the reference repository; restated from the publications):
+ *  Euler (Einfeldt, Munz, Roe, Sjogreen, JCP 92 (1991)): Roe averages with
+ *    sqrt(rho) weights of v and H = (E + p)/rho, c~ = sqrt((gamma-1)(H~ -
+ *    |v~|^2/2)), beta = sqrt((gamma-1)/(2 gamma)),
+ *    lmin = min(v~ - c~, v_l - beta c_l, 0), lmax = max(v~ + c~, v_r + beta c_r, 0);
+ *  ideal GLM-MHD (Cargo, Gallice, JCP 136 (1997), the fast speed of their
+ *    Roe-type matrix): v, H = (E + p + |B|^2/2)/rho with sqrt(rho) weights, B
+ *    with the crossed weights, X = |B_l - B_r|^2 / (2 (sqrt rho_l + sqrt rho_r)^2),
+ *    b^2 = |B~|^2 / sqrt(rho_l rho_r), a^2 = (2-gamma) X + (gamma-1)(H~ - |v~|^2/2 - b^2),
+ *    c_f~^2 = (a^2 + b^2 + sqrt((a^2 + b^2)^2 - 4 a^2 B~_o^2 / sqrt(rho_l rho_r)))/2,
+ *    lmin = min(v_l - c_f,l, v~ - c_f~), lmax = max(v_r + c_f,r, v~ + c_f~). */
+static void einfeldt_speeds(const phys_t *P, const double *ul, const double *ur, int o, double *lmin,
+                            double *lmax) {
+  const double g = P->gamma;
+  if (P->eq == ORC_EQ_MHD) {
+    double wl[9], wr[9];
+    mhd_prim(P, ul, wl);
+    mhd_prim(P, ur, wr);
+    const double sl = sqrt(wl[0]), sr = sqrt(wr[0]);
+    const double ql = sl / (sl + sr), qr = sr / (sl + sr), rho_hat = sl * sr;
+    double v[3], B[3], v2 = 0.0, b2 = 0.0, x = 0.0, ml = 0.0, mr = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      v[d] = ql * wl[1 + d] + qr * wr[1 + d];
+      B[d] = qr * wl[5 + d] + ql * wr[5 + d];
+      v2 += v[d] * v[d];
+      b2 += B[d] * B[d];
+      x += (wl[5 + d] - wr[5 + d]) * (wl[5 + d] - wr[5 + d]);
+      ml += wl[5 + d] * wl[5 + d];
+      mr += wr[5 + d] * wr[5 + d];
+    }
+    x = 0.5 * x / ((sl + sr) * (sl + sr));
+    b2 /= rho_hat;
+    const double hl = (ul[4] + wl[4] + 0.5 * ml) / wl[0], hr = (ur[4] + wr[4] + 0.5 * mr) / wr[0];
+    const double h = ql * hl + qr * hr;
+    const double a2 = (2.0 - g) * x + (g - 1.0) * (h - 0.5 * v2 - b2);
+    const double sum = a2 + b2;
+    const double cf = sqrt(0.5 * (sum + sqrt(sum * sum - 4.0 * a2 * B[o] * B[o] / rho_hat)));
+    const double cl = mhd_fast_speed(P, wl, o), cr = mhd_fast_speed(P, wr, o);
+    *lmin = fmin(wl[1 + o] - cl, v[o] - cf);
+    *lmax = fmax(wr[1 + o] + cr, v[o] + cf);
+    return;
+  }
+  double rl, rr, vl[3], vr[3], pl, pr;
+  cons2prim(P, ul, &rl, vl, &pl);
+  cons2prim(P, ur, &rr, vr, &pr);
+  const int dim = P->dim;
+  const double sl = sqrt(rl), sr = sqrt(rr);
+  const double hl = (ul[dim + 1] + pl) / rl, hr = (ur[dim + 1] + pr) / rr;
+  double v2 = 0.0, vo = 0.0;
+  for (int d = 0; d < dim; ++d) {
+    const double vd = (sl * vl[d] + sr * vr[d]) / (sl + sr);
+    v2 += vd * vd;
+    if (d == o) vo = vd;
+  }
+  const double h = (sl * hl + sr * hr) / (sl + sr);
+  const double c = sqrt((g - 1.0) * (h - 0.5 * v2));
+  const double beta = sqrt(0.5 * (g - 1.0) / g);
+  const double cl = sqrt(g * pl / rl), cr = sqrt(g * pr / rr);
+  *lmin = fmin(fmin(vo - c, vl[o] - beta * cl), 0.0);
+  *lmax = fmax(fmax(vo + c, vr[o] + beta * cr), 0.0);
+}
+
+/* flux_hlle: the HLL flux of flux_hll with Einfeldt's signal speeds. */
+static void flux_hlle(const phys_t *P, const double *ul, const double *ur, int o, double *f) {
+  double lmin, lmax, fl[NVMAX], fr[NVMAX];
+  einfeldt_speeds(P, ul, ur, o, &lmin, &lmax);
+  flux_phys(P, ul, o, fl);
+  flux_phys(P, ur, o, fr);
+  for (int v = 0; v < P->nv; ++v) {
+    if (lmin >= 0) f[v] = fl[v];
+    else if (lmax <= 0) f[v] = fr[v];
+    else f[v] = (lmax * fl[v] - lmin * fr[v] + lmin * lmax * (ur[v] - ul[v])) / (lmax - lmin);
+  }
+}
+
 static void two_point_flux(const phys_t *P, int kind, const double *ul, const double *ur, int o, double *f) {
   switch (kind) {
+    case ORC_FLUX_HLLE: flux_hlle(P, ul, ur, o, f); break;
     case ORC_FLUX_SHIMA_ETAL: flux_shima(P, ul, ur, o, f); break;
     case ORC_FLUX_HLL: flux_hll(P, ul, ur, o, f); break;
     case ORC_FLUX_RANOCHA: flux_ranocha(P, ul, ur, o, f); break;

@@ -178,7 +178,8 @@ def test_create_rejects_bad_mhd_fields(field, value, status):
     ("volume_flux", 4, 1),              # flux_hindenlang_gassner is the MHD flux
     ("surface_flux", 5, 2),             # flux_shima_etal as a surface flux
     ("volume_flux_fv", 5, 2),           # ... or as the FV flux
-    ("surface_flux", 7, 1),             # no such flux
+    ("surface_flux", 8, 1),             # no such flux
+    ("volume_flux", 7, 2),              # flux_hlle as a volume flux
 ])
 def test_create_rejects_bad_flux_pairs(field, value, status):
     d, keep, _ = _desc_from_mesh()
@@ -211,6 +212,15 @@ def test_mhd_boundary_rules():
     d.boundary_function, d.source_terms = 2, 1
     st, msg = _create(d)
     assert st == 2 and "source" in msg
+
+
+def test_create_rejects_shima_with_hlle():
+    """flux_hlle is compiled into the kernels with boundary support, which
+    flux_shima_etal does not have."""
+    d, keep, _ = _desc_from_mesh()
+    d.volume_flux, d.surface_flux = 5, 7
+    st, msg = _create(d)
+    assert st == 2 and "flux_hlle" in msg
 
 
 def test_create_rejects_bad_indicator_variable():

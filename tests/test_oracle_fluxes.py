@@ -1,4 +1,4 @@
-"""flux_shima_etal and flux_hll in the CPU oracle (no GPU), as the reference's
+"""flux_shima_etal, flux_hll and flux_hlle in the CPU oracle (no GPU), as the reference's
 tests use them: flux_shima_etal as the DG volume flux of shock capturing
 (test/tree_dgsem_{1,2}d/euler_shock.jl), flux_hll as the surface flux of the
 weak form (test/tree_dgsem_3d/euler_convergence.jl).  Pins: free-stream
@@ -30,6 +30,8 @@ CASES = [
     ("euler_weak", 3, 1, True, dict(surface_flux=T.flux_hll)),
     ("euler_fd", 3, 1, False, dict(surface_flux=T.flux_hll)),
     ("adv_weak", 2, 2, True, dict(surface_flux=T.flux_hll)),
+    ("euler_weak", 2, 2, True, dict(surface_flux=T.flux_hlle)),
+    ("euler_sc", 3, 1, True, dict(fv_flux=T.flux_hlle, surface_flux=T.flux_hlle)),
 ]
 
 
@@ -45,7 +47,10 @@ def test_free_stream(case):
     assert np.max(np.abs(du)) < 1e-12
 
 
-@pytest.mark.parametrize("case", CASES[1:5], ids=[f"{c[0]}-{c[1]}d" for c in CASES[1:5]])
+CONS = CASES[1:5] + CASES[7:]
+
+
+@pytest.mark.parametrize("case", CONS, ids=[f"{c[0]}-{c[1]}d-{'-'.join(f.name for f in c[4].values())}" for c in CONS])
 def test_conservation(case):
     """sum_e J_e sum_i w_i du_i = 0 per conserved variable on periodic meshes
     (also across mortars: the L2 mortar projection of the surface flux is
@@ -87,7 +92,8 @@ def _eoc_error(level, surface_flux, d=2, p=3, t_end=0.1):
     return float(np.sqrt(np.mean((u - ue) ** 2)))
 
 
-def test_hll_convergence_order():
-    """Weak form with flux_hll converges at about polydeg + 1."""
-    e0, e1 = _eoc_error(2, T.flux_hll), _eoc_error(3, T.flux_hll)
+@pytest.mark.parametrize("flux", [T.flux_hll, T.flux_hlle], ids=lambda f: f.name)
+def test_hll_convergence_order(flux):
+    """Weak form with flux_hll / flux_hlle converges at about polydeg + 1."""
+    e0, e1 = _eoc_error(2, flux), _eoc_error(3, flux)
     assert np.log2(e0 / e1) > 3.3, (e0, e1)

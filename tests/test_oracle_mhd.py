@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import trixicuda as T
-from oracle.oracle import (FLUX_CENTRAL, FLUX_HINDENLANG_GASSNER, FLUX_LLF, NONCONS_NONE, NONCONS_POWELL,
+from oracle.oracle import (FLUX_CENTRAL, FLUX_HINDENLANG_GASSNER, FLUX_HLLE, FLUX_LLF, NONCONS_NONE, NONCONS_POWELL,
                            VOL_FLUXDIFF, VOL_SHOCK_HG, Oracle, basis)
 
 MHD = {1: T.IdealGlmMhdEquations1D, 2: T.IdealGlmMhdEquations2D, 3: T.IdealGlmMhdEquations3D}
@@ -90,6 +90,10 @@ def _weights(cont, d, polydeg):
     (2, 2, FLUX_HINDENLANG_GASSNER, FLUX_HINDENLANG_GASSNER, VOL_SHOCK_HG, True),
     (3, 1, FLUX_HINDENLANG_GASSNER, FLUX_LLF, VOL_FLUXDIFF, True),
     (3, 1, FLUX_HINDENLANG_GASSNER, FLUX_HINDENLANG_GASSNER, VOL_SHOCK_HG, False),
+    (1, 3, FLUX_HINDENLANG_GASSNER, FLUX_HLLE, VOL_FLUXDIFF, False),
+    (2, 2, FLUX_HINDENLANG_GASSNER, FLUX_HLLE, VOL_FLUXDIFF, True),    # mhd_alfven_wave_mortar.jl
+    (2, 2, FLUX_HINDENLANG_GASSNER, FLUX_HLLE, VOL_SHOCK_HG, True),
+    (3, 1, FLUX_HINDENLANG_GASSNER, FLUX_HLLE, VOL_FLUXDIFF, True),
 ])
 def test_mhd_free_stream(d, level, vflux, sflux, vol, refined):
     """A constant state (with a magnetic field and psi) is preserved to
@@ -136,9 +140,9 @@ def test_mhd_entropy_conservation(d, level, c_h):
     assert float(np.sum(J[:, None] * w[None, :] * np.sum(v * du2, axis=2))) < -1e-8 * scale
 
 
-def _alfven_error(d, level, t_end=0.1, polydeg=3, vflux=FLUX_CENTRAL):
+def _alfven_error(d, level, t_end=0.1, polydeg=3, vflux=FLUX_CENTRAL, sflux=FLUX_LLF):
     lo, hi = (0.0, 1.0) if d == 1 else ((0.0, np.sqrt(2.0)) if d == 2 else (-1.0, 1.0))
-    eq, cont, orc = _oracle(d, level, polydeg=polydeg, lo=lo, hi=hi, vflux=vflux, sflux=FLUX_LLF,
+    eq, cont, orc = _oracle(d, level, polydeg=polydeg, lo=lo, hi=hi, vflux=vflux, sflux=sflux,
                             gamma=5.0 / 3.0, c_h=1.0)
     u = _state(eq, cont, T.initial_condition_convergence_test)
     h = (hi - lo) / 2 ** level
@@ -151,15 +155,17 @@ def _alfven_error(d, level, t_end=0.1, polydeg=3, vflux=FLUX_CENTRAL):
     return float(np.sqrt(np.mean((u - ue) ** 2)))
 
 
-@pytest.mark.parametrize("d,levels,vflux,min_eoc", [
-    (1, (2, 3), FLUX_HINDENLANG_GASSNER, 3.5),
-    (2, (2, 3), FLUX_CENTRAL, 3.0),
-    (2, (2, 3), FLUX_HINDENLANG_GASSNER, 3.0),
+@pytest.mark.parametrize("d,levels,vflux,sflux,min_eoc", [
+    (1, (2, 3), FLUX_HINDENLANG_GASSNER, FLUX_LLF, 3.5),
+    (2, (2, 3), FLUX_CENTRAL, FLUX_LLF, 3.0),
+    (2, (2, 3), FLUX_HINDENLANG_GASSNER, FLUX_LLF, 3.0),
+    (1, (2, 3), FLUX_HINDENLANG_GASSNER, FLUX_HLLE, 3.5),
+    (2, (2, 3), FLUX_HINDENLANG_GASSNER, FLUX_HLLE, 3.0),
 ])
-def test_mhd_alfven_wave_convergence(d, levels, vflux, min_eoc):
+def test_mhd_alfven_wave_convergence(d, levels, vflux, sflux, min_eoc):
     """The smooth Alfven waves converge at about polydeg + 1 (polydeg 3;
     measured 3.2-3.7 between these coarse levels, still pre-asymptotic)."""
-    e0, e1 = (_alfven_error(d, lv, vflux=vflux) for lv in levels)
+    e0, e1 = (_alfven_error(d, lv, vflux=vflux, sflux=sflux) for lv in levels)
     assert np.log2(e0 / e1) > min_eoc, (e0, e1)
 
 

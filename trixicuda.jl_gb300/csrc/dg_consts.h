@@ -16,6 +16,7 @@ constexpr int FLUX_LLF_NAIVE = 3;  // TRIXI_FLUX_LAX_FRIEDRICHS_NAIVE
 constexpr int FLUX_HG = 4;         // TRIXI_FLUX_HINDENLANG_GASSNER
 constexpr int FLUX_SHIMA = 5;      // TRIXI_FLUX_SHIMA_ETAL
 constexpr int FLUX_HLL = 6;        // TRIXI_FLUX_HLL
+constexpr int FLUX_HLLE = 7;       // TRIXI_FLUX_HLLE
 
 constexpr int NONCONS_NONE = 0;    // TRIXI_NONCONSERVATIVE_NONE
 constexpr int NONCONS_POWELL = 1;  // TRIXI_NONCONSERVATIVE_POWELL

@@ -393,9 +393,9 @@ struct FusedKernel {
       lds_rec<NV>(s.c(el, own), uo);
       lds_rec<NV>(s.w(el, own), wo);
       if (side == 0)
-        two_point_flux<DIM, EQ, R, O>(p.surface_flux, un, wn, uo, wo, f, p.pp);
+        two_point_flux<DIM, EQ, R, O, BND>(p.surface_flux, un, wn, uo, wo, f, p.pp);
       else
-        two_point_flux<DIM, EQ, R, O>(p.surface_flux, uo, wo, un, wn, f, p.pp);
+        two_point_flux<DIM, EQ, R, O, BND>(p.surface_flux, uo, wo, un, wn, f, p.pp);
       // nonconservative terms: each side adds 0.5 Phi(own, other)
       // (interface_flux_kernel!, src/solvers/dg_2d_kernel.jl:1009-1035)
       if constexpr (NC) P::template add_noncons<O>(wo, wn, R(0.5), f);
@@ -412,7 +412,7 @@ struct FusedKernel {
     lds_rec<NV>(s.w(el, nl), wl);
     lds_rec<NV>(s.c(el, nr), ur);
     lds_rec<NV>(s.w(el, nr), wr);
-    two_point_flux<DIM, EQ, R, O>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
+    two_point_flux<DIM, EQ, R, O, BND>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
     if constexpr (NC) {
       R g[NV];
 #pragma unroll

@@ -184,6 +184,12 @@ struct Physics<DIM, EQ_ADV, R> {
     lmin = pp.a[O];
     lmax = pp.a[O];
   }
+  // (flux_hlle is refused for linear advection on the host)
+  template <int O>
+  __device__ __forceinline__ static void min_max_speed_einfeldt(const R *, const R *wl, const R *, const R *wr,
+                                                                R &lmin, R &lmax, const PhysParams<R> &pp) {
+    min_max_speed<O>(wl, wr, lmin, lmax, pp);
+  }
 };
 
 template <int DIM, typename R>
@@ -293,6 +299,32 @@ struct Physics<DIM, EQ_EULER, R> {
     const R cr = dev_sqrt(dev_div(pp.gamma * wr[DIM + 1], wr[0]));
     lmin = fminf_(wl[1 + O] - cl, wr[1 + O] - cr);
     lmax = dev_fmax(wl[1 + O] + cl, wr[1 + O] + cr);
+  }
+  // Einfeldt's signal speeds (Einfeldt, Munz, Roe, Sjogreen, JCP 92 (1991)):
+  // Roe averages with sqrt(rho) weights, v~ and H~ = (E + p)/rho averaged,
+  // c~^2 = (gamma - 1)(H~ - |v~|^2/2); the states' sound speeds scaled by
+  // beta = sqrt((gamma - 1)/(2 gamma)); both bounds enclose zero:
+  // lmin = min(v~_O - c~, v_l,O - beta c_l, 0), lmax = max(v~_O + c~, v_r,O + beta c_r, 0)
+  template <int O>
+  __device__ __forceinline__ static void min_max_speed_einfeldt(const R *ul, const R *wl, const R *ur, const R *wr,
+                                                                R &lmin, R &lmax, const PhysParams<R> &pp) {
+    const R sl = dev_sqrt(wl[0]), sr = dev_sqrt(wr[0]);
+    const R inv = dev_rcp(sl + sr);
+    const R hl = dev_div(ul[DIM + 1] + wl[DIM + 1], wl[0]), hr = dev_div(ur[DIM + 1] + wr[DIM + 1], wr[0]);
+    R v2 = R(0), vo = R(0);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const R vd = (sl * wl[1 + d] + sr * wr[1 + d]) * inv;
+      v2 += vd * vd;
+      if (d == O) vo = vd;
+    }
+    const R h = (sl * hl + sr * hr) * inv;
+    const R c = dev_sqrt(pp.gm1 * (h - R(0.5) * v2));
+    const R beta = dev_sqrt(dev_div(R(0.5) * pp.gm1, pp.gamma));
+    const R cl = dev_sqrt(dev_div(pp.gamma * wl[DIM + 1], wl[0]));
+    const R cr = dev_sqrt(dev_div(pp.gamma * wr[DIM + 1], wr[0]));
+    lmin = fminf_(fminf_(vo - c, wl[1 + O] - beta * cl), R(0));
+    lmax = dev_fmax(dev_fmax(vo + c, wr[1 + O] + beta * cr), R(0));
   }
   __device__ __forceinline__ static R fminf_(R a, R b) { return a < b ? a : b; }
 };
@@ -445,6 +477,44 @@ struct Physics<DIM, EQ_MHD, R> {
     lmin = a < b ? a : b;
     lmax = dev_fmax(wl[1 + O] + cl, wr[1 + O] + cr);
   }
+  // Einfeldt's signal speeds with the Roe-type average of Cargo and Gallice
+  // (JCP 136 (1997)): sqrt(rho) weights for v and H = (E + p + |B|^2/2)/rho,
+  // crossed weights for B; rho^ = sqrt(rho_l rho_r),
+  // X = |B_l - B_r|^2 / (2 (sqrt(rho_l) + sqrt(rho_r))^2) (their eq. 4.12),
+  // b^2 = |B~|^2/rho^, a^2 = (2 - gamma) X + (gamma - 1)(H~ - |v~|^2/2 - b^2),
+  // c_f~^2 = (a^2 + b^2 + sqrt((a^2 + b^2)^2 - 4 a^2 B~_O^2/rho^))/2;
+  // lmin = min(v_l,O - c_f,l, v~_O - c_f~), lmax = max(v_r,O + c_f,r, v~_O + c_f~)
+  template <int O>
+  __device__ __forceinline__ static void min_max_speed_einfeldt(const R *ul, const R *wl, const R *ur, const R *wr,
+                                                                R &lmin, R &lmax, const PhysParams<R> &pp) {
+    const R sl = dev_sqrt(wl[0]), sr = dev_sqrt(wr[0]);
+    const R inv = dev_rcp(sl + sr), inv_prod = dev_rcp(sl * sr);
+    const R ql = sl * inv, qr = sr * inv;
+    const R ml = wl[5] * wl[5] + wl[6] * wl[6] + wl[7] * wl[7];
+    const R mr = wr[5] * wr[5] + wr[6] * wr[6] + wr[7] * wr[7];
+    const R hl = dev_div(ul[4] + wl[4] + R(0.5) * ml, wl[0]), hr = dev_div(ur[4] + wr[4] + R(0.5) * mr, wr[0]);
+    R v2 = R(0), b2 = R(0), x = R(0), vo = R(0), bo = R(0);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const R vd = wl[1 + d] * ql + wr[1 + d] * qr;
+      const R bd = wl[5 + d] * qr + wr[5 + d] * ql;
+      const R db = wl[5 + d] - wr[5 + d];
+      v2 += vd * vd;
+      b2 += bd * bd;
+      x += db * db;
+      if (d == O) { vo = vd; bo = bd; }
+    }
+    x *= R(0.5) * inv * inv;
+    b2 *= inv_prod;
+    const R h = hl * ql + hr * qr;
+    const R a2 = (R(2) - pp.gamma) * x + pp.gm1 * (h - R(0.5) * v2 - b2);
+    const R s = a2 + b2;
+    const R cf = dev_sqrt(R(0.5) * (s + dev_sqrt(s * s - R(4) * a2 * bo * bo * inv_prod)));
+    const R cl = fast_speed<O>(wl, pp), cr = fast_speed<O>(wr, pp);
+    const R a = wl[1 + O] - cl, b = vo - cf;
+    lmin = a < b ? a : b;
+    lmax = dev_fmax(wr[1 + O] + cr, vo + cf);
+  }
   template <int O>
   __device__ __forceinline__ static R max_speed(const R *, const R *wl, const R *, const R *wr, bool naive,
                                                 const PhysParams<R> &pp) {
@@ -483,15 +553,17 @@ __device__ __forceinline__ void ec_flux(const R *ul, const R *wl, const R *ur, c
   else P::template ranocha<O>(ul, wl, ur, wr, f, pp);
 }
 
-// HLL (Harten, Lax, van Leer 1983) with the naive signal-speed estimates:
+// HLL (Harten, Lax, van Leer 1983) with the naive signal-speed estimates
+// (flux_hll) or Einfeldt's (flux_hlle):
 // f_l when lmin >= 0, f_r when lmax <= 0, else
 // (lmax f_l - lmin f_r + lmin lmax (u_r - u_l)) / (lmax - lmin).
 template <int DIM, int EQ, typename R, int O>
 __device__ __forceinline__ void hll_flux(const R *ul, const R *wl, const R *ur, const R *wr, R *f,
-                                         const PhysParams<R> &pp) {
+                                         const PhysParams<R> &pp, bool einfeldt = false) {
   using P = Physics<DIM, EQ, R>;
   R lmin, lmax;
-  P::template min_max_speed<O>(wl, wr, lmin, lmax, pp);
+  if (einfeldt) P::template min_max_speed_einfeldt<O>(ul, wl, ur, wr, lmin, lmax, pp);
+  else P::template min_max_speed<O>(wl, wr, lmin, lmax, pp);
   R fl[P::NV], fr[P::NV];
   P::template flux<O>(ul, wl, fl, pp);
   P::template flux<O>(ur, wr, fr, pp);
@@ -508,15 +580,19 @@ __device__ __forceinline__ void hll_flux(const R *ul, const R *wl, const R *ur, 
   }
 }
 
-// Two-point flux dispatch (kind is warp-uniform).
-template <int DIM, int EQ, typename R, int O>
+// Two-point flux dispatch (kind is warp-uniform).  HLLE = 0 leaves
+// flux_hlle out: the periodic fused kernels are built without it (inlined at
+// their many runtime-dispatched call sites it slowed the 3D shock-capturing
+// kernel by 6 %, out of line by 3 %), and the host sends flux_hlle problems to
+// the instantiations with boundary support, which carry it.
+template <int DIM, int EQ, typename R, int O, int HLLE = 1>
 __device__ __forceinline__ void two_point_flux(int kind, const R *ul, const R *wl, const R *ur, const R *wr, R *f,
                                                const PhysParams<R> &pp) {
   using P = Physics<DIM, EQ, R>;
   if (kind == FLUX_RANOCHA || kind == FLUX_HG) {
     ec_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
-  } else if (kind == FLUX_HLL) {
-    hll_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
+  } else if (kind == FLUX_HLL || (HLLE && kind == FLUX_HLLE)) {
+    hll_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp, HLLE && kind == FLUX_HLLE);
   } else if (kind == FLUX_CENTRAL) {
     P::template central<O>(ul, wl, ur, wr, f, pp);
   } else {

@@ -231,7 +231,7 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   if (d->volume_integral < 0 || d->volume_integral > 2)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "volume_integral %d", d->volume_integral);
   for (int f : {d->volume_flux, d->surface_flux, d->volume_flux_fv})
-    if (f < 0 || f > 6) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux enum %d", f);
+    if (f < 0 || f > 7) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux enum %d", f);
   // flux_shima_etal is a volume flux (flux differencing / the DG part of shock
   // capturing); surface and FV fluxes are the runtime-selected kinds
   if (d->surface_flux == TRIXI_FLUX_SHIMA_ETAL || d->volume_flux_fv == TRIXI_FLUX_SHIMA_ETAL)
@@ -240,8 +240,15 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux_shima_etal needs the Euler equations");
   if (d->volume_flux == TRIXI_FLUX_SHIMA_ETAL && (d->nboundaries > 0 || d->source_terms != TRIXI_SOURCE_NONE))
     return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "flux_shima_etal: periodic meshes without source terms");
-  if (d->volume_flux == TRIXI_FLUX_HLL && d->volume_integral != TRIXI_VOLUME_WEAK_FORM)
-    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "flux_hll as a volume flux");
+  if (d->volume_flux == TRIXI_FLUX_SHIMA_ETAL &&
+      (d->surface_flux == TRIXI_FLUX_HLLE || d->volume_flux_fv == TRIXI_FLUX_HLLE))
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "flux_shima_etal with flux_hlle");
+  if ((d->volume_flux == TRIXI_FLUX_HLL || d->volume_flux == TRIXI_FLUX_HLLE) &&
+      d->volume_integral != TRIXI_VOLUME_WEAK_FORM)
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "flux_hll / flux_hlle as a volume flux");
+  if ((d->surface_flux == TRIXI_FLUX_HLLE || d->volume_flux_fv == TRIXI_FLUX_HLLE) &&
+      d->equation == TRIXI_EQ_LINEAR_ADVECTION)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux_hlle needs the Euler or MHD equations");
   for (int f : {d->volume_flux, d->surface_flux, d->volume_flux_fv}) {
     // flux_hindenlang_gassner is the MHD flux, flux_ranocha the Euler one
     if (f == TRIXI_FLUX_HINDENLANG_GASSNER && !mhd)

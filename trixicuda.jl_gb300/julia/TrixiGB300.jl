@@ -30,6 +30,7 @@ const FLUX_CENTRAL = Int32(2)
 const FLUX_HINDENLANG_GASSNER = Int32(4)
 const FLUX_SHIMA_ETAL = Int32(5)
 const FLUX_HLL = Int32(6)
+const FLUX_HLLE = Int32(7)
 const NONCONSERVATIVE_NONE = Int32(0)
 const NONCONSERVATIVE_POWELL = Int32(1)
 
@@ -90,7 +91,9 @@ flux_code(::typeof(Trixi.flux_central)) = FLUX_CENTRAL
 flux_code(::Trixi.FluxLaxFriedrichs) = FLUX_LAX_FRIEDRICHS
 flux_code(::typeof(Trixi.flux_hindenlang_gassner)) = FLUX_HINDENLANG_GASSNER
 flux_code(::typeof(Trixi.flux_shima_etal)) = FLUX_SHIMA_ETAL
-flux_code(::Trixi.FluxHLL) = FLUX_HLL
+# flux_hll is FluxHLL(min_max_speed_naive); flux_hlle takes Einfeldt's speeds
+flux_code(f::Trixi.FluxHLL) = f.min_max_speed === Trixi.min_max_speed_einfeldt ? FLUX_HLLE : FLUX_HLL
+flux_code(::typeof(Trixi.flux_hlle)) = FLUX_HLLE
 # equations with nonconservative terms pass (flux, nonconservative_flux) tuples
 flux_code(f::Tuple) = flux_code(first(f))
 noncons_code(::Any) = NONCONSERVATIVE_NONE

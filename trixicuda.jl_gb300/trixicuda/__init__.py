@@ -22,6 +22,7 @@ from .equations import (
     flux_central,
     flux_hindenlang_gassner,
     flux_hll,
+    flux_hlle,
     flux_lax_friedrichs,
     flux_lax_friedrichs_naive,
     flux_nonconservative_powell,

@@ -28,7 +28,7 @@ EQ_LINEAR_ADVECTION, EQ_COMPRESSIBLE_EULER, EQ_IDEAL_GLM_MHD = 0, 1, 2
 VOLUME_WEAK_FORM, VOLUME_FLUX_DIFFERENCING, VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
 FLUX_LAX_FRIEDRICHS, FLUX_RANOCHA, FLUX_CENTRAL, FLUX_LAX_FRIEDRICHS_NAIVE = 0, 1, 2, 3
 FLUX_HINDENLANG_GASSNER = 4
-FLUX_SHIMA_ETAL, FLUX_HLL = 5, 6
+FLUX_SHIMA_ETAL, FLUX_HLL, FLUX_HLLE = 5, 6, 7
 NONCONSERVATIVE_NONE, NONCONSERVATIVE_POWELL = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 

@@ -34,6 +34,7 @@ flux = NumericalFlux("flux", -1)  # physical flux (weak form)
 flux_hindenlang_gassner = NumericalFlux("flux_hindenlang_gassner", _lib.FLUX_HINDENLANG_GASSNER)
 flux_shima_etal = NumericalFlux("flux_shima_etal", _lib.FLUX_SHIMA_ETAL)
 flux_hll = NumericalFlux("flux_hll", _lib.FLUX_HLL)
+flux_hlle = NumericalFlux("flux_hlle", _lib.FLUX_HLLE)
 
 
 @dataclass(frozen=True)
