@@ -214,15 +214,6 @@ def test_mhd_boundary_rules():
     assert st == 2 and "source" in msg
 
 
-def test_create_rejects_shima_with_hlle():
-    """flux_hlle is compiled into the kernels with boundary support, which
-    flux_shima_etal does not have."""
-    d, keep, _ = _desc_from_mesh()
-    d.volume_flux, d.surface_flux = 5, 7
-    st, msg = _create(d)
-    assert st == 2 and "flux_hlle" in msg
-
-
 def test_create_rejects_bad_indicator_variable():
     import trixicuda as T
     from trixicuda.semidiscretization import build_problem_desc

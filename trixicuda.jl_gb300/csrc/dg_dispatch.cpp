@@ -19,12 +19,14 @@ bool fused_supported(int dim, int N, int eq, int vol, int vflux) {
 cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed, const FusedHost &h,
                          cudaStream_t s) {
   if (!fused_supported(dim, N, eq, vol, vflux)) return cudaErrorNotSupported;
-  // flux_hlle is compiled into the instantiations with boundary support only
-  // (they run periodic meshes as well)
-  const bool hlle = h.surface_flux == FLUX_HLLE || h.fv_flux == FLUX_HLLE;
+  // the HLL family (flux_hll, flux_hlle) is compiled into the instantiations
+  // with boundary support (they run periodic meshes as well) and into the
+  // flux_shima_etal ones, not into the other periodic kernels
+  const bool hll = (h.surface_flux == FLUX_HLL || h.surface_flux == FLUX_HLLE || h.fv_flux == FLUX_HLL ||
+                    h.fv_flux == FLUX_HLLE) && vflux != FLUX_SHIMA;
   if (eq == 2) {  // ideal GLM-MHD (no source terms)
     if (h.src_kind != 0) return cudaErrorNotSupported;
-    if (h.bc_kind >= 0 || hlle) {  // non-periodic or flux_hlle: the Dirichlet instantiations
+    if (h.bc_kind >= 0 || hll) {  // non-periodic or the HLL family: the Dirichlet instantiations
       switch (dim) {
         case 1: return mixed ? launch_fused_1d_f32_mhd_bnd(N, eq, vol, vflux, h, s) : launch_fused_1d_f64_mhd_bnd(N, eq, vol, vflux, h, s);
         case 2: return mixed ? launch_fused_2d_f32_mhd_bnd(N, eq, vol, vflux, h, s) : launch_fused_2d_f64_mhd_bnd(N, eq, vol, vflux, h, s);
@@ -39,7 +41,7 @@ cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed,
     }
     return cudaErrorNotSupported;
   }
-  if (h.bc_kind >= 0 || h.src_kind != 0 || hlle) {  // the instantiations with boundary states and sources
+  if (h.bc_kind >= 0 || h.src_kind != 0 || hll) {  // the instantiations with boundary states and sources
     if (vflux == 5) return cudaErrorNotSupported;  // flux_shima_etal: periodic kernels only
     switch (dim) {
       case 1:

@@ -198,6 +198,11 @@ template <int DIM, int N, int EQ, typename R, int VOL, int VFLUX, int BND = 0>
 struct FusedKernel {
   using P = Physics<DIM, EQ, R>;
   static constexpr int NV = P::NV;
+  // the HLL family (flux_hll, flux_hlle) as surface / FV flux: in the
+  // instantiations with boundary support, and in the flux_shima_etal ones
+  // (which have no such twin); left out of the other periodic kernels, whose
+  // code it grows by a fifth
+  static constexpr int HLL_FAMILY = (BND || VFLUX == FLUX_SHIMA) ? 1 : 0;
   // nonconservative terms (ideal GLM-MHD in 2D/3D: Powell + GLM transport)
   static constexpr bool NC = (EQ == EQ_MHD && DIM > 1);
   // FV subcell fluxes per interface: one, or with nonconservative terms one
@@ -393,9 +398,9 @@ struct FusedKernel {
       lds_rec<NV>(s.c(el, own), uo);
       lds_rec<NV>(s.w(el, own), wo);
       if (side == 0)
-        two_point_flux<DIM, EQ, R, O, BND>(p.surface_flux, un, wn, uo, wo, f, p.pp);
+        two_point_flux<DIM, EQ, R, O, HLL_FAMILY>(p.surface_flux, un, wn, uo, wo, f, p.pp);
       else
-        two_point_flux<DIM, EQ, R, O, BND>(p.surface_flux, uo, wo, un, wn, f, p.pp);
+        two_point_flux<DIM, EQ, R, O, HLL_FAMILY>(p.surface_flux, uo, wo, un, wn, f, p.pp);
       // nonconservative terms: each side adds 0.5 Phi(own, other)
       // (interface_flux_kernel!, src/solvers/dg_2d_kernel.jl:1009-1035)
       if constexpr (NC) P::template add_noncons<O>(wo, wn, R(0.5), f);
@@ -412,7 +417,7 @@ struct FusedKernel {
     lds_rec<NV>(s.w(el, nl), wl);
     lds_rec<NV>(s.c(el, nr), ur);
     lds_rec<NV>(s.w(el, nr), wr);
-    two_point_flux<DIM, EQ, R, O, BND>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
+    two_point_flux<DIM, EQ, R, O, HLL_FAMILY>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
     if constexpr (NC) {
       R g[NV];
 #pragma unroll

@@ -580,19 +580,20 @@ __device__ __forceinline__ void hll_flux(const R *ul, const R *wl, const R *ur, 
   }
 }
 
-// Two-point flux dispatch (kind is warp-uniform).  HLLE = 0 leaves
-// flux_hlle out: the periodic fused kernels are built without it (inlined at
-// their many runtime-dispatched call sites it slowed the 3D shock-capturing
-// kernel by 6 %, out of line by 3 %), and the host sends flux_hlle problems to
-// the instantiations with boundary support, which carry it.
-template <int DIM, int EQ, typename R, int O, int HLLE = 1>
+// Two-point flux dispatch (kind is warp-uniform).  HLL = 0 leaves the HLL
+// family (flux_hll, flux_hlle) out: the periodic fused kernels are built
+// without it, and the host sends those problems to the instantiations with
+// boundary support, which carry it.  Inlined at the kernels' many
+// runtime-dispatched call sites, flux_hlle alone slowed the 3D
+// shock-capturing kernel by 6 % (out of line, behind a call: 3 %).
+template <int DIM, int EQ, typename R, int O, int HLL = 1>
 __device__ __forceinline__ void two_point_flux(int kind, const R *ul, const R *wl, const R *ur, const R *wr, R *f,
                                                const PhysParams<R> &pp) {
   using P = Physics<DIM, EQ, R>;
   if (kind == FLUX_RANOCHA || kind == FLUX_HG) {
     ec_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
-  } else if (kind == FLUX_HLL || (HLLE && kind == FLUX_HLLE)) {
-    hll_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp, HLLE && kind == FLUX_HLLE);
+  } else if (HLL && (kind == FLUX_HLL || kind == FLUX_HLLE)) {
+    hll_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp, kind == FLUX_HLLE);
   } else if (kind == FLUX_CENTRAL) {
     P::template central<O>(ul, wl, ur, wr, f, pp);
   } else {

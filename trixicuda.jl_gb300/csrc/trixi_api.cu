@@ -240,9 +240,6 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "flux_shima_etal needs the Euler equations");
   if (d->volume_flux == TRIXI_FLUX_SHIMA_ETAL && (d->nboundaries > 0 || d->source_terms != TRIXI_SOURCE_NONE))
     return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "flux_shima_etal: periodic meshes without source terms");
-  if (d->volume_flux == TRIXI_FLUX_SHIMA_ETAL &&
-      (d->surface_flux == TRIXI_FLUX_HLLE || d->volume_flux_fv == TRIXI_FLUX_HLLE))
-    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "flux_shima_etal with flux_hlle");
   if ((d->volume_flux == TRIXI_FLUX_HLL || d->volume_flux == TRIXI_FLUX_HLLE) &&
       d->volume_integral != TRIXI_VOLUME_WEAK_FORM)
     return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "flux_hll / flux_hlle as a volume flux");
