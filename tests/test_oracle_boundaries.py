@@ -104,3 +104,14 @@ def test_convergence_with_dirichlet_boundaries_and_sources(d, levels, min_eoc):
     boundary states follow the RK stage times t + c_s dt)."""
     e0, e1 = (_eoc_error(d, lv) for lv in levels)
     assert np.log2(e0 / e1) > min_eoc, (e0, e1)
+
+
+@pytest.mark.parametrize("d,sflux", [(1, 7), (2, 7), (3, 6)])
+def test_free_stream_with_dirichlet_boundaries_hll_family(d, sflux):
+    """flux_hlle / flux_hll at Dirichlet faces holding the free stream: the
+    HLL fluxes are consistent, so the constant state stays put."""
+    eq = _euler(d)
+    state = np.concatenate([[1.2], 1.2 * np.array([0.3, -0.2, 0.1][:d]), [2.0 / 0.4 + 0.5 * 1.2 * 0.14]])
+    _, cont, orc = _oracle(d, 2, bc=0, bc_params=state, source=0, vol=1, vflux=1, sflux=sflux)
+    u = np.broadcast_to(state, (cont.nelements,) + (4,) * d + (eq.nvariables,)).copy()
+    assert np.max(np.abs(orc.rhs(u, 0.0))) < 1e-12
