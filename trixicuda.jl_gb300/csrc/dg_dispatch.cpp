@@ -24,6 +24,11 @@ cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed,
   // flux_shima_etal ones, not into the other periodic kernels
   const bool hll = (h.surface_flux == FLUX_HLL || h.surface_flux == FLUX_HLLE || h.fv_flux == FLUX_HLL ||
                     h.fv_flux == FLUX_HLLE) && vflux != FLUX_SHIMA;
+  // ... and the entropy-conservative surface / FV flux of shock capturing
+  // is left out of the periodic Euler and advection shock-capturing kernels
+  const bool ec_sc = vol == 2 && eq != 2 && vflux != FLUX_SHIMA &&
+                     (h.surface_flux == FLUX_RANOCHA || h.surface_flux == FLUX_HG ||
+                      h.fv_flux == FLUX_RANOCHA || h.fv_flux == FLUX_HG);
   if (eq == 2) {  // ideal GLM-MHD (no source terms)
     if (h.src_kind != 0) return cudaErrorNotSupported;
     if (h.bc_kind >= 0 || hll) {  // non-periodic or the HLL family: the Dirichlet instantiations
@@ -41,7 +46,7 @@ cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed,
     }
     return cudaErrorNotSupported;
   }
-  if (h.bc_kind >= 0 || h.src_kind != 0 || hll) {  // the instantiations with boundary states and sources
+  if (h.bc_kind >= 0 || h.src_kind != 0 || hll || ec_sc) {  // the instantiations with boundary states and sources
     if (vflux == 5) return cudaErrorNotSupported;  // flux_shima_etal: periodic kernels only
     switch (dim) {
       case 1:

@@ -203,6 +203,11 @@ struct FusedKernel {
   // (which have no such twin); left out of the other periodic kernels, whose
   // code it grows by a fifth
   static constexpr int HLL_FAMILY = (BND || VFLUX == FLUX_SHIMA) ? 1 : 0;
+  // the entropy-conservative flux (flux_ranocha) as the surface or FV flux
+  // of the periodic Euler / advection shock-capturing kernels: likewise left
+  // out (a quarter of their code; the reference's shock-capturing set-ups
+  // take flux_lax_friedrichs there) and served by the boundary-capable twins
+  static constexpr int SC_EC = (HLL_FAMILY || EQ == EQ_MHD || VOL != VOL_SC) ? 1 : 0;
   // nonconservative terms (ideal GLM-MHD in 2D/3D: Powell + GLM transport)
   static constexpr bool NC = (EQ == EQ_MHD && DIM > 1);
   // FV subcell fluxes per interface: one, or with nonconservative terms one
@@ -398,9 +403,9 @@ struct FusedKernel {
       lds_rec<NV>(s.c(el, own), uo);
       lds_rec<NV>(s.w(el, own), wo);
       if (side == 0)
-        two_point_flux<DIM, EQ, R, O, HLL_FAMILY>(p.surface_flux, un, wn, uo, wo, f, p.pp);
+        two_point_flux<DIM, EQ, R, O, HLL_FAMILY, SC_EC>(p.surface_flux, un, wn, uo, wo, f, p.pp);
       else
-        two_point_flux<DIM, EQ, R, O, HLL_FAMILY>(p.surface_flux, uo, wo, un, wn, f, p.pp);
+        two_point_flux<DIM, EQ, R, O, HLL_FAMILY, SC_EC>(p.surface_flux, uo, wo, un, wn, f, p.pp);
       // nonconservative terms: each side adds 0.5 Phi(own, other)
       // (interface_flux_kernel!, src/solvers/dg_2d_kernel.jl:1009-1035)
       if constexpr (NC) P::template add_noncons<O>(wo, wn, R(0.5), f);
@@ -417,7 +422,7 @@ struct FusedKernel {
     lds_rec<NV>(s.w(el, nl), wl);
     lds_rec<NV>(s.c(el, nr), ur);
     lds_rec<NV>(s.w(el, nr), wr);
-    two_point_flux<DIM, EQ, R, O, HLL_FAMILY>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
+    two_point_flux<DIM, EQ, R, O, HLL_FAMILY, SC_EC>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
     if constexpr (NC) {
       R g[NV];
 #pragma unroll

@@ -586,11 +586,11 @@ __device__ __forceinline__ void hll_flux(const R *ul, const R *wl, const R *ur, 
 // boundary support, which carry it.  Inlined at the kernels' many
 // runtime-dispatched call sites, flux_hlle alone slowed the 3D
 // shock-capturing kernel by 6 % (out of line, behind a call: 3 %).
-template <int DIM, int EQ, typename R, int O, int HLL = 1>
+template <int DIM, int EQ, typename R, int O, int HLL = 1, int EC = 1>
 __device__ __forceinline__ void two_point_flux(int kind, const R *ul, const R *wl, const R *ur, const R *wr, R *f,
                                                const PhysParams<R> &pp) {
   using P = Physics<DIM, EQ, R>;
-  if (kind == FLUX_RANOCHA || kind == FLUX_HG) {
+  if (EC && (kind == FLUX_RANOCHA || kind == FLUX_HG)) {
     ec_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp);
   } else if (HLL && (kind == FLUX_HLL || kind == FLUX_HLLE)) {
     hll_flux<DIM, EQ, R, O>(ul, wl, ur, wr, f, pp, kind == FLUX_HLLE);
