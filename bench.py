@@ -31,6 +31,7 @@ import sys
 import tempfile
 import time
 from pathlib import Path
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -471,6 +472,8 @@ def main():
     ap.add_argument("--profile", choices=["mixed", "fp64", "batched-mixed", "batched-fp64", "adjoint", "c3-mixed",
                                           "c3-fp64"], default=None,
                     help="run only the device-timed loop of one precision (for ncu captures)")
+    ap.add_argument("--suite", choices=["reference-benchmarks"], default=None,
+                    help="time rhs_gpu on the reference's own benchmark set-ups (advection, Euler, MHD) instead")
     ap.add_argument("--tile", default=None,
                     help="with --profile mixed/fp64: fixed tile WPGxGPB (e.g. 2x4) instead of the tuner")
     args = ap.parse_args()
@@ -505,6 +508,12 @@ def main():
     T._lib.check(lib.trixi_probe_fma_peak(0, 4096, C.byref(fp64_peak), None))
     T._lib.check(lib.trixi_probe_fma_peak(1, 16384, C.byref(fp32_peak), None))
 
+    if args.suite == "reference-benchmarks":
+        rows = reference_benchmark_suite(device)
+        print(json.dumps({"suite": "reference-benchmarks", "metric": "rhs time", "unit": "us",
+                          "data": "the reference's benchmark set-ups (synthetic initial conditions)",
+                          "cpu_threads": os.cpu_count(), "problems": rows}))
+        return 0
     if args.profile == "adjoint":
         # the adjoint workload (2D Euler level 6, polydeg 4) over `steps` RK steps, store-all
         r = adjoint_path(device, nsteps=max(2, args.steps), snapshots=max(1, args.steps - 1), ndirs=0)
@@ -655,6 +664,125 @@ def c1_path(device):
         torch.cuda.synchronize()
         err = u.cpu().numpy() - exact
         out[f"error_vs_exact_{p}"] = {"l2": float(np.sqrt(np.mean(err ** 2))), "linf": float(np.max(np.abs(err)))}
+    return out
+
+
+def reference_benchmark_problems():
+    """The advection, Euler and ideal GLM-MHD set-ups of the reference's own
+    rhs benchmark (benchmark/{advection,euler,mhd}_*.jl: domain, refinement
+    level and patches, polydeg 3, fluxes, volume integral, initial
+    condition), as (name, set-up) pairs; a set-up holds mesh, equations,
+    initial_condition and solver, and set-up.build(precision) returns the
+    SemidiscretizationHyperbolicGPU.  The reference runs them in Float32;
+    here they run FP32-mixed and FP64.  Its hyperbolic-diffusion and
+    shallow-water set-ups are other equation families, not built."""
+    import trixicuda as T
+
+    pw = lambda f: (f, T.flux_nonconservative_powell)  # noqa: E731
+    box = lambda lo, hi: dict(type="box", coordinates_min=lo, coordinates_max=hi)  # noqa: E731
+
+    def semi(d, lo, hi, level, eq, ic, sflux, vi=None, patches=()):
+        mesh = T.TreeMesh((lo,) * d if np.isscalar(lo) else lo, (hi,) * d if np.isscalar(hi) else hi,
+                          initial_refinement_level=level, refinement_patches=list(patches))
+        solver = T.DGSEMGPU(polydeg=3, surface_flux=sflux, volume_integral=vi or T.VolumeIntegralWeakForm())
+
+        def build(precision):
+            return T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, precision=precision)
+        return SimpleNamespace(mesh=mesh, equations=eq, initial_condition=ic, solver=solver, build=build)
+
+    def shock(eq, vflux, sflux):
+        ind = T.IndicatorHennemannGassner(eq, None, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True)
+        return T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=vflux, volume_flux_fv=sflux)
+
+    cv, wb = T.initial_condition_convergence_test, T.initial_condition_weak_blast_wave
+    llf, rc, hg = T.flux_lax_friedrichs, T.flux_ranocha, T.flux_hindenlang_gassner
+    fd = T.VolumeIntegralFluxDifferencing
+    e1, e2, e3 = (T.CompressibleEulerEquations1D(1.4), T.CompressibleEulerEquations2D(1.4),
+                  T.CompressibleEulerEquations3D(1.4))
+    s2 = float(np.sqrt(2.0))
+    return [
+        ("advection_basic_1d", semi(1, -1.0, 1.0, 3, T.LinearScalarAdvectionEquation1D((1.0,)), cv, llf)),
+        ("advection_basic_2d", semi(2, -1.0, 1.0, 3, T.LinearScalarAdvectionEquation2D((0.2, -0.7)), cv, llf)),
+        ("advection_basic_3d", semi(3, -1.0, 1.0, 3, T.LinearScalarAdvectionEquation3D((0.2, -0.7, 0.5)), cv, llf)),
+        ("advection_mortar_2d", semi(2, -1.0, 1.0, 2, T.LinearScalarAdvectionEquation2D((0.2, -0.7)), cv, llf,
+                                     patches=[box((0.0, -1.0), (1.0, 1.0))])),
+        ("advection_mortar_3d", semi(3, -1.0, 1.0, 2, T.LinearScalarAdvectionEquation3D((0.2, -0.7, 0.5)), cv, llf,
+                                     patches=[box((0.0, -1.0, -1.0), (1.0, 1.0, 1.0)),
+                                              box((0.0, -0.5, -0.5), (0.5, 0.5, 0.5))])),
+        ("euler_ec_1d", semi(1, -2.0, 2.0, 3, e1, wb, rc, fd(rc))),
+        ("euler_ec_2d", semi(2, -2.0, 2.0, 3, e2, wb, rc, fd(rc))),
+        ("euler_ec_3d", semi(3, -2.0, 2.0, 3, e3, wb, rc, fd(rc))),
+        ("euler_shock_1d", semi(1, -2.0, 2.0, 3, e1, wb, llf, shock(e1, T.flux_shima_etal, llf))),
+        ("euler_shock_2d", semi(2, -2.0, 2.0, 3, e2, wb, llf, shock(e2, T.flux_shima_etal, llf))),
+        ("euler_shock_3d", semi(3, -2.0, 2.0, 3, e3, wb, rc, shock(e3, rc, rc))),
+        ("mhd_alfven_wave_1d", semi(1, 0.0, 1.0, 2, T.IdealGlmMhdEquations1D(5.0 / 3.0), cv, llf, fd(hg))),
+        ("mhd_alfven_wave_2d", semi(2, 0.0, s2, 2, T.IdealGlmMhdEquations2D(5.0 / 3.0), cv, pw(llf),
+                                    fd(pw(T.flux_central)))),
+        ("mhd_alfven_wave_3d", semi(3, -1.0, 1.0, 2, T.IdealGlmMhdEquations3D(5.0 / 3.0), cv, pw(llf), fd(pw(hg)))),
+        ("mhd_alfven_wave_mortar_2d", semi(2, 0.0, s2, 2, T.IdealGlmMhdEquations2D(5.0 / 3.0), cv,
+                                           pw(T.flux_hlle), fd(pw(hg)),
+                                           patches=[box((0.25 * s2,) * 2, (0.75 * s2,) * 2)])),
+        ("mhd_alfven_wave_mortar_3d", semi(3, -1.0, 1.0, 2, T.IdealGlmMhdEquations3D(5.0 / 3.0), cv,
+                                           pw(T.flux_hlle), fd(pw(hg)),
+                                           patches=[box((-0.5,) * 3, (0.5,) * 3)])),
+        ("mhd_ec_1d", semi(1, 0.0, 1.0, 2, T.IdealGlmMhdEquations1D(2.0), wb, hg, fd(hg))),
+        ("mhd_ec_2d", semi(2, -2.0, 2.0, 2, T.IdealGlmMhdEquations2D(1.4), wb, pw(hg), fd(pw(hg)))),
+        ("mhd_ec_3d", semi(3, -2.0, 2.0, 2, T.IdealGlmMhdEquations3D(1.4), wb, pw(hg), fd(pw(hg)))),
+    ]
+
+
+def reference_benchmark_suite(device, calls=200, sync_calls=50):
+    """Times rhs_gpu on each set-up of reference_benchmark_problems, as the
+    reference's benchmark scripts time `CUDA.@sync rhs_gpu!` against the CPU
+    `rhs!`: per-call latency with a device synchronisation (host clock,
+    median), back-to-back device time per call (CUDA events over `calls`
+    calls), and the CPU oracle's rhs on all host cores (median of 5)."""
+    import torch
+
+    import trixicuda as T
+    from oracle.oracle import Oracle
+
+    out = []
+    for name, setup in reference_benchmark_problems():
+        row = {"problem": name}
+        for precision in ("mixed", "fp64"):
+            semi = setup.build(precision)
+            u_host = semi.compute_coefficients_host()
+            u = torch.from_numpy(u_host).to(device)
+            du = torch.empty_like(u)
+            for _ in range(5):
+                T.rhs_gpu(du, u, semi, 0.0)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            stream = torch.cuda.current_stream()
+            a.record(stream)
+            for _ in range(calls):
+                T.rhs_gpu(du, u, semi, 0.0)
+            b.record(stream)
+            torch.cuda.synchronize()
+            lat = []
+            for _ in range(sync_calls):
+                t0 = time.perf_counter()
+                T.rhs_gpu(du, u, semi, 0.0)
+                torch.cuda.synchronize()
+                lat.append(time.perf_counter() - t0)
+            row.update({f"{precision}_device_us": a.elapsed_time(b) * 1e3 / calls,
+                        f"{precision}_sync_us": statistics.median(lat) * 1e6})
+            if precision == "fp64":
+                orc = Oracle.from_semi(semi)
+                ref = orc.rhs(u_host)
+                row["fp64_rel_err_vs_oracle"] = float(np.linalg.norm(du.cpu().numpy() - ref) /
+                                                      max(np.linalg.norm(ref), 1e-300))
+                ts = []
+                for _ in range(5):
+                    t0 = time.perf_counter()
+                    orc.rhs(u_host)
+                    ts.append(time.perf_counter() - t0)
+                row["cpu_oracle_us"] = statistics.median(ts) * 1e6
+                row["elements"] = int(semi.nelements)
+                row["dofs"] = int(semi.ndofs())
+            del semi
+        out.append(row)
     return out
 
 

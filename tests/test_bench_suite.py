@@ -1,0 +1,38 @@
+"""The reference-benchmark set-ups of `bench.py --suite reference-benchmarks`
+(no GPU): every set-up builds its containers and passes the library's
+problem validation; only device allocation, which needs a GPU, is left."""
+import ctypes as C
+import sys
+from pathlib import Path
+
+import pytest
+
+sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+import bench  # noqa: E402
+
+
+def test_suite_covers_the_reference_families():
+    names = [n for n, _ in bench.reference_benchmark_problems()]
+    assert len(names) == len(set(names)) == 19
+    for fam, count in (("advection_", 5), ("euler_", 6), ("mhd_", 8)):
+        assert sum(n.startswith(fam) for n in names) == count
+
+
+@pytest.mark.parametrize("name", [n for n, _ in bench.reference_benchmark_problems()])
+def test_suite_problem_passes_validation(name):
+    import trixicuda as T
+    from trixicuda import _lib
+    from trixicuda.semidiscretization import build_problem_desc
+
+    setup = dict(bench.reference_benchmark_problems())[name]
+    d, keep, cont = build_problem_desc(setup.mesh, setup.equations, setup.solver)
+    assert cont.nelements > 0
+    if name.endswith("mortar_2d") or name.endswith("mortar_3d"):
+        assert cont.nmortars > 0
+    lib = _lib.load()
+    h = C.c_void_p()
+    st = lib.trixi_create(C.byref(d), C.byref(h))
+    if st == 0:
+        lib.trixi_destroy(h)
+    # INVALID_ARGUMENT (1) / UNSUPPORTED (2) would mean the set-up is refused
+    assert st not in (1, 2), _lib.last_error()
