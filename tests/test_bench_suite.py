@@ -36,3 +36,14 @@ def test_suite_problem_passes_validation(name):
         lib.trixi_destroy(h)
     # INVALID_ARGUMENT (1) / UNSUPPORTED (2) would mean the set-up is refused
     assert st not in (1, 2), _lib.last_error()
+
+
+def test_nan_aware_error():
+    import numpy as np
+
+    ref = np.array([1.0, 2.0, np.nan, 4.0])
+    r = bench._nan_aware_rel_err(np.array([1.0, 2.0, np.nan, 4.0 + 1e-12]), ref)
+    assert r["nan_positions_match"] and r["nonfinite_entries"] == 1
+    assert 0 < r["fp64_rel_err_vs_oracle"] < 1e-12
+    r = bench._nan_aware_rel_err(np.array([1.0, np.nan, 3.0, 4.0]), ref)
+    assert not r["nan_positions_match"]
