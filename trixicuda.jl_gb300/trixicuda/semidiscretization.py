@@ -17,6 +17,7 @@ current torch stream; none of them has a CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -312,7 +313,7 @@ class ODEProblem:
 
 def _check_state(semi, *arrays):
     torch = _torch()
-    n = int(np.prod(semi.u_shape()))
+    n = int(math.prod(semi.u_shape()))  # (np.prod costs ~3 us per call, on every rhs)
     for a in arrays:
         if not isinstance(a, torch.Tensor) or a.dtype != torch.float64 or not a.is_cuda:
             raise TypeError("state arrays must be float64 CUDA tensors")
