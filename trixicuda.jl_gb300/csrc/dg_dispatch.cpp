@@ -22,8 +22,9 @@ cudaError_t launch_fused(int dim, int N, int eq, int vol, int vflux, bool mixed,
   // the HLL family (flux_hll, flux_hlle) is compiled into the instantiations
   // with boundary support (they run periodic meshes as well) and into the
   // flux_shima_etal ones, not into the other periodic kernels
-  const bool hll = (h.surface_flux == FLUX_HLL || h.surface_flux == FLUX_HLLE || h.fv_flux == FLUX_HLL ||
-                    h.fv_flux == FLUX_HLLE) && vflux != FLUX_SHIMA;
+  // (the FV flux counts for shock capturing only)
+  const bool fv_hll = vol == 2 && (h.fv_flux == FLUX_HLL || h.fv_flux == FLUX_HLLE);
+  const bool hll = (h.surface_flux == FLUX_HLL || h.surface_flux == FLUX_HLLE || fv_hll) && vflux != FLUX_SHIMA;
   // ... and the entropy-conservative surface / FV flux of shock capturing
   // is left out of the periodic Euler and advection shock-capturing kernels
   const bool ec_sc = vol == 2 && eq != 2 && vflux != FLUX_SHIMA &&
