@@ -551,9 +551,12 @@ struct FusedKernel {
     const int n_all = NVOL_ITEMS + n_surf + DIM * PER_FV;
     for (int w = gt; w < n_all; w += GTr) {
       if (w < NVOL_ITEMS) {
-        const int dir = w / PER_VOL;
-        const int r0 = w - dir * PER_VOL;
-        const int el = r0 / VOL_PER_DIR, r = r0 - (r0 / VOL_PER_DIR) * VOL_PER_DIR;
+        // (the divisors are never 0 where this runs; the guards only keep the
+        // kernels without volume items, LINEAR, free of a constant division by 0)
+        constexpr int PV = PER_VOL > 0 ? PER_VOL : 1, VD = VOL_PER_DIR > 0 ? VOL_PER_DIR : 1;
+        const int dir = w / PV;
+        const int r0 = w - dir * PV;
+        const int el = r0 / VD, r = r0 - (r0 / VD) * VD;
         if (el >= ne) continue;
         if (dir == 0) volume_item<0>(p, s, el, r);
         if constexpr (DIM > 1) if (dir == 1) volume_item<1>(p, s, el, r);
