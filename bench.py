@@ -76,6 +76,20 @@ def build_problem_c3(precision: str):
     return mesh, eq, T.initial_condition_weak_blast_wave, solver
 
 
+def build_problem_c4(precision: str = "fp64"):
+    """The adjoint configuration: 2D Euler (flux_ranocha volume + surface) on
+    [-2,2]^2 periodic, level 6 (4096 elements), polydeg 4, seeded Fourier
+    initial condition (|k| <= 8)."""
+    import trixicuda as T
+
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEMGPU(polydeg=4, surface_flux=T.flux_ranocha,
+                        volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((-2.0, -2.0), (2.0, 2.0), initial_refinement_level=6)
+    ic = T.initial_condition_fourier_euler(eq, seed=20261203, kmax=8)
+    return mesh, eq, ic, solver
+
+
 def stable_dt(semi, level=LEVEL) -> float:
     """CFL 0.5 time step from the initial state (max |v| + c)."""
     u = semi.compute_coefficients_host().reshape(-1, semi.equations.nvariables).T
@@ -272,11 +286,7 @@ def adjoint_path(device, nsteps=200, snapshots=15, ndirs=16):
     import trixicuda as T
     from trixicuda import adjoint as ADJ
 
-    eq = T.CompressibleEulerEquations2D(1.4)
-    solver = T.DGSEMGPU(polydeg=4, surface_flux=T.flux_ranocha,
-                        volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
-    mesh = T.TreeMesh((-2.0, -2.0), (2.0, 2.0), initial_refinement_level=6)
-    ic = T.initial_condition_fourier_euler(eq, seed=20261203, kmax=8)
+    mesh, eq, ic, solver = build_problem_c4()
     semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver)
     u0 = semi.compute_coefficients()
     x = semi.containers.node_coordinates.reshape(-1, 2).T
@@ -400,23 +410,16 @@ def e2e_path(precision, steps, warmup, device, slots=3):
 
 def cpu_baseline(seconds_target=8.0, nthreads=None):
     """The oracle (CPU restatement, OpenMP) on a bounded sample of the same
-    workload: whole CK2N54 steps of the full level-7 mesh."""
-    import trixicuda as T
+    workload: whole CK2N54 steps of the full level-7 mesh.  Built from oracle
+    code alone (oracle/workloads.py: its own mesh, basis and initial
+    condition), so this leg neither imports trixicuda nor loads
+    libtrixi_b200.so."""
     from oracle import oracle as O
+    from oracle.workloads import euler2d_fd_workload
 
     nthreads = nthreads or os.cpu_count() or 1
     O.set_threads(nthreads)
-    mesh, eq, ic, solver = build_problem("fp64")
-    cont = mesh.build_containers(solver.basis.nodes)
-
-    class _S:
-        pass
-
-    s = _S()
-    s.equations, s.solver, s.containers = eq, solver, cont
-    orc = O.Oracle.from_semi(s)
-    x = cont.node_coordinates.reshape(-1, 2).T
-    u = np.ascontiguousarray(ic(x, 0.0, eq).T.reshape((cont.nelements, 4, 4, 4)))
+    orc, u, nelements = euler2d_fd_workload(LEVEL, POLYDEG)
     orc.rhs(u)  # warm-up
     t = time.perf_counter()
     orc.rk_ck2n54(u, 0.0, 1e-4, 1)
@@ -425,7 +428,7 @@ def cpu_baseline(seconds_target=8.0, nthreads=None):
     t = time.perf_counter()
     orc.rk_ck2n54(u, 0.0, 1e-4, nsteps)
     el = time.perf_counter() - t
-    dofs = cont.nelements * (POLYDEG + 1) ** 2
+    dofs = nelements * (POLYDEG + 1) ** 2
     return {"value": 5 * dofs * nsteps / el, "unit": METRIC, "cores": nthreads, "kind": "port",
             "sample": f"{nsteps} CarpenterKennedy2N54 steps (5 rhs each) of the full level-7 workload, FP64, "
                       f"oracle/trixi_oracle.c (CPU restatement of the reference algorithm, not Trixi.jl)",
@@ -505,8 +508,9 @@ def main():
     lib = T._lib.load()
     fp64_peak = C.c_double()
     fp32_peak = C.c_double()
-    T._lib.check(lib.trixi_probe_fma_peak(0, 4096, C.byref(fp64_peak), None))
-    T._lib.check(lib.trixi_probe_fma_peak(1, 16384, C.byref(fp32_peak), None))
+    diag = T._lib.load_diag()
+    T._lib.check(diag.trixi_diag_fma_peak(0, 4096, C.byref(fp64_peak), None))
+    T._lib.check(diag.trixi_diag_fma_peak(1, 16384, C.byref(fp32_peak), None))
 
     if args.suite == "reference-benchmarks":
         rows = reference_benchmark_suite(device)

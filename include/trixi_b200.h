@@ -5,8 +5,8 @@
  * The library replaces the device side of TrixiCUDA.jl's `rhs_gpu!` path
  * (the `cuda_*` stage launchers and their CUDA.jl kernels).  Julia keeps its
  * `DGSEMGPU` / `SemidiscretizationHyperbolicGPU` / `semidiscretizeGPU` API and
- * calls these entry points with `ccall`; the binding is shown in
- * INTEGRATION.md.  All arrays use the reference's layouts (column-major,
+ * calls these entry points with `ccall` (julia/TrixiGB300.jl holds the
+ * binding).  All arrays use the reference's layouts (column-major,
  * first index fastest, integer tables 1-based Int64):
  *
  *   u, du, k             [nvars, N, (N, (N,)) nelements]           src/solvers/dg.jl:14-20
@@ -267,19 +267,33 @@ int trixi_indicator(trixi_handle *h, const double *u, double *alpha, void *strea
  *   TRIXI_IC_CONVERGENCE_TEST  params = (c, A, L); advection default (1, 0.5, 2),
  *                              Euler default (2, 0.1, 2); ideal GLM-MHD: the
  *                              smooth Alfven waves, no params
- *   TRIXI_IC_WEAK_BLAST_WAVE   Euler, ideal GLM-MHD (in B = (1, 1, 1)); no params */
+ *   TRIXI_IC_WEAK_BLAST_WAVE   Euler, ideal GLM-MHD (in B = (1, 1, 1)); no params
+ *   TRIXI_IC_EOC_TEST_COUPLED_EULER_GRAVITY
+ *                              Euler: the manufactured solution of the
+ *                              Euler-gravity convergence test,
+ *                              rho = 2 + 0.1 sin(pi (sum_d x_d - t)), v_d = 1,
+ *                              p = 2 G rho^2 / (ndims pi) with G = 1 (the
+ *                              pressure of hydrostatic balance with the
+ *                              gravitational potential of rho); no params
+ *                              (test/tree_dgsem_3d/euler_convergence.jl:11) */
 typedef enum trixi_initial_condition_kind {
   TRIXI_IC_CONSTANT = 0,
   TRIXI_IC_CONVERGENCE_TEST = 1,
-  TRIXI_IC_WEAK_BLAST_WAVE = 2
+  TRIXI_IC_WEAK_BLAST_WAVE = 2,
+  TRIXI_IC_EOC_TEST_COUPLED_EULER_GRAVITY = 3
 } trixi_initial_condition_kind;
 
-/* Source terms (desc.source_terms): the Euler convergence test's
- * source_terms_convergence_test, the source of its manufactured solution
- * rho = rho v_d = c + A sin(2 pi/L (sum_d x_d - t)), E = rho^2. */
+/* Source terms (desc.source_terms), Euler only:
+ *   TRIXI_SOURCE_CONVERGENCE_TEST  source_terms_convergence_test, the source of
+ *       the manufactured solution rho = rho v_d = c + A sin(2 pi/L (sum_d x_d - t)),
+ *       E = rho^2;
+ *   TRIXI_SOURCE_EOC_TEST_EULER    source_terms_eoc_test_euler, the source that
+ *       makes TRIXI_IC_EOC_TEST_COUPLED_EULER_GRAVITY an exact solution of the
+ *       Euler equations without gravity (test/tree_dgsem_3d/euler_convergence.jl:24). */
 typedef enum trixi_source_terms_kind {
   TRIXI_SOURCE_NONE = 0,
-  TRIXI_SOURCE_CONVERGENCE_TEST = 1
+  TRIXI_SOURCE_CONVERGENCE_TEST = 1,
+  TRIXI_SOURCE_EOC_TEST_EULER = 2
 } trixi_source_terms_kind;
 
 /* u = initial condition at the nodes (needs desc.node_coordinates); 1D
@@ -311,8 +325,10 @@ typedef enum trixi_integral_kind {
 int trixi_integrate(trixi_handle *h, const double *u, const double *du, int which, double *out_host, int64_t count,
                     void *stream);
 
-/* The integrals of trixi_integrate for callers that cannot allocate device
- * memory.  No counterpart in the reference: it exists for callers whose GPU
+/* The integrals of trixi_integrate, for linear advection and compressible
+ * Euler (equation TRIXI_EQ_LINEAR_ADVECTION or TRIXI_EQ_COMPRESSIBLE_EULER;
+ * ideal GLM-MHD is refused with TRIXI_ERR_INVALID_ARGUMENT -- use
+ * trixi_integrate), for callers that cannot allocate device memory.  No counterpart in the reference: it exists for callers whose GPU
  * memory belongs to another allocator (a CUDA.jl or PyTorch caching pool that
  * has reserved the device) and for loops that must not pay the device-wide
  * synchronisation of cudaMalloc / cudaFree.  It needs no handle and calls no
@@ -346,19 +362,6 @@ int trixi_basis(const trixi_handle *h, int which, double *host_out, int64_t coun
 
 /* Same operators without a handle (pure host code, no GPU needed). */
 int trixi_lgl_basis(int polydeg, int which, double *host_out, int64_t count);
-
-/* Diagnostic without a counterpart in the reference: measures the CUDA-core
- * FMA throughput (FLOP/s, 2 per FMA) of the current device in FP64
- * (TRIXI_PRECISION_FP64) or FP32 (TRIXI_PRECISION_MIXED), the roofline of
- * the flux-differencing kernels.  Synchronizes the stream. */
-int trixi_probe_fma_peak(int precision, int iters, double *flops_per_s, void *stream);
-
-/* Diagnostic without a counterpart in the reference: the mixed-precision
- * kernels' integer-pipe conversions (double -> float, round to nearest even;
- * float -> double, exact) applied elementwise to device arrays of length n,
- * so that tests can compare them bit for bit with the hardware conversions. */
-int trixi_probe_convert(const double *in_d, float *out_f, const float *in_f, double *out_d, int64_t n,
-                        void *stream);
 
 /* ---- Batched ensembles (no counterpart in the reference, which solves one
  * problem at a time) --------------------------------------------------------

@@ -164,9 +164,23 @@ class Oracle:
         self.nelements = containers.nelements
         self.nchild = 2 ** (ndims - 1)
 
+    @staticmethod
+    def own_containers(mesh, polydeg):
+        """The oracle's own connectivity for a TreeMesh's parameters (domain,
+        level, refinement boxes, periodicity), built by oracle/treemesh.py
+        with the oracle's LGL nodes -- no product code involved."""
+        from .treemesh import OracleTreeMesh
+
+        tm = OracleTreeMesh(mesh.coordinates_min, mesh.coordinates_max, mesh.initial_refinement_level,
+                            getattr(mesh, "refinement_patches", ()), getattr(mesh, "periodicity", True))
+        return tm.containers(basis(polydeg)["nodes"])
+
     @classmethod
     def from_semi(cls, semi):
-        """Oracle for the same problem as a SemidiscretizationHyperbolicGPU."""
+        """Oracle for the same problem as a SemidiscretizationHyperbolicGPU.
+        When the semi carries its TreeMesh, the oracle computes on its own
+        connectivity (own_containers); a semi that only carries containers
+        (a partition's local mesh with ghosts) is taken as given."""
         from trixicuda.semidiscretization import flux_codes
         from trixicuda.solver import VolumeIntegralShockCapturingHG
 
@@ -193,7 +207,9 @@ class Oracle:
             kw.update(boundary_function=code, boundary_params=params)
         if d is not None and d.source_terms:
             kw.update(source_terms=int(d.source_terms))
-        return cls(semi.containers, eq.ndims, sol.polydeg, eq.nvariables, eq.code,
+        mesh = getattr(semi, "mesh", None)
+        cont = cls.own_containers(mesh, sol.polydeg) if hasattr(mesh, "initial_refinement_level") else semi.containers
+        return cls(cont, eq.ndims, sol.polydeg, eq.nvariables, eq.code,
                    gamma=getattr(eq, "gamma", 1.4), advection_velocity=av, **kw)
 
     def __del__(self):

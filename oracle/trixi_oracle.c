@@ -1159,6 +1159,20 @@ void oracle_eval_ic(oracle_handle *h, int kind, const double *params, const doub
     u[DIM + 1] = ini * ini;
     return;
   }
+  if (kind == ORC_IC_EOC_EULER_GRAVITY) {
+    /* Euler-gravity convergence test (Schlottke-Lakemper et al., JCP 442 (2021)):
+     * rho = 2 + 0.1 sin(pi (sum x - t)), v_d = 1, and the pressure of
+     * hydrostatic balance grad p = -rho grad phi with lap phi = 4 pi G rho,
+     * G = 1: p = 2 rho^2 / (DIM pi) */
+    double sx = 0.0;
+    for (int d = 0; d < DIM; ++d) sx += x[d];
+    const double rho = 2.0 + 0.1 * sin(ORC_PI * (sx - t));
+    const double p = 2.0 * rho * rho / (DIM * ORC_PI);
+    u[0] = rho;
+    for (int d = 0; d < DIM; ++d) u[1 + d] = rho;
+    u[DIM + 1] = p / (h->P.gamma - 1.0) + 0.5 * rho * DIM;
+    return;
+  }
   /* weak blast wave: r <= 0.5: rho 1.1691, radial velocity 0.1882, p 1.245; else 1, 0, 1.
    * The radial direction from the polar angles phi = atan2(y, x) (and
    * theta = acos(z / r) in 3D), so that the centre itself moves along phi = 0
@@ -1274,8 +1288,43 @@ static void source_convergence(int DIM, double g, const double *prm, const doubl
   }
 }
 
+/* Source of the Euler-gravity convergence test without gravity
+ * (source_terms_eoc_test_euler of test/tree_dgsem_3d/euler_convergence.jl:24):
+ * S_q = d U_q/dt + sum_k d F_k,q / dx_k on the manufactured solution of
+ * ORC_IC_EOC_EULER_GRAVITY, by the chain rule in the phase
+ * xi = pi (sum x - t): d/dt = -r', d/dx_k = +r' with r' = pi A cos(xi) times
+ * the derivative in rho; U = (rho, rho [DIM], E), F_k = (rho, rho + delta_ik p,
+ * E + p) as v = 1; E(rho) = p/(g-1) + DIM rho/2, p(rho) = K rho^2, K = 2/(DIM pi). */
+static void source_eoc_euler(int DIM, double g, const double *x, double t, double *s) {
+  const double A = 0.1, K = 2.0 / (DIM * ORC_PI);
+  double sx = 0.0;
+  for (int d = 0; d < DIM; ++d) sx += x[d];
+  const double rho = 2.0 + A * sin(ORC_PI * (sx - t));
+  const double rp = ORC_PI * A * cos(ORC_PI * (sx - t));
+  const double dp = 2.0 * K * rho, dE = dp / (g - 1.0) + 0.5 * DIM;
+  s[0] = -rp;
+  for (int k = 0; k < DIM; ++k) s[0] += rp;
+  for (int i = 0; i < DIM; ++i) {
+    s[1 + i] = -rp;
+    for (int k = 0; k < DIM; ++k) s[1 + i] += rp * (1.0 + (k == i ? dp : 0.0));
+  }
+  s[DIM + 1] = -dE * rp;
+  for (int k = 0; k < DIM; ++k) s[DIM + 1] += (dE + dp) * rp;
+}
+
 void oracle_sources(oracle_handle *h, double *du, double t) {
-  if (h->d.source_terms != ORC_SRC_CONVERGENCE_TEST || h->P.eq != ORC_EQ_EULER) return;
+  if (h->d.source_terms == ORC_SRC_NONE || h->P.eq != ORC_EQ_EULER) return;
+  if (h->d.source_terms == ORC_SRC_EOC_EULER) {
+    const int NN = h->NN, NV = h->NV;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < h->d.nelements; ++e)
+      for (int n = 0; n < NN; ++n) {
+        double s[NVMAX];
+        source_eoc_euler(h->DIM, h->P.gamma, node_x(h, e, n), t, s);
+        for (int v = 0; v < NV; ++v) du[v + NV * (n + (int64_t)NN * e)] += s[v];
+      }
+    return;
+  }
   const int NN = h->NN, NV = h->NV;
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < h->d.nelements; ++e)

@@ -39,8 +39,8 @@ enum { ORC_VOL_WEAK = 0, ORC_VOL_FLUXDIFF = 1, ORC_VOL_SHOCK_HG = 2 };
 enum { ORC_FLUX_LLF = 0, ORC_FLUX_RANOCHA = 1, ORC_FLUX_CENTRAL = 2, ORC_FLUX_LLF_NAIVE = 3,
        ORC_FLUX_HINDENLANG_GASSNER = 4, ORC_FLUX_SHIMA_ETAL = 5, ORC_FLUX_HLL = 6,
        ORC_FLUX_HLLE = 7 };
-enum { ORC_IC_CONSTANT = 0, ORC_IC_CONVERGENCE_TEST = 1, ORC_IC_WEAK_BLAST_WAVE = 2 };
-enum { ORC_SRC_NONE = 0, ORC_SRC_CONVERGENCE_TEST = 1 };
+enum { ORC_IC_CONSTANT = 0, ORC_IC_CONVERGENCE_TEST = 1, ORC_IC_WEAK_BLAST_WAVE = 2, ORC_IC_EOC_EULER_GRAVITY = 3 };
+enum { ORC_SRC_NONE = 0, ORC_SRC_CONVERGENCE_TEST = 1, ORC_SRC_EOC_EULER = 2 };
 
 typedef struct {
   int32_t ndims, polydeg, nvars, equation;

@@ -24,7 +24,10 @@ CASES = [("euler_fd", 2, 2, 3, None, {}), ("euler_fd", 3, 1, 3, None, {}), ("eul
          ("euler_fd", 2, 2, 3, None, dict(surface_flux=T.flux_ranocha, volume_flux=T.flux_central)),
          ("euler_fd", 2, 2, 4, None, dict(surface_flux=T.flux_central, volume_flux=T.flux_ranocha)),
          ("adv_weak", 2, 2, 3, None, {}), ("adv_weak", 1, 3, 3, None, {}), ("adv_fd", 3, 1, 3, None, {}),
-         ("adv_weak", 2, 2, 3, None, dict(surface_flux=T.flux_central))]
+         ("adv_weak", 2, 2, 3, None, dict(surface_flux=T.flux_central)),
+         # flux_hll on linear advection is the upwind flux (signal speeds lmin = lmax = a)
+         ("adv_weak", 2, 2, 3, None, dict(surface_flux=T.flux_hll)),
+         ("adv_weak", 1, 3, 3, None, dict(surface_flux=T.flux_hll))]
 
 
 @pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}-{c[1]}d-p{c[3]}-{c[4]}-{len(c[5])}" for c in CASES])

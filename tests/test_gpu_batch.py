@@ -93,6 +93,6 @@ def test_batch_matches_oracle(cuda):
             pass
 
         s = _S()
-        s.equations, s.solver, s.containers = pb.equations, pb.solver, batch.containers[i]
+        s.equations, s.solver, s.containers, s.mesh = pb.equations, pb.solver, batch.containers[i], pb.mesh
         ref = Oracle.from_semi(s).rhs(hosts[i])
         assert_rel(batch.view(du, i).cpu().numpy(), ref, 1e-12, f"instance {i}")

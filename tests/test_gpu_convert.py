@@ -32,8 +32,8 @@ def test_integer_conversions_match_hardware(cuda):
     tf = cuda.from_numpy(f).to(dev)
     of = cuda.empty(d.size, dtype=cuda.float32, device=dev)
     od = cuda.empty(d.size, dtype=cuda.float64, device=dev)
-    st = _lib.load().trixi_probe_convert(C.c_void_p(td.data_ptr()), C.c_void_p(of.data_ptr()),
-                                         C.c_void_p(tf.data_ptr()), C.c_void_p(od.data_ptr()), d.size, None)
+    st = _lib.load_diag().trixi_diag_convert(C.c_void_p(td.data_ptr()), C.c_void_p(of.data_ptr()),
+                                            C.c_void_p(tf.data_ptr()), C.c_void_p(od.data_ptr()), d.size, None)
     assert st == 0
     cuda.cuda.synchronize()
     hw_f = td.float()

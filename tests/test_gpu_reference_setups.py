@@ -77,3 +77,50 @@ def test_euler_source_terms_periodic(d, level, polydeg, refined, cuda):
     if refined:
         assert semi.containers.nmortars > 0
     _check(semi, orc, cuda)
+
+
+@pytest.mark.parametrize("d,level,precision", [(3, 2, "fp64"), (2, 3, "fp64"), (3, 2, "mixed")])
+def test_euler_convergence_euler_gravity(d, level, precision, cuda):
+    """test/tree_dgsem_3d/euler_convergence.jl: gamma = 2,
+    initial_condition_eoc_test_coupled_euler_gravity,
+    source_terms_eoc_test_euler, flux_hll surface flux, weak form, periodic
+    [0, 2]^3 at level 2 (and the 2D analogue): rhs, the stage functions and RK
+    steps against the oracle; FP32-mixed within the mixed bar (5e-4)."""
+    eq = {2: T.CompressibleEulerEquations2D, 3: T.CompressibleEulerEquations3D}[d](2.0)
+    mesh = T.TreeMesh((0.0,) * d, (2.0,) * d, initial_refinement_level=level)
+    solver = T.DGSEMGPU(polydeg=3, surface_flux=T.flux_hll, volume_integral=T.VolumeIntegralWeakForm())
+    semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, T.initial_condition_eoc_test_coupled_euler_gravity, solver,
+                                             source_terms=T.source_terms_eoc_test_euler, precision=precision)
+    orc = Oracle.from_semi(semi)
+    if precision == "mixed":
+        u_host = semi.compute_coefficients_host()
+        u = cuda.from_numpy(u_host).to(semi.device)
+        du = cuda.empty_like(u)
+        T.rhs_gpu(du, u, semi, 0.0)
+        T.synchronize(semi)
+        assert_rel(du.cpu().numpy(), orc.rhs(u_host), 5e-4, "mixed rhs")
+        return
+    _check(semi, orc, cuda)
+    # stage by stage, as the reference test does
+    u_host = semi.compute_coefficients_host()
+    u = cuda.from_numpy(u_host).to(semi.device)
+    du = cuda.empty_like(u)
+    T.cuda_volume_integral(du, u, semi)
+    du_o = orc.volume_integral(u_host)
+    assert_rel(du.cpu().numpy(), du_o, 1e-12, "volume integral")
+    T.cuda_prolong2interfaces(u, semi)
+    T.cuda_interface_flux(semi)
+    T.cuda_prolong2boundaries(u, semi)
+    T.cuda_boundary_flux(0.0, semi)
+    T.cuda_prolong2mortars(u, semi)
+    T.cuda_mortar_flux(semi)
+    sfv_o = orc.interface_flux(orc.prolong2interfaces(u_host))
+    sfv = semi.container(T._lib.CONTAINER_SURFACE_FLUX_VALUES)
+    assert_rel(sfv.cpu().numpy(), sfv_o, 1e-12, "surface_flux_values (flux_hll)")
+    T.cuda_surface_integral(du, semi)
+    T.cuda_jacobian(du, semi)
+    T.cuda_sources(du, u, 0.0, semi)
+    T.synchronize(semi)
+    du_o = orc.sources(orc.jacobian(orc.surface_integral(du_o, sfv_o)), 0.0)
+    assert_rel(du.cpu().numpy(), du_o, 1e-12, "after cuda_sources")
+    assert_rel(du.cpu().numpy(), orc.rhs(u_host), 1e-12, "staged == oracle rhs")

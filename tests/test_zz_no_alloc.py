@@ -78,3 +78,46 @@ def test_noalloc_integrate_rejects_oversize(cuda):
                                      MAX_PARTIALS // 4 + 1, _lib.INTEGRAL_STATE, C.c_void_p(out.data_ptr()), None)
     assert st == 1  # TRIXI_ERR_INVALID_ARGUMENT
     assert "exceed" in _lib.last_error()
+
+
+CASES = [("adv_weak", 1, 4), ("adv_weak", 2, 3), ("adv_weak", 3, 2), ("euler_fd", 1, 4), ("euler_fd", 3, 2),
+         ("euler_sc", 3, 2)]
+KINDS = [(_lib.INTEGRAL_STATE, "state"), (_lib.INTEGRAL_ENTROPY, "entropy"),
+         (_lib.INTEGRAL_ENTROPY_PRODUCTION, "entropy_production"), (_lib.INTEGRAL_DU, "du")]
+
+
+@pytest.mark.parametrize("kind,d,level", CASES, ids=[f"{k}-{d}d" for k, d, _ in CASES])
+def test_noalloc_every_integral_kind(kind, d, level, cuda):
+    """Every integral kind, for linear advection and Euler in 1D/2D/3D: two
+    calls in a row through the C ABI, each against trixi_integrate."""
+    torch = cuda
+    lib = _lib.load()
+    mesh, eq, ic, solver, precision = make(kind, d, level, polydeg=3)
+    semi = T.SemidiscretizationHyperbolicGPU(mesh, eq, ic, solver, precision=precision)
+    u = semi.compute_coefficients()
+    du = torch.empty_like(u)
+    T.rhs_gpu(du, u, semi, 0.0)
+    inv_jac = torch.from_numpy(np.ascontiguousarray(semi.containers.inverse_jacobian)).to(u.device)
+    stream = torch.cuda.current_stream(u.device)
+    nv = eq.nvariables
+    # magnitudes for the integrals that are zero up to round-off (conservation
+    # of du, entropy production of entropy-conservative fluxes)
+    du_scale = np.abs(T.integrate(du.abs(), semi, "state")[:nv])
+    ent_scale = abs(T.integrate(u, semi, "entropy")[0])
+    out = torch.full((16,), np.nan, dtype=torch.float64, device=u.device)
+    for which, name in KINDS:
+        nq = nv if name in ("state", "du") else 1
+        ref = T.integrate(u, semi, name, du=du)[:nq]
+        for call in range(2):
+            out.fill_(np.nan)
+            st = _noalloc(lib, semi, u, du, inv_jac, which, out, stream.cuda_stream)
+            assert st == _lib.TRIXI_OK, _lib.last_error()
+            stream.synchronize()
+            got = out[:nq].cpu().numpy()
+            assert np.all(np.isnan(out[nq:].cpu().numpy())), "wrote beyond its results"
+            if name == "du":
+                assert np.all(np.abs(got - ref) <= RTOL64 * np.maximum(du_scale, np.abs(ref))), (name, call, got, ref)
+            elif name == "entropy_production":
+                assert abs(got[0] - ref[0]) <= RTOL64 * max(ent_scale, abs(ref[0])), (name, call, got, ref)
+            else:
+                assert_rel(got, ref, RTOL64, f"noalloc {name}, call {call}")

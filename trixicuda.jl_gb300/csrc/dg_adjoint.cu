@@ -10,7 +10,13 @@ namespace trixi {
 bool adjoint_supported(int dim, int N, int eq, int vol, int vflux, int sflux, bool has_mortars) {
   if (has_mortars || dim < 1 || dim > 3 || N < 2 || N > HOST_NMAX) return false;
   auto smooth_flux = [](int f) { return f == FLUX_RANOCHA || f == FLUX_CENTRAL; };
-  if (eq == EQ_ADV) return vol == VOL_WEAK || (vol == VOL_FD && vflux == FLUX_CENTRAL);
+  if (eq == EQ_ADV) {
+    // surface fluxes whose cotangents Adjoint<DIM, EQ_ADV>::two_point_vjp forms:
+    // the upwind family (LLF, HLL) and the central average (central, ranocha)
+    const bool sflux_ok = sflux == FLUX_LLF || sflux == FLUX_LLF_NAIVE || sflux == FLUX_HLL ||
+                          sflux == FLUX_CENTRAL || sflux == FLUX_RANOCHA;
+    return sflux_ok && (vol == VOL_WEAK || (vol == VOL_FD && vflux == FLUX_CENTRAL));
+  }
   return vol == VOL_FD && smooth_flux(vflux) && smooth_flux(sflux);
 }
 

@@ -65,7 +65,9 @@ struct Adjoint<DIM, EQ_ADV> {
                                                       const double *, const double *, double, const double *g,
                                                       double *ul_bar, double *ur_bar, const PhysParams<double> &pp) {
     const double a = pp.a[O];
-    if (kind == FLUX_LLF || kind == FLUX_LLF_NAIVE) {
+    // LLF with |a| and HLL with the signal speeds lmin = lmax = a are both the
+    // upwind flux a u_upwind, so they share the upwind cotangents
+    if (kind == FLUX_LLF || kind == FLUX_LLF_NAIVE || kind == FLUX_HLL) {
       ul_bar[0] = 0.5 * (a + fabs(a)) * g[0];
       ur_bar[0] = 0.5 * (a - fabs(a)) * g[0];
     } else {

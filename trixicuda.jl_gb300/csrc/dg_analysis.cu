@@ -12,6 +12,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 #include "../../include/trixi_b200.h"
 #include "basis.h"
@@ -539,8 +540,9 @@ cudaError_t launch_error_norms_all(const ErrorNormHost &h, cudaStream_t s) {
 }  // namespace trixi
 
 // ===========================================================================
-// trixi_integrate_noalloc: the quadrature integrals of trixi_integrate for
-// callers that cannot allocate device memory -- for example an application
+// trixi_integrate_noalloc: the quadrature integrals of trixi_integrate (linear
+// advection and compressible Euler; ideal GLM-MHD only through
+// trixi_integrate) for callers that cannot allocate device memory -- for example an application
 // whose device memory is owned entirely by another allocator (a Julia
 // CUDA.jl or PyTorch caching pool that has reserved the GPU), or a
 // time-critical loop that must not pay for the device-wide synchronisation
@@ -584,6 +586,19 @@ int noalloc_scratch(double **out) {
   return TRIXI_OK;
 }
 
+// LGL quadrature weights per polydeg, computed once per process:
+// lgl_weights_fixed runs a long-double Newton iteration per node, which a
+// per-call entry point meant for time-critical loops should not repeat
+const double *noalloc_weights(int polydeg) {
+  constexpr int kMaxDeg = 15;
+  static std::once_flag once[kMaxDeg + 1];
+  static double table[kMaxDeg + 1][16];
+  static bool ok[kMaxDeg + 1];
+  if (polydeg < 1 || polydeg > kMaxDeg) return nullptr;
+  std::call_once(once[polydeg], [polydeg] { ok[polydeg] = trixi::lgl_weights_fixed(polydeg, table[polydeg]); });
+  return ok[polydeg] ? table[polydeg] : nullptr;
+}
+
 }  // namespace
 extern "C" int trixi_integrate_noalloc(int ndims, int polydeg, int equation, double gamma, const double *u,
                                        const double *du, const double *inverse_jacobian, int64_t nelements,
@@ -612,7 +627,9 @@ extern "C" int trixi_integrate_noalloc(int ndims, int polydeg, int equation, dou
   if (noalloc_scratch(&partials) != TRIXI_OK)
     return reject(TRIXI_ERR_CUDA, "integrate_noalloc: cudaGetSymbolAddress of the scratch array failed");
   WeightsArg wa{};
-  if (!lgl_weights_fixed(polydeg, wa.w)) return reject(TRIXI_ERR_INVALID_ARGUMENT, "integrate_noalloc: weights");
+  const double *w = noalloc_weights(polydeg);
+  if (!w) return reject(TRIXI_ERR_INVALID_ARGUMENT, "integrate_noalloc: weights");
+  for (int j = 0; j <= polydeg; ++j) wa.w[j] = w[j];
   cudaStream_t s = (cudaStream_t)stream;
   const int per_block = 8;
   const unsigned grid = (unsigned)((nelements + per_block - 1) / per_block);

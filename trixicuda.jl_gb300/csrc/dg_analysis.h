@@ -10,6 +10,8 @@ namespace trixi {
 constexpr int IC_CONSTANT = 0;          // TRIXI_IC_CONSTANT
 constexpr int IC_CONVERGENCE_TEST = 1;  // TRIXI_IC_CONVERGENCE_TEST
 constexpr int IC_WEAK_BLAST_WAVE = 2;   // TRIXI_IC_WEAK_BLAST_WAVE
+constexpr int IC_EOC_EULER_GRAVITY = 3; // TRIXI_IC_EOC_TEST_COUPLED_EULER_GRAVITY
+constexpr int IC_LAST = IC_EOC_EULER_GRAVITY;
 
 struct IcParams {
   double p[9];       // kind-specific parameters (a constant state: nvars values)

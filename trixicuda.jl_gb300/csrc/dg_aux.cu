@@ -490,7 +490,7 @@ __global__ void boundary_flux_kernel(int N, int64_t B, const double *__restrict_
 // calc_sources!: du += source(x, t) at every node (after the Jacobian)
 template <int DIM, int EQ>
 __global__ void sources_kernel(int N, int64_t E, const double *__restrict__ coords, double t, double c, double A,
-                               double L, double gamma, double *__restrict__ du) {
+                               double L, double gamma, double *__restrict__ du, int kind) {
   constexpr int NV = NVarsOf<DIM, EQ>::value;
   int NN = 1;
   for (int d = 0; d < DIM; ++d) NN *= N;
@@ -498,7 +498,7 @@ __global__ void sources_kernel(int N, int64_t E, const double *__restrict__ coor
   if (q >= E * NN) return;
   const double prm[3] = {c, A, L};
   double s[NV];
-  source_convergence<DIM, EQ>(prm, gamma, coords + q * DIM, t, s);
+  source_convergence<DIM, EQ>(prm, gamma, coords + q * DIM, t, s, kind);
 #pragma unroll
   for (int v = 0; v < NV; ++v) du[q * NV + v] += s[v];
 }
@@ -785,22 +785,22 @@ cudaError_t stage_boundary_flux(const StageHost &sh, double t, cudaStream_t s) {
 }
 
 cudaError_t stage_sources(const StageHost &sh, double *du, double t, cudaStream_t s) {
-  if (sh.src_kind != SRC_CONVERGENCE_TEST || sh.eq != EQ_EULER) return cudaSuccess;
+  if (sh.src_kind == SRC_NONE || sh.eq != EQ_EULER) return cudaSuccess;
   int NN = 1;
   for (int d = 0; d < sh.dim; ++d) NN *= sh.N;
   const int64_t n = sh.nelements * NN;
   switch (sh.dim) {
     case 1:
       sources_kernel<1, EQ_EULER><<<blocks_for(n, 256), 256, 0, s>>>(sh.N, sh.nelements, sh.coords, t, sh.src[0],
-                                                                     sh.src[1], sh.src[2], sh.gamma, du);
+                                                                     sh.src[1], sh.src[2], sh.gamma, du, sh.src_kind);
       break;
     case 2:
       sources_kernel<2, EQ_EULER><<<blocks_for(n, 256), 256, 0, s>>>(sh.N, sh.nelements, sh.coords, t, sh.src[0],
-                                                                     sh.src[1], sh.src[2], sh.gamma, du);
+                                                                     sh.src[1], sh.src[2], sh.gamma, du, sh.src_kind);
       break;
     default:
       sources_kernel<3, EQ_EULER><<<blocks_for(n, 256), 256, 0, s>>>(sh.N, sh.nelements, sh.coords, t, sh.src[0],
-                                                                     sh.src[1], sh.src[2], sh.gamma, du);
+                                                                     sh.src[1], sh.src[2], sh.gamma, du, sh.src_kind);
   }
   return cudaGetLastError();
 }

@@ -740,8 +740,9 @@ struct FusedKernel {
 #pragma unroll
       for (int v = 0; v < NV; ++v) src[v] = 0.0;
       if constexpr (BND) {
-        if (p.src_kind == SRC_CONVERGENCE_TEST)
-          source_convergence<DIM, EQ>(p.src, p.bc.gamma, p.coords + ((e0 + el) * NN + node) * DIM, p.t, src);
+        if (p.src_kind != SRC_NONE)
+          source_convergence<DIM, EQ>(p.src, p.bc.gamma, p.coords + ((e0 + el) * NN + node) * DIM, p.t, src,
+                                      p.src_kind);
       }
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
@@ -765,8 +766,9 @@ struct FusedKernel {
 #pragma unroll
       for (int v = 0; v < NV; ++v) src[v] = 0.0;
       if constexpr (BND) {
-        if (p.src_kind == SRC_CONVERGENCE_TEST) {
-          source_convergence<DIM, EQ>(p.src, p.bc.gamma, p.coords + ((e0 + el) * NN + node) * DIM, p.t, src);
+        if (p.src_kind != SRC_NONE) {
+          source_convergence<DIM, EQ>(p.src, p.bc.gamma, p.coords + ((e0 + el) * NN + node) * DIM, p.t, src,
+                                      p.src_kind);
           const double f = (mode == MODE_RK) ? (p.dt_elem ? p.dt_elem[e0 + el] : p.dt) : 1.0;
 #pragma unroll
           for (int v = 0; v < NV; ++v) src[v] *= f;

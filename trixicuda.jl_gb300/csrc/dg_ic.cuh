@@ -9,6 +9,26 @@ namespace trixi {
 
 constexpr int SRC_NONE = 0;              // TRIXI_SOURCE_NONE
 constexpr int SRC_CONVERGENCE_TEST = 1;  // TRIXI_SOURCE_CONVERGENCE_TEST
+constexpr int SRC_EOC_EULER = 2;         // TRIXI_SOURCE_EOC_TEST_EULER
+
+// The manufactured solution of the Euler-gravity convergence test
+// (Schlottke-Lakemper, Winters, Ranocha, Gassner, "A purely hyperbolic
+// discretization of the Poisson equation for self-gravitating flows", JCP 442
+// (2021)): rho = c + A sin(pi (sum_d x_d - t)) with c = 2, A = 0.1, v_d = 1.
+// Its gravitational potential solves lap phi = 4 pi G (rho - c):
+// phi = -4 G A sin(.) / (ndims pi), so grad p = -rho grad phi holds with
+// p = K rho^2, K = 2 G / (ndims pi), G = 1.
+template <int DIM>
+struct EocEulerGravity {
+  static constexpr double c = 2.0, A = 0.1, pi = 3.14159265358979323846;
+  static constexpr double K = 2.0 / (DIM * pi);
+  __device__ __forceinline__ static void phase(const double *x, double t, double &sn, double &cs) {
+    double s = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) s += x[d];
+    sincos(pi * (s - t), &sn, &cs);
+  }
+};
 
 // Ideal GLM-MHD: the convergence tests are the smooth circularly polarised
 // Alfven waves -- 1D and 2D after Derigs et al., JCP 317 (2016) (rho = 1,
@@ -130,6 +150,16 @@ __device__ void eval_ic(int kind, const double *x, double t, const IcParams &ip,
     }
     return;
   }
+  if (kind == IC_EOC_EULER_GRAVITY) {
+    using M = EocEulerGravity<DIM>;
+    double sn, cs;
+    M::phase(x, t, sn, cs);
+    const double rho = M::c + M::A * sn;
+    u[0] = rho;
+    for (int d = 0; d < DIM; ++d) u[1 + d] = rho;
+    u[DIM + 1] = M::K * rho * rho / (ip.gamma - 1.0) + 0.5 * DIM * rho;
+    return;
+  }
   // IC_WEAK_BLAST_WAVE (Euler): inside r <= 0.5 rho 1.1691, radial v 0.1882, p 1.245
   double r2 = 0.0;
   for (int d = 0; d < DIM; ++d) r2 += x[d] * x[d];
@@ -170,9 +200,30 @@ __device__ void eval_ic(int kind, const double *x, double t, const IcParams &ip,
 //   2D: (rho_x, rho_x (2 g rho - g - 2 rho + 2) [x2], 2 rho_x (2 g rho - g - rho + 1))
 //   3D: (2 rho_x, rho_x (4 g rho - 3 g - 4 rho + 7)/2 [x3], rho_x (12 g rho - 9 g - 4 rho + 9)/2)
 // prm = (c, A, L).  Linear advection has none (its convergence test is exact).
+// kind SRC_EOC_EULER: S = du/dt + div F(u) for the Euler-gravity manufactured
+// solution above (derived symbolically; rx = pi A cos(pi (sum_d x_d - t)),
+// K = 2/(ndims pi), g = gamma): the gravity terms -rho grad phi, -rho v.grad phi
+// that the Euler equations lack, plus the mass and momentum left over in 2D/3D:
+//   mass      (ndims - 1) rx
+//   momentum  rx ((ndims - 1) + 2 K rho)                     [each component]
+//   energy    rx ((ndims - 1)(2 K rho/(g - 1) + ndims/2) + 2 ndims K rho)
 template <int DIM, int EQ>
 __device__ __forceinline__ void source_convergence(const double *prm, double g, const double *x, double t,
-                                                   double *s) {
+                                                   double *s, int kind = SRC_CONVERGENCE_TEST) {
+  if constexpr (EQ == EQ_EULER) {
+    if (kind == SRC_EOC_EULER) {
+      using M = EocEulerGravity<DIM>;
+      double sn, cs;
+      M::phase(x, t, sn, cs);
+      const double rho = M::c + M::A * sn, rx = M::pi * M::A * cs;
+      const double kr2 = 2.0 * M::K * rho;
+      s[0] = (DIM - 1) * rx;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) s[1 + d] = rx * ((DIM - 1) + kr2);
+      s[DIM + 1] = rx * ((DIM - 1) * (kr2 / (g - 1.0) + 0.5 * DIM) + DIM * kr2);
+      return;
+    }
+  }
   if constexpr (EQ == EQ_EULER) {
     const double omega = 2.0 * 3.14159265358979323846 / prm[2];
     double sx = 0.0;

@@ -1,4 +1,6 @@
-// dg_probe.cu -- CUDA-core FMA throughput probe (FP64 / FP32).
+// dg_probe.cu -- measurement diagnostics of libtrixi_diag.so (not part of
+// libtrixi_b200.so): the CUDA-core FMA throughput probe (FP64 / FP32) and the
+// elementwise integer-pipe conversions of the mixed-precision kernels.
 //
 // The roofline of the FP64 flux-differencing kernels is the FP64 pipe, whose
 // peak on GB300 is not published with the HBM and tensor peaks; this kernel
@@ -8,8 +10,8 @@
 
 #include <cstdint>
 
-#include "../../include/trixi_b200.h"
-#include "dg_convert.cuh"
+#include "trixi_diag.h"
+#include "../dg_convert.cuh"
 
 namespace {
 
@@ -35,7 +37,7 @@ int run(int iters, double *flops_per_s, cudaStream_t s) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int block = 256, grid = sms * 8;
   R *out = nullptr;
-  if (cudaMalloc(&out, sizeof(R) * (size_t)grid * block) != cudaSuccess) return TRIXI_ERR_OUT_OF_MEMORY;
+  if (cudaMalloc(&out, sizeof(R) * (size_t)grid * block) != cudaSuccess) return TRIXI_DIAG_ERR_OUT_OF_MEMORY;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -49,17 +51,17 @@ int run(int iters, double *flops_per_s, cudaStream_t s) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(out);
-  if (err != cudaSuccess || ms <= 0.f) return TRIXI_ERR_CUDA;
+  if (err != cudaSuccess || ms <= 0.f) return TRIXI_DIAG_ERR_CUDA;
   const double fmas = (double)grid * block * (double)iters * 16.0 * 8.0;
   *flops_per_s = 2.0 * fmas / (ms * 1e-3);
-  return TRIXI_OK;
+  return TRIXI_DIAG_OK;
 }
 
 }  // namespace
 
-extern "C" int trixi_probe_fma_peak(int precision, int iters, double *flops_per_s, void *stream) {
-  if (!flops_per_s || iters <= 0) return TRIXI_ERR_INVALID_ARGUMENT;
-  if (precision == TRIXI_PRECISION_FP64) return run<double>(iters, flops_per_s, (cudaStream_t)stream);
+extern "C" int trixi_diag_fma_peak(int precision, int iters, double *flops_per_s, void *stream) {
+  if (!flops_per_s || iters <= 0) return TRIXI_DIAG_ERR_INVALID_ARGUMENT;
+  if (precision == TRIXI_DIAG_FP64) return run<double>(iters, flops_per_s, (cudaStream_t)stream);
   return run<float>(iters, flops_per_s, (cudaStream_t)stream);
 }
 
@@ -72,10 +74,10 @@ __global__ void convert_kernel(const double *in_d, float *out_f, const float *in
 }
 }  // namespace
 
-extern "C" int trixi_probe_convert(const double *in_d, float *out_f, const float *in_f, double *out_d, int64_t n,
+extern "C" int trixi_diag_convert(const double *in_d, float *out_f, const float *in_f, double *out_d, int64_t n,
                                    void *stream) {
-  if (n < 0 || (n > 0 && (!in_d || !out_f || !in_f || !out_d))) return TRIXI_ERR_INVALID_ARGUMENT;
-  if (n == 0) return TRIXI_OK;
+  if (n < 0 || (n > 0 && (!in_d || !out_f || !in_f || !out_d))) return TRIXI_DIAG_ERR_INVALID_ARGUMENT;
+  if (n == 0) return TRIXI_DIAG_OK;
   convert_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(in_d, out_f, in_f, out_d, n);
-  return cudaGetLastError() == cudaSuccess ? TRIXI_OK : TRIXI_ERR_CUDA;
+  return cudaGetLastError() == cudaSuccess ? TRIXI_DIAG_OK : TRIXI_DIAG_ERR_CUDA;
 }

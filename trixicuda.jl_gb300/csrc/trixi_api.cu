@@ -279,17 +279,22 @@ int trixi_create(const trixi_problem_desc *d, trixi_handle **out) {
   if (d->nboundaries < 0 || (d->nboundaries > 0 && (!d->boundary_neighbor_ids || !d->boundary_neighbor_sides ||
                                                     !d->boundary_orientations)))
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "boundary tables");
-  if (d->nboundaries > 0 && (d->boundary_function < TRIXI_IC_CONSTANT || d->boundary_function > TRIXI_IC_WEAK_BLAST_WAVE))
+  if (d->nboundaries > 0 && (d->boundary_function < TRIXI_IC_CONSTANT ||
+                             d->boundary_function > TRIXI_IC_EOC_TEST_COUPLED_EULER_GRAVITY))
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "boundary_function %d", d->boundary_function);
   if (d->nboundaries > 0 && d->boundary_function == TRIXI_IC_WEAK_BLAST_WAVE && d->equation == TRIXI_EQ_LINEAR_ADVECTION)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "the weak blast wave needs the Euler or MHD equations");
+  if (d->nboundaries > 0 && d->boundary_function == TRIXI_IC_EOC_TEST_COUPLED_EULER_GRAVITY &&
+      d->equation != TRIXI_EQ_COMPRESSIBLE_EULER)
+    return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "the Euler-gravity convergence test needs the Euler equations");
   if (d->nboundary_params < 0 || d->nboundary_params > 8 || d->nsource_params < 0 || d->nsource_params > 3)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "nboundary_params %d / nsource_params %d", d->nboundary_params,
                 d->nsource_params);
-  if (d->source_terms != TRIXI_SOURCE_NONE && d->source_terms != TRIXI_SOURCE_CONVERGENCE_TEST)
+  if (d->source_terms != TRIXI_SOURCE_NONE && d->source_terms != TRIXI_SOURCE_CONVERGENCE_TEST &&
+      d->source_terms != TRIXI_SOURCE_EOC_TEST_EULER)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "source_terms %d", d->source_terms);
-  if (d->source_terms == TRIXI_SOURCE_CONVERGENCE_TEST && d->equation != TRIXI_EQ_COMPRESSIBLE_EULER)
-    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "source_terms_convergence_test is defined for the Euler equations");
+  if (d->source_terms != TRIXI_SOURCE_NONE && d->equation != TRIXI_EQ_COMPRESSIBLE_EULER)
+    return fail(nullptr, TRIXI_ERR_UNSUPPORTED, "source terms %d are defined for the Euler equations", d->source_terms);
   if ((d->nboundaries > 0 || d->source_terms != TRIXI_SOURCE_NONE) && !d->node_coordinates)
     return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "boundaries and source terms need node_coordinates");
   if (d->nmortars < 0 || (d->nmortars > 0 && (!d->mortar_neighbor_ids || !d->mortar_large_sides || !d->mortar_orientations)))
@@ -1018,9 +1023,11 @@ IcParams ic_params(const trixi_handle *h, int kind, const double *params, int64_
 }
 
 int check_ic(trixi_handle *h, int kind, int64_t nparams, const double *params) {
-  if (kind < IC_CONSTANT || kind > IC_WEAK_BLAST_WAVE) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "ic kind %d", kind);
+  if (kind < IC_CONSTANT || kind > IC_LAST) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "ic kind %d", kind);
   if (kind == IC_WEAK_BLAST_WAVE && h->eq == EQ_ADV)
     return fail(h, TRIXI_ERR_UNSUPPORTED, "weak blast wave needs the Euler or MHD equations");
+  if (kind == IC_EOC_EULER_GRAVITY && h->eq != EQ_EULER)
+    return fail(h, TRIXI_ERR_UNSUPPORTED, "the Euler-gravity convergence test needs the Euler equations");
   if (kind == IC_CONSTANT && (!params || nparams < h->nv))
     return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "constant state needs %d params", h->nv);
   if (nparams < 0 || nparams > 9) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "nparams %lld", (long long)nparams);

@@ -30,12 +30,14 @@ from .equations import (
     flux_shima_etal,
     initial_condition_constant,
     initial_condition_convergence_test,
+    initial_condition_eoc_test_coupled_euler_gravity,
     initial_condition_fourier_advection,
     initial_condition_fourier_euler,
     initial_condition_weak_blast_wave,
     BoundaryConditionDirichlet,
     boundary_condition_periodic,
     source_terms_convergence_test,
+    source_terms_eoc_test_euler,
 )
 from .mesh import TreeMesh
 from .semidiscretization import (

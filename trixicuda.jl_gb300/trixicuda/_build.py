@@ -2,8 +2,10 @@
 
 Every translation unit under ``csrc/`` is compiled in parallel to
 ``_build/obj`` and linked into ``_build/libtrixi_b200.so``; an object is
-rebuilt when its source or any header is newer.  Nothing is installed into
-site-packages.
+rebuilt when its source or any header is newer.  The measurement
+diagnostics under ``csrc/diag/`` (FMA-peak probe, conversion check) are
+linked into a separate ``_build/libtrixi_diag.so`` that only the benchmark
+and the tests load.  Nothing is installed into site-packages.
 """
 from __future__ import annotations
 
@@ -18,11 +20,16 @@ CSRC = PKG_ROOT / "csrc"
 INCLUDE = PKG_ROOT.parent / "include"
 BUILD = PKG_ROOT / "_build"
 LIB_NAME = "libtrixi_b200.so"
+DIAG_NAME = "libtrixi_diag.so"
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 def library_path() -> Path:
     return BUILD / LIB_NAME
+
+
+def diag_library_path() -> Path:
+    return BUILD / DIAG_NAME
 
 
 def _nvcc() -> str:
@@ -33,7 +40,8 @@ def _nvcc() -> str:
 
 
 def _newest_header() -> float:
-    hdrs = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
+    hdrs = (list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h")) +
+            list((CSRC / "diag").glob("*.h")))
     return max((h.stat().st_mtime for h in hdrs), default=0.0)
 
 
@@ -46,7 +54,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     common = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", f"-I{CSRC}"]
 
     def compile_one(src: Path) -> Path:
-        obj = obj_dir / (src.stem + ".o")
+        obj = obj_dir / (("diag_" if src.parent.name == "diag" else "") + src.stem + ".o")
         if obj.exists() and obj.stat().st_mtime >= max(src.stat().st_mtime, hdr_time):
             return obj
         cmd = [nvcc, *common, *ARCH_FLAGS, "-c", str(src), "-o", str(obj)]
@@ -59,18 +67,26 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
             print(res.stdout, res.stderr)
         return obj
 
-    workers = jobs or max(1, min(len(sources), os.cpu_count() or 4))
+    diag_sources = sorted((CSRC / "diag").glob("*.cu"))
+    workers = jobs or max(1, min(len(sources) + len(diag_sources), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
-        objs = list(ex.map(compile_one, sources))
-    lib = library_path()
-    if not lib.exists() or lib.stat().st_mtime < max(o.stat().st_mtime for o in objs):
-        tmp = lib.with_suffix(".so.tmp")
-        cmd = [nvcc, "-shared", *ARCH_FLAGS, "-o", str(tmp), *map(str, objs)]
+        objs_all = list(ex.map(compile_one, sources + diag_sources))
+    objs, diag_objs = objs_all[:len(sources)], objs_all[len(sources):]
+
+    def link(path: Path, name: str, parts) -> None:
+        if path.exists() and path.stat().st_mtime >= max(o.stat().st_mtime for o in parts):
+            return
+        tmp = path.with_suffix(".so.tmp")
+        cmd = [nvcc, "-shared", *ARCH_FLAGS, "-o", str(tmp), *map(str, parts)]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
-            raise RuntimeError(f"linking {LIB_NAME} failed:\n{res.stdout}\n{res.stderr}")
-        os.replace(tmp, lib)
-    return lib
+            raise RuntimeError(f"linking {name} failed:\n{res.stdout}\n{res.stderr}")
+        os.replace(tmp, path)
+
+    link(library_path(), LIB_NAME, objs)
+    if diag_objs:
+        link(diag_library_path(), DIAG_NAME, diag_objs)
+    return library_path()
 
 
 if __name__ == "__main__":

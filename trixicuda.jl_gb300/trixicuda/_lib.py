@@ -1,7 +1,7 @@
 """ctypes binding of libtrixi_b200.so (the C ABI declared in include/trixi_b200.h).
 
 This is the Python counterpart of the `ccall` glue a Julia maintainer adds to
-TrixiCUDA.jl.  The library is loaded from the in-tree
+TrixiCUDA.jl (julia/TrixiGB300.jl).  The library is loaded from the in-tree
 build folder; if it is missing the import fails loudly -- there is no CPU or
 PyTorch fallback for any compute entry point.
 """
@@ -32,8 +32,8 @@ FLUX_SHIMA_ETAL, FLUX_HLL, FLUX_HLLE = 5, 6, 7
 NONCONSERVATIVE_NONE, NONCONSERVATIVE_POWELL = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
-IC_CONSTANT, IC_CONVERGENCE_TEST, IC_WEAK_BLAST_WAVE = 0, 1, 2
-SOURCE_NONE, SOURCE_CONVERGENCE_TEST = 0, 1
+IC_CONSTANT, IC_CONVERGENCE_TEST, IC_WEAK_BLAST_WAVE, IC_EOC_TEST_COUPLED_EULER_GRAVITY = 0, 1, 2, 3
+SOURCE_NONE, SOURCE_CONVERGENCE_TEST, SOURCE_EOC_TEST_EULER = 0, 1, 2
 INTEGRAL_STATE, INTEGRAL_ENTROPY, INTEGRAL_ENTROPY_PRODUCTION, INTEGRAL_DU = 0, 1, 2, 3
 
 CONTAINER_INTERFACES_U = 0
@@ -135,7 +135,6 @@ SIGNATURES = {
     "trixi_basis": (C.c_int, [_VP, _I, C.POINTER(C.c_double), _I64]),
     "trixi_lgl_basis": (C.c_int, [_I, _I, C.POINTER(C.c_double), _I64]),
     "trixi_synchronize": (C.c_int, [_VP, _VP]),
-    "trixi_probe_fma_peak": (C.c_int, [_I, _I, C.POINTER(C.c_double), _VP]),
     "trixi_compute_coefficients": (C.c_int, [_VP, _I, C.POINTER(C.c_double), _I64, _D, _DP, _VP]),
     "trixi_max_dt": (C.c_int, [_VP, _DP, _DP, _VP]),
     "trixi_rhs_vjp": (C.c_int, [_VP, _DP, _DP, _DP, _VP]),
@@ -160,7 +159,6 @@ SIGNATURES = {
     "trixi_integrate_noalloc": (C.c_int, [_I, _I, _I, C.c_double, _VP, _VP, _VP, _I64, _I, _VP, _VP]),
     "trixi_calc_error_norms": (C.c_int, [_VP, _DP, _DP, _I, C.POINTER(C.c_double), _I64, _D,
                                          C.POINTER(C.c_double), C.POINTER(C.c_double), _VP]),
-    "trixi_probe_convert": (C.c_int, [_VP, _VP, _VP, _VP, _I64, _VP]),
     "trixi_set_glm_speed": (C.c_int, [_VP, _D]),
 }
 
@@ -190,6 +188,28 @@ def load(build_if_missing: bool = False):
         fn.restype = res
         fn.argtypes = args
     _lib = lib
+    return lib
+
+
+_diag = None
+
+
+def load_diag():
+    """Loads libtrixi_diag.so, the measurement diagnostics (FMA-peak probe,
+    conversion check) that the benchmark and the tests use; not part of the
+    rhs library."""
+    global _diag
+    if _diag is not None:
+        return _diag
+    path = _build.diag_library_path()
+    if not path.exists():
+        raise ImportError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(path))
+    lib.trixi_diag_fma_peak.restype = C.c_int
+    lib.trixi_diag_fma_peak.argtypes = [_I, _I, C.POINTER(C.c_double), _VP]
+    lib.trixi_diag_convert.restype = C.c_int
+    lib.trixi_diag_convert.argtypes = [_VP, _VP, _VP, _VP, _I64, _VP]
+    _diag = lib
     return lib
 
 

@@ -400,11 +400,53 @@ def source_terms_convergence_test(u, x, t, equations):
     return s
 
 
+def initial_condition_eoc_test_coupled_euler_gravity(x, t, equations):
+    """The manufactured solution of the Euler-gravity convergence test
+    (Schlottke-Lakemper, Winters, Ranocha, Gassner, JCP 442 (2021)):
+    rho = 2 + 0.1 sin(pi (sum_d x_d - t)), v_d = 1 and the pressure of
+    hydrostatic balance with the potential of rho (lap phi = 4 pi G rho,
+    grad p = -rho grad phi), p = 2 G rho^2 / (ndims pi) with G = 1.  The
+    reference's euler_convergence.jl (3D) runs it with gamma = 2.  x: (ndims, n)."""
+    if not isinstance(equations, _CompressibleEuler):
+        raise ValueError("the Euler-gravity convergence test needs the Euler equations")
+    x = np.atleast_2d(x)
+    d = equations.ndims
+    rho = 2.0 + 0.1 * np.sin(np.pi * (np.sum(x, axis=0) - t))
+    p = 2.0 * rho * rho / (d * np.pi)
+    u = np.empty((d + 2,) + rho.shape)
+    u[0] = rho
+    u[1:1 + d] = rho
+    u[-1] = p / (equations.gamma - 1) + 0.5 * rho * d
+    return u
+
+
+def source_terms_eoc_test_euler(u, x, t, equations):
+    """Source that makes initial_condition_eoc_test_coupled_euler_gravity an
+    exact solution of the Euler equations without gravity (host version; the
+    library evaluates it on the device): with rx = 0.1 pi cos(pi (sum x - t))
+    and K = 2/(ndims pi), mass (ndims-1) rx, momentum rx (ndims-1 + 2 K rho)
+    per component, energy rx ((ndims-1)(2 K rho/(gamma-1) + ndims/2)
+    + 2 ndims K rho).  x: (ndims, n)."""
+    x = np.atleast_2d(x)
+    d = equations.ndims
+    g = equations.gamma
+    arg = np.pi * (np.sum(x, axis=0) - t)
+    rho = 2.0 + 0.1 * np.sin(arg)
+    rx = 0.1 * np.pi * np.cos(arg)
+    kr2 = 2.0 * (2.0 / (d * np.pi)) * rho
+    s = np.empty((d + 2,) + rho.shape)
+    s[0] = (d - 1) * rx
+    s[1:1 + d] = rx * ((d - 1) + kr2)
+    s[-1] = rx * ((d - 1) * (kr2 / (g - 1) + 0.5 * d) + d * kr2)
+    return s
+
+
 def boundary_function_code(func):
     """trixi_initial_condition_kind of a built-in boundary value function."""
     codes = {initial_condition_constant: _lib.IC_CONSTANT,
              initial_condition_convergence_test: _lib.IC_CONVERGENCE_TEST,
-             initial_condition_weak_blast_wave: _lib.IC_WEAK_BLAST_WAVE}
+             initial_condition_weak_blast_wave: _lib.IC_WEAK_BLAST_WAVE,
+             initial_condition_eoc_test_coupled_euler_gravity: _lib.IC_EOC_TEST_COUPLED_EULER_GRAVITY}
     if func not in codes:
         raise NotImplementedError("Dirichlet boundary values: the built-in initial conditions only")
     return codes[func]

@@ -91,6 +91,7 @@ class TreeMesh:
         self.coordinates_min = cmin
         self.coordinates_max = cmax
         self.initial_refinement_level = int(initial_refinement_level)
+        self.refinement_patches = [dict(p) for p in refinement_patches]
         # the tree: set of all cells and set of leaves, keyed (level, coords)
         root = (0, (0,) * self.ndims)
         self.cells = {root}

@@ -172,14 +172,17 @@ def build_problem_desc(mesh_or_containers, equations: AbstractEquations, solver:
     d.nboundary_params = 0 if params is None else len(params)
     for i in range(d.nboundary_params):
         d.boundary_params[i] = float(params[i])
-    from .equations import source_terms_convergence_test
+    from .equations import source_terms_convergence_test, source_terms_eoc_test_euler
 
     if source_terms is None:
         d.source_terms = _lib.SOURCE_NONE
     elif source_terms is source_terms_convergence_test:
         d.source_terms = _lib.SOURCE_CONVERGENCE_TEST
+    elif source_terms is source_terms_eoc_test_euler:
+        d.source_terms = _lib.SOURCE_EOC_TEST_EULER
     else:
-        raise NotImplementedError("source terms: source_terms_convergence_test only")
+        raise NotImplementedError("source terms: source_terms_convergence_test or source_terms_eoc_test_euler; "
+                                  "other Julia source callables cannot cross the C ABI")
     d.nsource_params = 0
     return d, keep, cont
 
@@ -434,7 +437,8 @@ def tile(semi):
 
 # -- analysis, time step and initial conditions on the GPU (reference callbacks) ----
 _IC_KINDS = {"constant": _lib.IC_CONSTANT, "convergence_test": _lib.IC_CONVERGENCE_TEST,
-             "weak_blast_wave": _lib.IC_WEAK_BLAST_WAVE}
+             "weak_blast_wave": _lib.IC_WEAK_BLAST_WAVE,
+             "eoc_test_coupled_euler_gravity": _lib.IC_EOC_TEST_COUPLED_EULER_GRAVITY}
 
 
 def _ic_args(kind, params):
