@@ -31,6 +31,19 @@ const FLUX_HINDENLANG_GASSNER = Int32(4)
 const FLUX_SHIMA_ETAL = Int32(5)
 const FLUX_HLL = Int32(6)
 const FLUX_HLLE = Int32(7)
+const SOURCE_NONE = Int32(0)
+const SOURCE_CONVERGENCE_TEST = Int32(1)
+const SOURCE_EOC_TEST_EULER = Int32(2)
+
+# Source terms cross the C ABI as enums: the library has device code for
+# these two Trixi functions only; any other Julia callable is refused.
+function source_code(source_terms)
+    source_terms === nothing && return SOURCE_NONE
+    source_terms === Trixi.source_terms_convergence_test && return SOURCE_CONVERGENCE_TEST
+    source_terms === Trixi.source_terms_eoc_test_euler && return SOURCE_EOC_TEST_EULER
+    error("libtrixi_b200: source terms $(source_terms) have no device code in the library " *
+          "(supported: source_terms_convergence_test, source_terms_eoc_test_euler)")
+end
 const NONCONSERVATIVE_NONE = Int32(0)
 const NONCONSERVATIVE_POWELL = Int32(1)
 
@@ -114,7 +127,13 @@ already creates with Trixi's `init_*` (semidiscretization_hyperbolic.jl:69-72):
 the connectivity containers are passed as host pointers in their Julia layout,
 together with Trixi's own basis matrices (so both sides use identical operators).
 """
-function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
+function create_handle(mesh, equations, solver, cache_cpu; precision = 0, source_terms = nothing)
+    # this glue passes periodic meshes; Dirichlet boundaries go through the
+    # descriptor's boundary fields with a built-in boundary function kind
+    all(Trixi.isperiodic(mesh)) ||
+        error("libtrixi_b200 glue: non-periodic TreeMesh needs the boundaries container and a built-in " *
+              "BoundaryConditionDirichlet function kind in the descriptor")
+    src = source_code(source_terms)
     elements, interfaces, mortars = cache_cpu.elements, cache_cpu.interfaces, cache_cpu.mortars
     basis = solver.basis
     vi = solver.volume_integral
@@ -150,7 +169,7 @@ function create_handle(mesh, equations, solver, cache_cpu; precision = 0)
                        0, Trixi.nmortars(mortars), pointer(mortars.neighbor_ids), pointer(mortars.large_sides),
                        pointer(mortars.orientations), pointer(weights), pointer(dsplit), pointer(dhat),
                        C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, pointer(elements.node_coordinates), 0,
-                       C_NULL, C_NULL, C_NULL, Int32(-1), Int32(0), Int32(0), Int32(0),
+                       C_NULL, C_NULL, C_NULL, Int32(-1), src, Int32(0), Int32(0),
                        ntuple(_ -> 0.0, 8), ntuple(_ -> 0.0, 3), noncons, Int32(0), c_h)
     desc.struct_size = Int32(sizeof(ProblemDesc))
     handle = Ref{Ptr{Cvoid}}(C_NULL)
