@@ -29,6 +29,7 @@
 #pragma once
 #include "dg_convert.cuh"
 #include "dg_ic.cuh"
+#include "dg_packed.cuh"
 #include "dg_physics.cuh"
 
 namespace trixi {
@@ -239,7 +240,17 @@ struct FusedKernel {
   // 10 % faster).  The other systems stage one flux per node and direction
   // (weak form) or per pair (flux differencing).
   static constexpr bool LINEAR = (EQ == EQ_ADV) && (VOL == VOL_WEAK || sizeof(R) == 4);
-  static constexpr int VOL_PER_DIR = LINEAR ? 0 : (VOL == VOL_WEAK) ? NN : NF * NP;
+  // Flux differencing in FP32 ("owner pairs"): the thread that owns node i
+  // evaluates f#(u_i, u_m) for its N-1 line partners in every direction and
+  // sums D_split[i,m] f# straight into its registers -- twice the flux
+  // arithmetic of the symmetric pairs, but no pair decoding, no pair staging
+  // in shared memory and no gather in phase C.  The FP32 kernels are bound by
+  // instruction issue, where the pair bookkeeping cost more than the second
+  // evaluation (measured: integer instructions were 42 % of the 2D Euler
+  // stage kernel's, FP32 arithmetic 20 %).  FP64 keeps the symmetric pairs:
+  // it is bound by GB300's FP64 pipe, where the flux arithmetic is the cost.
+  static constexpr bool OWNER_PAIRS = (VOL != VOL_WEAK) && !LINEAR && sizeof(R) == 4;
+  static constexpr int VOL_PER_DIR = (LINEAR || OWNER_PAIRS) ? 0 : (VOL == VOL_WEAK) ? NN : NF * NP;
   static constexpr int SURF_PER_EL = 2 * DIM * NF;
   static constexpr int FV_PER_DIR = (VOL == VOL_SC) ? NF * (N - 1) : 0;
   static constexpr int ITEMS_PER_EL = DIM * VOL_PER_DIR + SURF_PER_EL + DIM * FV_PER_DIR;
@@ -434,14 +445,90 @@ struct FusedKernel {
     sts_rec<NV>(s.fv(el, O, t, a), f);
   }
 
+  // owner-pair volume term of direction O for node `node` (position ci on
+  // its line): acc += sum_{m != ci} D_split[ci, m] f#_O(u_node, u_m), the
+  // partners visited as m = ci + 1, ..., ci + N - 1 (mod N) so that every
+  // lane of a warp evaluates a flux in every step
+  template <int O>
+  __device__ __forceinline__ static void owner_volume(const FusedParams<R> &p, const Smem &s, int el, int node,
+                                                      int ci, const R *ui, const R *wi, R *acc) {
+    constexpr int stride = (O == 0) ? 1 : (O == 1) ? N : N * N;
+    const int n0 = node - ci * stride;
+    const R *drow = s.dsplit + ci * N;
+#pragma unroll
+    for (int k = 1; k < N; ++k) {
+      int m = ci + k;
+      if (m >= N) m -= N;
+      R um[NV], wm[NV], f[NV];
+      lds_rec<NV>(s.c(el, n0 + m * stride), um);
+      lds_rec<NV>(s.w(el, n0 + m * stride), wm);
+      two_point_flux_t<DIM, EQ, R, O, VFLUX>(ui, wi, um, wm, f, p.pp);
+      const R dm = drow[m];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[v] += dm * f[v];
+    }
+  }
+
+  // Euler flux_ranocha in FP32: the owner's DIM (N-1) partner fluxes, taken
+  // two at a time in the halves of float2 registers (ranocha_x2, packed FP32
+  // instructions); partner J of the flattened list is k = 1 + J % (N-1)
+  // steps along direction J / (N-1).  Measured on the 2D Euler level-7
+  // stage kernel: FP32 instructions -36 %, all instructions -7 % (the pairs
+  // cost register moves), 18.35 -> 17.41 us per launch.  Used in 2D up to
+  // N = 4 only: the 3D and higher-N kernels spill at their register caps with
+  // it and did not gain (3D shock capturing: 210.9 us either way).
+  static constexpr bool PACKED = OWNER_PAIRS && EQ == EQ_EULER && VFLUX == FLUX_RANOCHA && DIM == 2 && N <= 4;
+  template <int J>
+  __device__ __forceinline__ static void partner(const Smem &s, int node, const int *coord, int &nm, R &dm) {
+    constexpr int O = J / (N - 1), k = 1 + J % (N - 1);
+    constexpr int stride = (O == 0) ? 1 : (O == 1) ? N : N * N;
+    const int ci = coord[O];
+    int m = ci + k;
+    if (m >= N) m -= N;
+    nm = node + (m - ci) * stride;
+    dm = s.dsplit[ci * N + m];
+  }
+  template <int J>
+  __device__ __forceinline__ static void owner_volume_packed(const FusedParams<R> &p, const Smem &s, int el, int node,
+                                                             const int *coord, const R *wi, float2 *acc2, R *acc) {
+    constexpr int NPART = DIM * (N - 1);
+    if constexpr (J + 1 < NPART) {
+      int na, nb;
+      R da, db;
+      partner<J>(s, node, coord, na, da);
+      partner<J + 1>(s, node, coord, nb, db);
+      R wa[NV], wb[NV];
+      lds_rec<NV>(s.w(el, na), wa);
+      lds_rec<NV>(s.w(el, nb), wb);
+      float2 f[NV];
+      ranocha_x2<DIM, J / (N - 1), (J + 1) / (N - 1)>(wi, wa, wb, f, p.pp);
+      const float2 dd = pk::mk(da, db);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc2[v] = pk::fma2(dd, f[v], acc2[v]);
+      owner_volume_packed<J + 2>(p, s, el, node, coord, wi, acc2, acc);
+    } else if constexpr (J < NPART) {
+      int nm;
+      R dm;
+      partner<J>(s, node, coord, nm, dm);
+      R ui[NV], um[NV], wm[NV], f[NV];
+      lds_rec<NV>(s.c(el, node), ui);
+      lds_rec<NV>(s.c(el, nm), um);
+      lds_rec<NV>(s.w(el, nm), wm);
+      two_point_flux_t<DIM, EQ, R, J / (N - 1), VFLUX>(ui, wi, um, wm, f, p.pp);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[v] += dm * f[v];
+    }
+  }
+
   __device__ __forceinline__ static void run(const FusedParams<R> &p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // runtime tile: p.wpg warps per group (>= the owners of EPG elements),
-    // p.gpb groups per block (launch_one validates both)
+    // p.gpb groups per block (launch_one validates both); the block is
+    // (32 * wpg, gpb), so threadIdx.y is the group and the threads of a group
+    // are consecutive warps
     const int GTr = 32 * p.wpg;
-    const int gid = threadIdx.x / GTr;  // group within the block
-    const int gt = threadIdx.x - gid * GTr;
-    if (gid >= p.gpb) return;
+    const int gid = threadIdx.y;  // group within the block
+    const int gt = threadIdx.x;
     Smem s;
     s.cons = reinterpret_cast<R *>(smem_raw + gid * GROUP_SMEM);
     s.prim = s.cons + N_CONS;
@@ -585,10 +672,9 @@ struct FusedKernel {
         if constexpr (DIM > 2) if (dir == 2) fv_item<2>(p, s, el, t, a);
       }
     }
-    group_sync(gid, p.wpg, GTr);
 
-    // phase C: the thread that loaded node q finishes it
-    if (!has_node) return;
+    // node coordinates of the owner thread, and the face index of its line
+    // through each face
     const int el = my_el, node = my_node;
     int coord[3] = {0, 0, 0}, tface[3] = {0, 0, 0};
     {
@@ -610,10 +696,37 @@ struct FusedKernel {
     R acc[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) acc[v] = R(0);
+    if constexpr (OWNER_PAIRS) {
+      // the owner-pair volume term needs only the node records, already
+      // visible after phase A's barrier
+      if (has_node) {
+        R ui[NV], wi[NV];
+        lds_rec<NV>(s.c(el, node), ui);
+        lds_rec<NV>(s.w(el, node), wi);
+        if constexpr (PACKED) {
+          float2 acc2[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) acc2[v] = pk::bc(0.0f);
+          owner_volume_packed<0>(p, s, el, node, coord, wi, acc2, acc);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) acc[v] += acc2[v].x + acc2[v].y;
+        } else {
+          owner_volume<0>(p, s, el, node, coord[0], ui, wi, acc);
+          if constexpr (DIM > 1) owner_volume<1>(p, s, el, node, coord[1], ui, wi, acc);
+          if constexpr (DIM > 2) owner_volume<2>(p, s, el, node, coord[2], ui, wi, acc);
+        }
+      }
+    }
+    group_sync(gid, p.wpg, GTr);
+
+    // phase C: the thread that loaded node q finishes it
+    if (!has_node) return;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const int ci = coord[d];
-      if constexpr (LINEAR) {
+      if constexpr (OWNER_PAIRS) {
+        // (the volume term is in acc already)
+      } else if constexpr (LINEAR) {
         // linear advection: sum_m D_hat[i,m] a_d u_m (weak form) or
         // sum_m D_split[i,m] a_d (u_i + u_m)/2 (flux differencing), with a_d
         // taken out of the sum: one multiply per direction (FP64 multiplies

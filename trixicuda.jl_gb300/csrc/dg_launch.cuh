@@ -74,7 +74,7 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   p.wpg = wpg;
   p.gpb = gpb;
   const int epb = gpb * K::EPG;  // elements per block
-  const int block = 32 * wpg * gpb;
+  const dim3 block(32 * wpg, gpb);  // x: threads of a group, y: groups
   const size_t smem = (size_t)gpb * K::GROUP_SMEM;
   // opt in once per instantiation to the large dynamic shared-memory carve-out
   constexpr auto kernel = fused_entry<DIM, N, EQ, R, VOL, VF, BND>();
@@ -89,7 +89,7 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
     p.pdl = 1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3((unsigned)block);
+    cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
