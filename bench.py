@@ -163,10 +163,13 @@ def _tile_report(semi):
 
 
 def time_gpu_path(precision, steps, warmup, device, flush, tile=None, c3=False):
-    """Device-timed CK2N54 steps through trixi_rk_stage (ping-pong buffers).
-    Returns per-step ms (back-to-back launches), per-launch ms of the stage
-    (a second loop with events around every stage: the fused kernel, plus the
-    indicator for shock capturing), the semi, final u."""
+    """Device-timed CK2N54 steps.  Throughput: one trixi_rk_steps call (the
+    public stepping entry point) per step, CUDA events around each step, L2
+    flushed before it; the five stage launches run back to back (programmatic
+    dependent launches).  A second loop calls trixi_rk_stage with events
+    around every stage (the fused kernel, plus the standalone indicator for
+    shock capturing) for the isolated per-launch time.  Returns per-step ms,
+    isolated per-launch ms, the semi, final u, dt."""
     import torch
 
     import trixicuda as T
@@ -195,18 +198,21 @@ def time_gpu_path(precision, steps, warmup, device, flush, tile=None, c3=False):
         T._lib.check(st, h)
         cur = 1 - cur
 
+    u_steps = u0.clone()
     for _ in range(warmup):
         for s in range(5):
             stage(s)
+        T._lib.check(lib.trixi_rk_steps(h, C.c_void_p(u_steps.data_ptr()), C.c_void_p(k.data_ptr()), 0.0, dt, 1,
+                                        sh), h)
     torch.cuda.synchronize()
-    # throughput: whole steps, back-to-back stage launches, events only at the
-    # step boundaries (L2 flushed before every step)
+    # throughput: whole steps through trixi_rk_steps, events only at the step
+    # boundaries (L2 flushed before every step)
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
     for i in range(steps):
         flush.zero_()
         ev[i][0].record(stream)
-        for s in range(5):
-            stage(s)
+        T._lib.check(lib.trixi_rk_steps(h, C.c_void_p(u_steps.data_ptr()), C.c_void_p(k.data_ptr()), 0.0, dt, 1,
+                                        sh), h)
         ev[i][1].record(stream)
     torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -266,6 +272,7 @@ def batched_path(precision, steps, warmup, device, flush, n=512):
         group_tiles.append({"kind": kinds.get(gi, "?"), "tile": f"{wpg}x{gpb}", "elements_per_group": epg,
                             "best_us": round(min(table.values()) * 1e3, 2) if table else None,
                             "worst_us": round(max(table.values()) * 1e3, 2) if table else None})
+    breakdown = batched_group_breakdown(batch, problems, u, kinds)
     return {"instances": n, "groups": batch.ngroups, "dofs": dofs, "values": nvals,
             "state_mb_fp64": nvals * 8 / 1e6, "ms_per_step": mean_ms,
             "dof_updates_per_s": 5 * dofs / (mean_ms * 1e-3),
@@ -273,7 +280,59 @@ def batched_path(precision, steps, warmup, device, flush, n=512):
             "achieved_gbs": step_bytes / (mean_ms * 1e-3) / 1e9, "setup_s": setup_s,
             "graph": "one CUDA graph per step: groups as parallel branches, 5 stage launches each",
             "tuned_branches": branches, "tuner_ms_per_step": {str(b): v for b, v in tune_ms.items()},
-            "group_tiles": group_tiles}
+            "group_tiles": group_tiles, "group_breakdown": breakdown}
+
+
+def batched_group_breakdown(batch, problems, u, kinds, reps=5):
+    """Per group of the batch: its five stage launches of one CK2N54 step
+    timed alone (CUDA events, median of `reps`, on the group's own slice of
+    the state through its merged handle), its algorithmic bytes per step
+    (read u, k and write u, k in every stage; stage 1 reads no k), the
+    achieved GB/s, and its share of the sum of the groups' times.  The step
+    graph runs groups as parallel branches, so the graph's step is shorter
+    than the sum."""
+    import torch
+
+    import trixicuda as T
+    from trixicuda.time_integration import CK2N54_A, CK2N54_B
+
+    lib = T._lib.load()
+    stream = torch.cuda.current_stream()
+    sh = C.c_void_p(stream.cuda_stream)
+    rows = []
+    for g in range(batch.ngroups):
+        idx = [i for i in range(len(problems)) if batch.group_of(i) == g]
+        lo = int(min(batch.value_offsets[i] for i in idx))
+        hi = int(max(batch.value_offsets[i] + batch.nvalues[i] for i in idx))
+        h = C.c_void_p()
+        T._lib.check(lib.trixi_batch_handle(batch._h, g, C.byref(h)))
+        ua = u[lo:hi].clone()
+        ub = torch.empty_like(ua)
+        k = torch.zeros_like(ua)
+        times = []
+        for r in range(reps + 2):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            bufs = (ua, ub)
+            for st in range(5):
+                T._lib.check(lib.trixi_rk_stage(h, C.c_void_p(bufs[(st + 1) % 2].data_ptr()),
+                                                C.c_void_p(bufs[st % 2].data_ptr()), C.c_void_p(k.data_ptr()),
+                                                CK2N54_A[st], CK2N54_B[st], 1e-6, 0.0, sh), h)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if r >= 2:
+                times.append(a.elapsed_time(b))
+        ms = statistics.median(times)
+        nval = hi - lo
+        step_bytes = nval * 8 * (3 + 4 * 4)
+        dofs = sum(batch.containers[i].nelements * (problems[i].solver.polydeg + 1) ** problems[i].mesh.ndims
+                   for i in idx)
+        rows.append({"group": g, "kind": kinds.get(g, "?"), "instances": len(idx), "dofs": dofs, "values": nval,
+                     "ms_per_step_alone": ms, "achieved_gbs": step_bytes / (ms * 1e-3) / 1e9})
+    total = sum(r["ms_per_step_alone"] for r in rows)
+    for r in rows:
+        r["time_share"] = r["ms_per_step_alone"] / total
+    return rows
 
 
 def adjoint_path(device, nsteps=200, snapshots=15, ndirs=16):
@@ -299,8 +358,9 @@ def adjoint_path(device, nsteps=200, snapshots=15, ndirs=16):
         T.rk_steps(u, k, 0.0, dt, nsteps, semi)
         return u
 
-    def timed(fn, reps=2):
-        best = None
+    def timed(fn, reps=5):
+        """Median of `reps` runs (CUDA events), and every run's time."""
+        runs = []
         for _ in range(reps):
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -308,16 +368,16 @@ def adjoint_path(device, nsteps=200, snapshots=15, ndirs=16):
             out = fn()
             b.record()
             torch.cuda.synchronize()
-            ms = a.elapsed_time(b)
-            best = ms if best is None else min(best, ms)
-        return best, out
+            runs.append(a.elapsed_time(b))
+        return statistics.median(runs), out, runs
 
     fwd()  # warm-up
-    f_ms, _ = timed(fwd)
+    f_ms, _, f_runs = timed(fwd)
     res = {}
     for label, s_ in (("binomial", snapshots), ("store_all", nsteps - 1)):
-        g_ms, (J, grad, nrec) = timed(lambda: ADJ.gradient_density_l2(semi, u0, rt, dt, nsteps, s_))
+        g_ms, (J, grad, nrec), g_runs = timed(lambda: ADJ.gradient_density_l2(semi, u0, rt, dt, nsteps, s_))
         res[label] = {"snapshots": s_, "gradient_ms": g_ms, "ratio_to_forward": g_ms / f_ms,
+                      "ratio_runs": [g / f for g, f in zip(g_runs, f_runs)], "statistic": "median of 5 runs",
                       "forward_steps_recomputed": nrec}
     rng = np.random.default_rng(20261203)
     errs = []
@@ -559,7 +619,13 @@ def main():
     bytes_launch = [nval * 8 * (3 if s == 0 else 4) + E * 8 + E * 4 * 4 for s in range(5)]
     mean_bytes = sum(bytes_launch) / 5
     mean_launch_ms = statistics.mean(launch_ms)
-    achieved = mean_bytes / (mean_launch_ms * 1e-3) / 1e9
+    # the stage kernel's average launch duration in the timed region: the
+    # timed steps hold nothing but its 5 launches per step (back to back, each
+    # overlapping its launch with the previous one's tail), so it is the
+    # step time over 5; the isolated time of one launch with events around it
+    # (launch latency and tail included) is reported beside it
+    steady_launch_ms = statistics.mean(step_ms) / 5
+    achieved = mean_bytes / (steady_launch_ms * 1e-3) / 1e9
     value64 = per_step_updates / (statistics.mean(step64) * 1e-3)
     # equal-L2 check: 100 steps of mixed vs FP64 from the same state
     l2 = l2_mixed_vs_fp64(semi, semi64, dt, nsteps=100)
@@ -588,7 +654,10 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
                      "kernel": "dg_fused_kernel (RK stage)", "algorithmic_bytes_per_launch": mean_bytes,
-                     "mean_launch_ms": mean_launch_ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+                     "mean_launch_ms": steady_launch_ms, "isolated_launch_ms": mean_launch_ms,
+                     "frac_isolated": mean_bytes / (mean_launch_ms * 1e-3) / 1e9 / hbm_peak,
+                     "launch_time": "timed steps / 5 (5 back-to-back stage launches per step)",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
         "tiles": {"mixed": _tile_report(semi), "fp64": _tile_report(semi64)},
         "fp64": {"value": value64, "unit": METRIC, "ms_per_step": statistics.mean(step64),
                  "mean_launch_ms": statistics.mean(launch64),
@@ -604,6 +673,10 @@ def main():
         "shock_capturing_3d": c3,
         "advection_1d": c1,
         "cpu_baseline": cpu,
+        "vs_cpu_baseline": None if not cpu else {
+            "fp64_over_fp64_cpu": value64 / cpu["value"], "mixed_over_fp64_cpu": value / cpu["value"],
+            "e2e_mixed_over_fp64_cpu": per_step_updates / (e2e_ms * 1e-3) / cpu["value"],
+            "note": "like for like is the FP64 line; the CPU leg is the oracle (FP64), not Trixi.jl"},
         "gpu_launches": 5 * args.steps,
         "clocks": clocks,
     }
@@ -625,15 +698,17 @@ def c3_path(steps, warmup, device, flush, hbm_peak):
         semis[prec] = (semi, dt)
         dofs, nv, E = semi.ndofs(), semi.equations.nvariables, semi.nelements
         nval = dofs * nv
-        # algorithmic bytes of one stage: the fused kernel reads u, k and writes u_out, k
-        # (stage 1 does not read k), plus J^{-1}, alpha and the face table; the
-        # indicator reads u once more
-        stage_bytes = statistics.mean([nval * 8 * (3 if st == 0 else 4) + E * (8 + 8 + 6 * 4) + nval * 8
-                                       for st in range(5)])
+        # algorithmic bytes of one stage: read u, k and write u_out, k (stage 1
+        # does not read k), plus J^{-1}, alpha and the face table.  A second
+        # read of u by a standalone indicator kernel is implementation traffic
+        # and not counted (the FP32 steps compute the indicator inside the
+        # stage kernel).
+        stage_bytes = statistics.mean([nval * 8 * (3 if st == 0 else 4) + E * (8 + 8 + 6 * 4) for st in range(5)])
         ms = statistics.mean(step_ms)
-        ach = stage_bytes / (statistics.mean(stage_ms) * 1e-3) / 1e9
+        ach = stage_bytes / (ms / 5 * 1e-3) / 1e9
         out[prec] = {"value": 5 * dofs / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms,
-                     "mean_stage_ms": statistics.mean(stage_ms), "algorithmic_bytes_per_stage": stage_bytes,
+                     "stage_ms": ms / 5, "isolated_stage_ms": statistics.mean(stage_ms),
+                     "algorithmic_bytes_per_stage": stage_bytes,
                      "achieved_gbs": ach, "hbm_frac": ach / hbm_peak, "tile": _tile_report(semi)}
     # FP32-mixed against FP64 after 50 steps from the same state
     out["equal_l2"] = l2_mixed_vs_fp64(semis["mixed"][0], semis["fp64"][0], semis["fp64"][1], nsteps=50)
@@ -747,6 +822,9 @@ def _nan_aware_rel_err(got, ref):
             "nonfinite_entries": int(ref.size - int(fin.sum()))}
 
 
+GLM_SPEED_SUITE = 1.0
+
+
 def reference_benchmark_suite(device, calls=200, sync_calls=50):
     """Times rhs_gpu on each set-up of reference_benchmark_problems, as the
     reference's benchmark scripts time `CUDA.@sync rhs_gpu!` against the CPU
@@ -763,6 +841,12 @@ def reference_benchmark_suite(device, calls=200, sync_calls=50):
         row = {"problem": name}
         for precision in ("mixed", "fp64"):
             semi = setup.build(precision)
+            if hasattr(setup.equations, "c_h") and setup.mesh.ndims > 1:
+                # Trixi starts c_h as NaN and GlmSpeedCallback sets a finite
+                # cleaning speed before the first step; the suite does the same
+                # (c_h = 1; its value does not change the cost of the rhs), so
+                # the MHD rows time finite arithmetic
+                T.set_glm_speed(semi, GLM_SPEED_SUITE)
             u_host = semi.compute_coefficients_host()
             u = torch.from_numpy(u_host).to(device)
             du = torch.empty_like(u)
@@ -823,7 +907,10 @@ def l2_mixed_vs_fp64(semi_mixed, semi64, dt, nsteps):
     return {"steps": nsteps, "dt": dt, "l2_diff_per_var": l2.tolist(), "linf_diff_per_var": linf.tolist(),
             "rel_l2_per_var": (l2 / scale).tolist(), "rel_l2_state": rel_state,
             "within_1e-6": bool(rel_state < 1e-6), "criterion": "rel_l2_state < 1e-6",
-            "abs_l2_per_var_within_1e-6": bool(np.all(l2 < 1e-6))}
+            "abs_l2_per_var_within_1e-6": bool(np.all(l2 < 1e-6)),
+            "verdict": ("relative: " + ("pass" if rel_state < 1e-6 else "FAIL") + "; absolute per variable: " +
+                        ("pass" if np.all(l2 < 1e-6) else
+                         "FAIL (" + ", ".join(f"var {i}: {x:.2e}" for i, x in enumerate(l2) if x >= 1e-6) + ")"))}
 
 
 if __name__ == "__main__":

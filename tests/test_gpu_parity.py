@@ -189,3 +189,4 @@ def test_rhs_rejects_bad_pointers(cuda):
     assert st == 1
     st = lib.trixi_rhs(semi.handle, C.c_void_p(u.data_ptr()), C.c_void_p(u.data_ptr()), 0.0, None)
     assert st == 1  # du aliases u
+

@@ -8,6 +8,7 @@
 #include "dg_host.h"
 #include "dg_ic.cuh"
 #include "dg_convert.cuh"
+#include "dg_indicator.cuh"
 #include "dg_physics.cuh"
 
 namespace trixi {
@@ -234,14 +235,6 @@ template <typename R>
 __device__ __forceinline__ R ind_load(const double *p) { return R(*p); }
 template <>
 __device__ __forceinline__ float ind_load<float>(const double *p) { return from_double<float>(*p); }
-__device__ __forceinline__ double ind_div(double a, double b) { return a / b; }
-__device__ __forceinline__ float ind_div(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ double ind_mul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float ind_mul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double ind_add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float ind_add(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ double ind_exp(double x) { return exp(x); }
-__device__ __forceinline__ float ind_exp(float x) { return __expf(x); }
 
 template <int DIM, int N, typename R>
 __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const double *__restrict__ u,
@@ -259,34 +252,14 @@ __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const dou
   const int64_t e = e0 + warp;
   R *a = s_iv + N * N + warp * 2 * NN, *b = a + NN;
   if (e < E) {
-    const R half = R(0.5), gm1 = R(gamma_ - 1.0);
+    const R gm1 = R(gamma_ - 1.0);
     for (int n = lane; n < NN; n += 32) {
       const double *un = u + (e * NN + n) * nv;
-      const R rho = ind_load<R>(un);
-      const R inv = ind_div(R(1), rho);  // one reciprocal, not a division per component
-      R kin = R(0), p;
-      if (mhd) {  // p = (gamma-1)(E - rho|v|^2/2 - |B|^2/2 - psi^2/2)
-        R mag = R(0);
+      R c[9];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const R m = ind_load<R>(un + 1 + d), B = ind_load<R>(un + 5 + d);
-          kin += m * (m * inv);
-          mag += B * B;
-        }
-        if (nv == 9) {
-          const R psi = ind_load<R>(un + 8);
-          mag += psi * psi;
-        }
-        p = gm1 * (ind_load<R>(un + 4) - half * kin - half * mag);
-      } else {
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          const R m = ind_load<R>(un + 1 + d);
-          kin += m * (m * inv);
-        }
-        p = gm1 * (ind_load<R>(un + DIM + 1) - half * kin);
-      }
-      a[n] = variable ? p : rho * p;  // pressure or density_pressure
+      for (int v = 0; v < 9; ++v)
+        if (v < nv) c[v] = ind_load<R>(un + v);
+      a[n] = ind_value<DIM, R>(c, gm1, mhd != 0, nv, variable);
     }
     __syncwarp();
     R *src = a, *dst = b;
@@ -310,33 +283,23 @@ __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const dou
   }
   // the transform alternates between a and b per dimension: after DIM passes
   // the coefficients sit in a when DIM is even, in b when it is odd
+  if constexpr (sizeof(R) == 4) {
+    // FP32: each warp folds its own element
+    if (e < E) {
+      float total, clip1, clip2;
+      ind_energy_sums_warp<DIM, N>((DIM & 1) ? b : a, lane, total, clip1, clip2);
+      if (lane == 0) alpha_raw[e] = ind_alpha<R>(total, clip1, clip2, threshold_, param_s_, amax, amin);
+    }
+    return;
+  }
   __syncthreads();
   if (warp != 0) return;
   const int el = lane / 3, which = lane - 3 * (lane / 3);  // which: 0 all modes, 1 without the highest, 2 without two
   const bool active = lane < 3 * WPB && e0 + el < E;
   R sum = R(0);
-  if (active) {
-    const R *c = s_iv + N * N + el * 2 * NN + ((DIM & 1) ? NN : 0);
-    for (int n = 0; n < NN; ++n) {
-      int maxc = n % N;
-      if (DIM > 1) maxc = max(maxc, (n / N) % N);
-      if (DIM > 2) maxc = max(maxc, n / (N * N));
-      const bool take = (which == 0) || (which == 1 && maxc < N - 1) || (which == 2 && maxc < N - 2);
-      if (take) sum = ind_add(sum, ind_mul(c[n], c[n]));  // no contraction: the oracle's roundings
-    }
-  }
+  if (active) sum = ind_energy_sum<DIM, N, R>(s_iv + N * N + el * 2 * NN + ((DIM & 1) ? NN : 0), which);
   const R clip1 = __shfl_down_sync(0xffffffffu, sum, 1), clip2 = __shfl_down_sync(0xffffffffu, sum, 2);
-  if (active && which == 0) {
-    const R total = sum;
-    const R f1 = (total != R(0)) ? (total - clip1) / total : R(0);
-    const R f2 = (clip1 != R(0)) ? (clip1 - clip2) / clip1 : R(0);
-    const R energy = f1 > f2 ? f1 : f2;
-    const R threshold = R(threshold_);
-    double al = double(R(1) / (R(1) + ind_exp(-R(param_s_) / threshold * (energy - threshold))));
-    if (al < amin) al = 0.0;
-    if (al > 1.0 - amin) al = 1.0;
-    alpha_raw[e0 + el] = fmin(amax, al);
-  }
+  if (active && which == 0) alpha_raw[e0 + el] = ind_alpha<R>(sum, clip1, clip2, threshold_, param_s_, amax, amin);
 }
 
 template <int DIM, int N>
