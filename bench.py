@@ -568,9 +568,6 @@ def main():
     lib = T._lib.load()
     fp64_peak = C.c_double()
     fp32_peak = C.c_double()
-    diag = T._lib.load_diag()
-    T._lib.check(diag.trixi_diag_fma_peak(0, 4096, C.byref(fp64_peak), None))
-    T._lib.check(diag.trixi_diag_fma_peak(1, 16384, C.byref(fp32_peak), None))
 
     if args.suite == "reference-benchmarks":
         rows = reference_benchmark_suite(device)
@@ -593,9 +590,13 @@ def main():
         step_ms, launch_ms, semi, _, _ = time_gpu_path(args.profile.split("-")[-1], args.steps, args.warmup, device,
                                                        flush, tile, c3=c3)
         print(json.dumps({"profile": args.profile, "ms_per_step": statistics.mean(step_ms),
-                          "mean_launch_ms": statistics.mean(launch_ms), "fp64_fma_peak_tflops": fp64_peak.value / 1e12,
-                          "fp32_fma_peak_tflops": fp32_peak.value / 1e12}))
+                          "mean_launch_ms": statistics.mean(launch_ms)}))
         return 0
+    # the CUDA-core FMA peaks (the FP64 kernels' roofline), measured before the
+    # timed loops (the --profile modes skip them)
+    diag = T._lib.load_diag()
+    T._lib.check(diag.trixi_diag_fma_peak(0, 4096, C.byref(fp64_peak), None))
+    T._lib.check(diag.trixi_diag_fma_peak(1, 16384, C.byref(fp32_peak), None))
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:

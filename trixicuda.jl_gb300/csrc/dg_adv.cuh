@@ -1,0 +1,207 @@
+// dg_adv.cuh -- the rhs / RK-stage kernel of linear scalar advection on
+// periodic and mortar meshes (weak form or flux differencing with the
+// central flux; every surface flux of the reference's advection set-ups).
+//
+// The generic fused kernel (dg_fused.cuh) stages neighbour traces, surface
+// flux items and node records per element group with group barriers and a
+// tile that the tuner picks; ncu counted 510 thread instructions per node on
+// its 3D N = 6 weak-form stage kernel, whose arithmetic is ~20 multiply-adds.
+// Here a block holds floor(512 / N^d) whole elements, threads of consecutive
+// elements contiguous, and three phases separated by block barriers:
+//   A. thread = node: load u (and k), store the narrowed value; thread =
+//      face node of the block's element faces (2 d N^(d-1) per element):
+//      load the neighbour's adjacent value (or the mortar kernel's flux);
+//   B. thread = face node: the surface flux from its own node's value and the
+//      neighbour's -- linear in both, a few operations -- to shared memory;
+//   C. thread = node: the volume term over its lines (D_hat for the weak
+//      form: a_d sum_m D_hat[i,m] u_m; D_split for flux differencing:
+//      a_d/2 sum_m D_split[i,m] (u_i + u_m)), the surface terms -/+ lhat f*,
+//      -J^{-1} and du or the 2N RK update, as phase C of the generic kernel.
+// Every phase maps threads to uniform work (no per-node face branches in
+// the loads).  Boundary conditions are not handled here: non-periodic meshes
+// use the generic kernel's boundary-capable instantiations.
+#pragma once
+#include "dg_fused.cuh"
+
+namespace trixi {
+
+template <int DIM, int N, typename R, int VOL>
+struct AdvKernel {
+  static constexpr int NN = ipow(N, DIM);
+  static constexpr int NF = ipow(N, DIM - 1);
+  static constexpr int EPB = (512 / NN) > 0 ? 512 / NN : 1;  // elements per block
+  static constexpr int BLOCK = ((EPB * NN + 31) / 32) * 32;
+
+  // the surface flux kinds of linear advection: central and flux_ranocha
+  // (the arithmetic mean), Lax-Friedrichs (speed |a|) and HLL (lmin = lmax =
+  // a: the upwind value), as the generic kernel's two_point_flux forms them
+  __device__ __forceinline__ static R face_flux(int kind, R a, R ul, R ur) {
+    if (kind == FLUX_HLL || kind == FLUX_HLLE) return a >= R(0) ? a * ul : a * ur;
+    R f = R(0.5) * (a * ul + a * ur);
+    if (kind == FLUX_LLF || kind == FLUX_LLF_NAIVE) f += -R(0.5) * dev_fabs(a) * (ur - ul);
+    return f;
+  }
+
+  // the neighbour's value narrowed on the FP64 pipe (as the generic kernel's
+  // neighbour traces); the owner's own value on the integer pipe in 1D/2D
+  __device__ __forceinline__ static R narrow_hw(double x) { return R(x); }
+
+  static constexpr int FPE = 2 * DIM * NF;                    // face nodes per element
+  static constexpr int ITEMS = EPB * FPE;                      // face nodes per block
+  static constexpr int IPT = (ITEMS + BLOCK - 1) / BLOCK;      // face nodes per thread
+
+  __device__ __forceinline__ static void run(const FusedParams<R> &p) {
+    __shared__ R s_u[EPB * NN];
+    __shared__ R s_f[ITEMS];   // [element][face][face node]
+    __shared__ R s_op[N * N];  // D_hat (weak form) or D_split (flux differencing), row-major
+    const int tid = threadIdx.x;
+    for (int q = tid; q < N * N; q += BLOCK) s_op[q] = (VOL == VOL_WEAK) ? p.dhat[q] : p.dsplit[q];
+    const int64_t e0 = (int64_t)blockIdx.x * EPB;
+    const int el = tid / NN, node = tid - (tid / NN) * NN;
+    const int64_t e = e0 + el;
+    const bool has = el < EPB && e < p.nelements;
+    const int mode = p.mode;
+    const bool surface = mode != MODE_VOLUME;
+    const bool use_k = mode == MODE_RK && p.use_k;
+    if (p.pdl) {
+      asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+      asm volatile("griddepcontrol.wait;" ::: "memory");
+    }
+    // phase A: node values, and the outer values of the block's face nodes
+    double ureg = 0.0, kreg = 0.0;
+    R ui = R(0);
+    if (has) {
+      const int64_t g = e * NN + node;
+      ureg = p.u_in[g];
+      if (use_k) kreg = p.k[g];
+      if constexpr (DIM == 3) ui = narrow_hw(ureg);
+      else ui = from_double<R>(ureg);
+      s_u[el * NN + node] = ui;
+    }
+    R outer[IPT];
+    bool conforming[IPT];
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      outer[i] = R(0);
+      conforming[i] = true;
+      const int j = tid + i * BLOCK;
+      if (!surface || j >= ITEMS) continue;
+      const int fe = j / FPE, r = j - (j / FPE) * FPE;
+      const int face = r / NF, t = r - (r / NF) * NF;
+      if (e0 + fe >= p.nelements) continue;
+      const int32_t nb = p.face_table[(e0 + fe) * (2 * DIM) + face];
+      if (nb >= 0) {
+        const int other = line_node_rt<DIM, N>(face >> 1, t, (face & 1) ? 0 : N - 1);
+        outer[i] = narrow_hw(p.u_in[(int64_t)nb * NN + other]);
+      } else {
+        outer[i] = narrow_hw(p.mortar_flux[(int64_t)(-nb - 1) * NF + t]);
+        conforming[i] = false;
+      }
+    }
+    __syncthreads();
+    // phase B: the surface flux of every face node (the element's own value
+    // on the inner side; a mortar face's flux comes from the mortar kernel)
+    if (surface) {
+      const int kind = p.surface_flux;
+#pragma unroll
+      for (int i = 0; i < IPT; ++i) {
+        const int j = tid + i * BLOCK;
+        if (j >= ITEMS) continue;
+        const int fe = j / FPE, r = j - (j / FPE) * FPE;
+        const int face = r / NF, t = r - (r / NF) * NF;
+        if (e0 + fe >= p.nelements) continue;
+        R f = outer[i];
+        if (conforming[i]) {
+          const int o = face >> 1;
+          const R own = s_u[fe * NN + line_node_rt<DIM, N>(o, t, (face & 1) ? N - 1 : 0)];
+          const R a = p.pp.a[o];
+          f = (face & 1) ? face_flux(kind, a, own, outer[i]) : face_flux(kind, a, outer[i], own);
+        }
+        s_f[j] = f;
+      }
+    }
+    __syncthreads();
+    if (!has) return;
+    // phase C
+    constexpr int strides[3] = {1, N, N * N};
+    int coord[3] = {0, 0, 0}, tface[3] = {0, 0, 0};
+    {
+      int qq = node;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        coord[d] = qq % N;
+        qq /= N;
+      }
+      if constexpr (DIM == 2) {
+        tface[0] = coord[1];
+        tface[1] = coord[0];
+      } else if constexpr (DIM == 3) {
+        tface[0] = coord[1] + N * coord[2];
+        tface[1] = coord[0] + N * coord[2];
+        tface[2] = coord[0] + N * coord[1];
+      }
+    }
+    R acc = R(0);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const int ci = coord[d];
+      const R *row = s_op + ci * N;
+      const R *line = s_u + el * NN + node - ci * strides[d];
+      R sum = R(0);
+      if constexpr (VOL == VOL_WEAK) {
+#pragma unroll
+        for (int m = 0; m < N; ++m) sum += row[m] * line[m * strides[d]];
+        acc += p.pp.a[d] * sum;
+      } else {
+#pragma unroll
+        for (int m = 0; m < N; ++m) {
+          if (m == ci) continue;
+          sum += row[m] * (ui + line[m * strides[d]]);
+        }
+        acc += (R(0.5) * p.pp.a[d]) * sum;
+      }
+    }
+    if (surface) {
+      const R *fel = s_f + el * FPE;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        if (coord[d] == 0) acc -= p.lhat_l * fel[(2 * d) * NF + tface[d]];
+        if (coord[d] == N - 1) acc += p.lhat_r * fel[(2 * d + 1) * NF + tface[d]];
+      }
+    }
+    const int64_t g = e * NN + node;
+    if (mode == MODE_VOLUME) {
+      p.out[g] = to_double(acc);
+      return;
+    }
+    const double dte = p.dt_elem ? p.dt_elem[e] : p.dt;
+    if constexpr (sizeof(R) == sizeof(double)) {
+      const double du = double(acc) * -p.inv_jac[e];
+      if (mode == MODE_RHS) {
+        p.out[g] = du;
+      } else {
+        const double kk = (use_k ? p.rk_a * kreg : 0.0) + dte * du;
+        p.k[g] = kk;
+        p.out[g] = ureg + p.rk_b * kk;
+      }
+    } else {
+      // mixed precision: scale in FP32, widen exactly, accumulate in FP64
+      const R sc = from_double<R>(-p.inv_jac[e] * (mode == MODE_RK ? dte : 1.0));
+      const double dd = to_double(acc * sc);
+      if (mode == MODE_RHS) {
+        p.out[g] = dd;
+      } else {
+        const double kk = use_k ? fma(p.rk_a, kreg, dd) : dd;
+        p.k[g] = kk;
+        p.out[g] = fma(p.rk_b, kk, ureg);
+      }
+    }
+  }
+};
+
+template <int DIM, int N, typename R, int VOL>
+__global__ void __launch_bounds__(AdvKernel<DIM, N, R, VOL>::BLOCK) dg_adv_kernel(const FusedParams<R> p) {
+  AdvKernel<DIM, N, R, VOL>::run(p);
+}
+
+}  // namespace trixi

@@ -4,6 +4,7 @@
 #pragma once
 #include <algorithm>
 
+#include "dg_adv.cuh"
 #include "dg_fused.cuh"
 #include "dg_host.h"
 
@@ -55,6 +56,42 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   for (int i = 0; i < NMAXT; ++i) p.invw[i] = R(i < N ? h.invw[i] : 0.0);
   p.lhat_l = R(h.lhat_l);
   p.lhat_r = R(h.lhat_r);
+  if constexpr (EQ == EQ_ADV && BND == 0) {
+    // linear advection on periodic / mortar meshes: the dedicated one-thread-
+    // per-node kernel (dg_adv.cuh).  Its block shape is fixed; the tile
+    // reported is one element group of the warps that hold an element's nodes
+    // and is the only one accepted, so the tile tuner has a single candidate
+    using A = AdvKernel<DIM, N, R, VOL>;
+    if (h.tile_out) {
+      h.tile_out->epg = 1;
+      h.tile_out->min_wpg = h.tile_out->def_wpg = h.tile_out->max_warps = (A::NN + 31) / 32;
+      h.tile_out->def_gpb = 1;
+      h.tile_out->group_smem = 0;
+      return cudaSuccess;
+    }
+    p.wpg = p.gpb = 1;
+    const int64_t grid = (h.nelements + A::EPB - 1) / A::EPB;
+    if (grid <= 0) return cudaSuccess;
+    if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
+    constexpr auto kernel = &dg_adv_kernel<DIM, N, R, VOL>;
+    if (h.pdl) {
+      p.pdl = 1;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)grid);
+      cfg.blockDim = dim3(A::BLOCK);
+      cfg.dynamicSmemBytes = 0;
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[0].val.programmaticStreamSerializationAllowed = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      return cudaLaunchKernelEx(&cfg, kernel, p);
+    }
+    p.pdl = 0;
+    kernel<<<(unsigned)grid, A::BLOCK, 0, s>>>(p);
+    return cudaGetLastError();
+  }
   if (h.tile_out) {
     h.tile_out->epg = K::EPG;
     h.tile_out->min_wpg = K::warps_for(K::EPG);
