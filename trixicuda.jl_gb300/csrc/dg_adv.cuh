@@ -25,6 +25,52 @@
 
 namespace trixi {
 
+// Index tables of one element shape, built at compile time into device
+// memory (every block reads the same few hundred bytes, which stay in L1):
+// per node its coordinates (4 bits each) and the face index of its line
+// through each face direction (6 bits each); per face node (face f, node t
+// of the face) the element's own node on that face, the neighbour's adjacent
+// node, f and t.  They replace per-thread divisions and branches.
+template <int DIM, int N>
+struct AdvTables {
+  static constexpr int NN = ipow(N, DIM), NF = ipow(N, DIM - 1), FPE = 2 * DIM * NF;
+  uint32_t node[NN];
+  uint32_t face[FPE];
+  static constexpr int lnode(int o, int t, int a) {
+    return DIM == 1 ? a
+           : DIM == 2 ? (o == 0 ? a + t * N : t + a * N)
+                      : (o == 0 ? a + (t % N) * N + (t / N) * N * N
+                                : o == 1 ? (t % N) + a * N + (t / N) * N * N : (t % N) + (t / N) * N + a * N * N);
+  }
+  static constexpr AdvTables make() {
+    AdvTables tb{};
+    for (int q = 0; q < NN; ++q) {
+      int c[3] = {0, 0, 0}, tf[3] = {0, 0, 0}, qq = q;
+      for (int d = 0; d < DIM; ++d) {
+        c[d] = qq % N;
+        qq /= N;
+      }
+      if (DIM == 2) {
+        tf[0] = c[1];
+        tf[1] = c[0];
+      } else if (DIM == 3) {
+        tf[0] = c[1] + N * c[2];
+        tf[1] = c[0] + N * c[2];
+        tf[2] = c[0] + N * c[1];
+      }
+      tb.node[q] = (uint32_t)(c[0] | (c[1] << 4) | (c[2] << 8) | (tf[0] << 12) | (tf[1] << 18) | (tf[2] << 24));
+    }
+    for (int r = 0; r < FPE; ++r) {
+      const int f = r / NF, t = r % NF, o = f / 2;
+      const int own = lnode(o, t, (f & 1) ? N - 1 : 0), other = lnode(o, t, (f & 1) ? 0 : N - 1);
+      tb.face[r] = (uint32_t)(own | (other << 8) | (f << 16) | (t << 19));
+    }
+    return tb;
+  }
+};
+template <int DIM, int N>
+__device__ const AdvTables<DIM, N> g_adv_tables = AdvTables<DIM, N>::make();
+
 template <int DIM, int N, typename R, int VOL>
 struct AdvKernel {
   static constexpr int NN = ipow(N, DIM);
@@ -43,7 +89,7 @@ struct AdvKernel {
   }
 
   // the neighbour's value narrowed on the FP64 pipe (as the generic kernel's
-  // neighbour traces); the owner's own value on the integer pipe in 1D/2D
+  // neighbour traces); the owner's own value on the integer pipe
   __device__ __forceinline__ static R narrow_hw(double x) { return R(x); }
 
   static constexpr int FPE = 2 * DIM * NF;                    // face nodes per element
@@ -54,6 +100,7 @@ struct AdvKernel {
     __shared__ R s_u[EPB * NN];
     __shared__ R s_f[ITEMS];   // [element][face][face node]
     __shared__ R s_op[N * N];  // D_hat (weak form) or D_split (flux differencing), row-major
+    __shared__ R s_scale[EPB];  // FP32 path: -J^{-1} (rhs) or -J^{-1} dt (RK) per element
     const int tid = threadIdx.x;
     for (int q = tid; q < N * N; q += BLOCK) s_op[q] = (VOL == VOL_WEAK) ? p.dhat[q] : p.dsplit[q];
     const int64_t e0 = (int64_t)blockIdx.x * EPB;
@@ -74,27 +121,38 @@ struct AdvKernel {
       const int64_t g = e * NN + node;
       ureg = p.u_in[g];
       if (use_k) kreg = p.k[g];
-      if constexpr (DIM == 3) ui = narrow_hw(ureg);
-      else ui = from_double<R>(ureg);
+      // the FP64 pipe carries the neighbours' narrowing and the RK update
+      // here, so the owner's value narrows on the integer pipe
+      ui = from_double<R>(ureg);
       s_u[el * NN + node] = ui;
+      if constexpr (sizeof(R) == 4) {
+        // the element's scale, once per element (as phase A of the generic kernel)
+        if (node == 0) {
+          const double dte = p.dt_elem ? p.dt_elem[e] : p.dt;
+          s_scale[el] = from_double<R>(-p.inv_jac[e] * (mode == MODE_RK ? dte : 1.0));
+        }
+      }
     }
+    const AdvTables<DIM, N> &tab = g_adv_tables<DIM, N>;
     R outer[IPT];
     bool conforming[IPT];
+    uint32_t item[IPT];
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
       outer[i] = R(0);
       conforming[i] = true;
+      item[i] = 0;
       const int j = tid + i * BLOCK;
       if (!surface || j >= ITEMS) continue;
       const int fe = j / FPE, r = j - (j / FPE) * FPE;
-      const int face = r / NF, t = r - (r / NF) * NF;
       if (e0 + fe >= p.nelements) continue;
+      item[i] = __ldg(&tab.face[r]);
+      const int face = (item[i] >> 16) & 7;
       const int32_t nb = p.face_table[(e0 + fe) * (2 * DIM) + face];
       if (nb >= 0) {
-        const int other = line_node_rt<DIM, N>(face >> 1, t, (face & 1) ? 0 : N - 1);
-        outer[i] = narrow_hw(p.u_in[(int64_t)nb * NN + other]);
+        outer[i] = narrow_hw(p.u_in[(int64_t)nb * NN + ((item[i] >> 8) & 255)]);
       } else {
-        outer[i] = narrow_hw(p.mortar_flux[(int64_t)(-nb - 1) * NF + t]);
+        outer[i] = narrow_hw(p.mortar_flux[(int64_t)(-nb - 1) * NF + (item[i] >> 19)]);
         conforming[i] = false;
       }
     }
@@ -107,14 +165,13 @@ struct AdvKernel {
       for (int i = 0; i < IPT; ++i) {
         const int j = tid + i * BLOCK;
         if (j >= ITEMS) continue;
-        const int fe = j / FPE, r = j - (j / FPE) * FPE;
-        const int face = r / NF, t = r - (r / NF) * NF;
+        const int fe = j / FPE;
         if (e0 + fe >= p.nelements) continue;
         R f = outer[i];
         if (conforming[i]) {
-          const int o = face >> 1;
-          const R own = s_u[fe * NN + line_node_rt<DIM, N>(o, t, (face & 1) ? N - 1 : 0)];
-          const R a = p.pp.a[o];
+          const int face = (item[i] >> 16) & 7;
+          const R own = s_u[fe * NN + (item[i] & 255)];
+          const R a = p.pp.a[face >> 1];
           f = (face & 1) ? face_flux(kind, a, own, outer[i]) : face_flux(kind, a, outer[i], own);
         }
         s_f[j] = f;
@@ -124,21 +181,13 @@ struct AdvKernel {
     if (!has) return;
     // phase C
     constexpr int strides[3] = {1, N, N * N};
-    int coord[3] = {0, 0, 0}, tface[3] = {0, 0, 0};
+    int coord[3], tface[3];
     {
-      int qq = node;
+      const uint32_t nd = __ldg(&tab.node[node]);
 #pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        coord[d] = qq % N;
-        qq /= N;
-      }
-      if constexpr (DIM == 2) {
-        tface[0] = coord[1];
-        tface[1] = coord[0];
-      } else if constexpr (DIM == 3) {
-        tface[0] = coord[1] + N * coord[2];
-        tface[1] = coord[0] + N * coord[2];
-        tface[2] = coord[0] + N * coord[1];
+      for (int d = 0; d < 3; ++d) {
+        coord[d] = (nd >> (4 * d)) & 15;
+        tface[d] = (nd >> (12 + 6 * d)) & 63;
       }
     }
     R acc = R(0);
@@ -174,8 +223,8 @@ struct AdvKernel {
       p.out[g] = to_double(acc);
       return;
     }
-    const double dte = p.dt_elem ? p.dt_elem[e] : p.dt;
     if constexpr (sizeof(R) == sizeof(double)) {
+      const double dte = p.dt_elem ? p.dt_elem[e] : p.dt;
       const double du = double(acc) * -p.inv_jac[e];
       if (mode == MODE_RHS) {
         p.out[g] = du;
@@ -186,8 +235,7 @@ struct AdvKernel {
       }
     } else {
       // mixed precision: scale in FP32, widen exactly, accumulate in FP64
-      const R sc = from_double<R>(-p.inv_jac[e] * (mode == MODE_RK ? dte : 1.0));
-      const double dd = to_double(acc * sc);
+      const double dd = to_double(acc * s_scale[el]);
       if (mode == MODE_RHS) {
         p.out[g] = dd;
       } else {
