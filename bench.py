@@ -400,16 +400,16 @@ def adjoint_path(device, nsteps=200, snapshots=15, ndirs=16):
 
 
 def e2e_path(precision, steps, warmup, device, slots=3):
-    """The public API call with host buffers.  Every step copies its input
-    state from pinned host memory (H2D), advances it one CK2N54 step through
-    trixicuda.rk_steps (the C ABI's trixi_rk_steps) and copies the result back
-    (D2H); every byte crosses the host link inside the timed region.  The
-    steps are independent problems: `slots` of them are in flight on separate
-    streams, each with its own handle, device buffers and host buffers, so one
-    step's copies overlap another step's compute (H2D and D2H use separate
-    copy engines).  The computes themselves stay serialised (each waits for
-    the previous step's), so only the transfers are hidden.  slots = 1 is the
-    serial form.  Returns ms per step."""
+    """The public API call with host buffers: trixicuda.rk_steps_host (the C
+    ABI's trixi_rk_steps_host).  Every step uploads its input state from
+    pinned host memory (H2D), advances it one CK2N54 step and downloads the
+    result (D2H), all inside the timed region.  The steps are independent
+    problems: `slots` of them are in flight on separate streams, each with its
+    own handle and host buffers, so one step's copies overlap another step's
+    compute (H2D and D2H use separate copy engines).  The computes themselves
+    stay serialised -- each step's first stage waits for the previous step's
+    last (the call's wait_event / done_event hooks) -- so only the transfers
+    are hidden.  slots = 1 is the serial form.  Returns ms per step."""
     import torch
 
     import trixicuda as T
@@ -422,24 +422,15 @@ def e2e_path(precision, steps, warmup, device, slots=3):
         T.autotune(sm.compute_coefficients(), sm)  # setup, outside the timed region
     host = [torch.from_numpy(u0.copy()).pin_memory() for _ in range(slots)]
     out = [torch.empty_like(h).pin_memory() for h in host]
-    u = [torch.empty(h.shape, dtype=torch.float64, device=device) for h in host]
-    k = [torch.zeros_like(x) for x in u]
     streams = [torch.cuda.Stream(device=device) for _ in range(slots)]
-
-    done = [None]  # the previous step's compute: steps compute one after another, as in `value`
+    done = [torch.cuda.Event() for _ in range(slots)]
+    prev = [None]  # the previous step's done event: steps compute one after another, as in `value`
 
     def step(i):
         j = i % slots
-        st = streams[j]
-        with torch.cuda.stream(st):
-            u[j].copy_(host[j], non_blocking=True)
-            if done[0] is not None:
-                st.wait_event(done[0])
-            T.rk_steps(u[j], k[j], 0.0, dt, 1, semis[j], stream=st)
-            ev = torch.cuda.Event()
-            ev.record(st)
-            done[0] = ev
-            out[j].copy_(u[j], non_blocking=True)
+        T.rk_steps_host(host[j], out[j], 0.0, dt, 1, semis[j], stream=streams[j], wait_event=prev[0],
+                        done_event=done[j])
+        prev[0] = done[j]
 
     for i in range(warmup * slots):
         step(i)
@@ -665,7 +656,7 @@ def main():
                  "fp64_fma_peak_tflops": fp64_peak.value / 1e12, "fp32_fma_peak_tflops": fp32_peak.value / 1e12},
         "equal_l2": l2,
         "e2e": {"value": per_step_updates / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "api": "trixicuda.rk_steps (C ABI trixi_rk_steps)",
+                "d2h_bytes_per_step": nbytes, "api": "trixicuda.rk_steps_host (C ABI trixi_rk_steps_host)",
                 "pipeline": ("3 independent steps in flight on 3 streams (one handle each): H2D, step, D2H; "
                              "the steps' computes serialised, the copies overlap them"),
                 "serial_value": per_step_updates / (e2e_serial_ms * 1e-3)},

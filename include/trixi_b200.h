@@ -211,6 +211,23 @@ int trixi_rk_stage(trixi_handle *h, double *u_out, const double *u_in, double *k
 int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt,
                    int64_t nsteps, void *stream);
 
+/* trixi_rk_steps on a state in host memory, for callers whose state lives on
+ * the host between steps (no counterpart in the reference, whose rhs_gpu!
+ * works on device arrays): copies u_in (host, the handle's state layout) to
+ * a library-owned device buffer, runs nsteps CarpenterKennedy2N54 steps
+ * there (the 2N register is library-owned too: a step's first stage does not
+ * read it) and copies the result to u_out (host; may be u_in).  Everything
+ * is enqueued on `stream`; with page-locked host buffers the call returns
+ * before the copies finish (synchronise the stream before reading u_out),
+ * with pageable ones the copies block.  Optional ordering hooks for several
+ * calls in flight on different streams (NULL: none): `stream` waits for
+ * `wait_event` (a cudaEvent_t) after the upload and before the first stage,
+ * and `done_event` is recorded after the last stage, before the download.
+ * Calls on the same handle share its device buffers: calls that overlap on
+ * the GPU race. */
+int trixi_rk_steps_host(trixi_handle *h, const double *u_in, double *u_out, double t, double dt, int64_t nsteps,
+                        void *wait_event, void *done_event, void *stream);
+
 /* Tile tuner (no counterpart in the reference).  The fused kernel's tile --
  * warps per element group and groups per block, i.e. threads per node and
  * elements per block -- is a launch parameter.  trixi_autotune times the RK

@@ -130,6 +130,7 @@ def test_null_arguments():
     lib = _lib.load()
     assert lib.trixi_create(None, None) == 1
     assert lib.trixi_rhs(None, None, None, 0.0, None) == 1
+    assert lib.trixi_rk_steps_host(None, None, None, 0.0, 1e-3, 1, None, None, None) == 1
     assert lib.trixi_destroy(None) == 0
     buf = C.create_string_buffer(4)
     lib.trixi_last_error(None, buf, 4)

@@ -110,6 +110,30 @@ struct AdvKernel {
     const int mode = p.mode;
     const bool surface = mode != MODE_VOLUME;
     const bool use_k = mode == MODE_RK && p.use_k;
+    // the connectivity, the face-node tables and the geometry are constant:
+    // loaded before the wait for the previous kernel, so that the neighbour
+    // values need one global round trip after it
+    const AdvTables<DIM, N> &tab = g_adv_tables<DIM, N>;
+    R outer[IPT];
+    bool conforming[IPT];
+    uint32_t item[IPT];
+    int32_t nbs[IPT];
+#pragma unroll
+    for (int i = 0; i < IPT; ++i) {
+      item[i] = 0;
+      nbs[i] = 0;
+      const int j = tid + i * BLOCK;
+      if (!surface || j >= ITEMS) continue;
+      const int fe = j / FPE, r = j - (j / FPE) * FPE;
+      if (e0 + fe >= p.nelements) continue;
+      item[i] = __ldg(&tab.face[r]);
+      nbs[i] = __ldg(p.face_table + (e0 + fe) * (2 * DIM) + ((item[i] >> 16) & 7));
+    }
+    double inv_jac_e = 0.0, dt_e = p.dt;
+    if (has) {
+      inv_jac_e = __ldg(p.inv_jac + e);
+      if (p.dt_elem) dt_e = __ldg(p.dt_elem + e);
+    }
     if (p.pdl) {
       asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
       asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -127,28 +151,18 @@ struct AdvKernel {
       s_u[el * NN + node] = ui;
       if constexpr (sizeof(R) == 4) {
         // the element's scale, once per element (as phase A of the generic kernel)
-        if (node == 0) {
-          const double dte = p.dt_elem ? p.dt_elem[e] : p.dt;
-          s_scale[el] = from_double<R>(-p.inv_jac[e] * (mode == MODE_RK ? dte : 1.0));
-        }
+        if (node == 0) s_scale[el] = from_double<R>(-inv_jac_e * (mode == MODE_RK ? dt_e : 1.0));
       }
     }
-    const AdvTables<DIM, N> &tab = g_adv_tables<DIM, N>;
-    R outer[IPT];
-    bool conforming[IPT];
-    uint32_t item[IPT];
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
       outer[i] = R(0);
       conforming[i] = true;
-      item[i] = 0;
       const int j = tid + i * BLOCK;
       if (!surface || j >= ITEMS) continue;
-      const int fe = j / FPE, r = j - (j / FPE) * FPE;
+      const int fe = j / FPE;
       if (e0 + fe >= p.nelements) continue;
-      item[i] = __ldg(&tab.face[r]);
-      const int face = (item[i] >> 16) & 7;
-      const int32_t nb = p.face_table[(e0 + fe) * (2 * DIM) + face];
+      const int32_t nb = nbs[i];
       if (nb >= 0) {
         outer[i] = narrow_hw(p.u_in[(int64_t)nb * NN + ((item[i] >> 8) & 255)]);
       } else {
@@ -224,8 +238,8 @@ struct AdvKernel {
       return;
     }
     if constexpr (sizeof(R) == sizeof(double)) {
-      const double dte = p.dt_elem ? p.dt_elem[e] : p.dt;
-      const double du = double(acc) * -p.inv_jac[e];
+      const double dte = dt_e;
+      const double du = double(acc) * -inv_jac_e;
       if (mode == MODE_RHS) {
         p.out[g] = du;
       } else {

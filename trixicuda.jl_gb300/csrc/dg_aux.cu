@@ -235,9 +235,14 @@ template <typename R>
 __device__ __forceinline__ R ind_load(const double *p) { return R(*p); }
 template <>
 __device__ __forceinline__ float ind_load<float>(const double *p) { return from_double<float>(*p); }
+// the FP32 copy of u that trixi_rk_steps keeps between FP32-mixed stages
+// holds the same narrowing of u
+template <typename R>
+__device__ __forceinline__ R ind_load(const float *p) { return *p; }
 
-template <int DIM, int N, typename R>
-__global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const double *__restrict__ u,
+// In: double (u itself) or float (its FP32 copy, FP32 arithmetic only)
+template <int DIM, int N, typename R, typename In = double>
+__global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const In *__restrict__ u,
                                                             double *__restrict__ alpha_raw, double gamma_, double amax,
                                                             double amin, double threshold_, double param_s_,
                                                             IvdmMat ivdm, int mhd, int nv, int variable) {
@@ -254,7 +259,7 @@ __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const dou
   if (e < E) {
     const R gm1 = R(gamma_ - 1.0);
     for (int n = lane; n < NN; n += 32) {
-      const double *un = u + (e * NN + n) * nv;
+      const In *un = u + (e * NN + n) * nv;
       R c[9];
 #pragma unroll
       for (int v = 0; v < 9; ++v)
@@ -308,7 +313,12 @@ static cudaError_t launch_indicator_raw(const IndicatorHost &ih, cudaStream_t s)
   const int64_t grid = (ih.nelements + 7) / 8;
   IvdmMat iv;
   std::copy(ih.ivdm, ih.ivdm + HOST_NMAX * HOST_NMAX, iv.m);
-  if (ih.mixed) {
+  if (ih.mixed && ih.u32) {
+    const size_t smem = sizeof(float) * (size_t)(N * N + 8 * 2 * NN);
+    indicator_raw_kernel<DIM, N, float, float><<<(unsigned)grid, 256, smem, s>>>(
+        ih.nelements, ih.u32, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
+        ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable);
+  } else if (ih.mixed) {
     const size_t smem = sizeof(float) * (size_t)(N * N + 8 * 2 * NN);
     indicator_raw_kernel<DIM, N, float><<<(unsigned)grid, 256, smem, s>>>(
         ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,

@@ -63,6 +63,12 @@ struct FusedParams {
   double src[3];                            // (c, A, L) of the convergence-test source
   int vec16;                                // u_in, out, k, mortar_flux 16-byte aligned
   double atol;                              // dg-only test for alpha
+  // FP32-mixed RK stages inside trixi_rk_steps: the previous stage's output
+  // narrowed to FP32 (round to nearest even, the narrowing phase A applies to
+  // u_in), read in place of u_in for the flux states, and this stage's output
+  // narrowed the same way for the next stage; null when absent
+  const float *__restrict__ u32_in;         // [E][NN][NV]
+  float *__restrict__ u32_out;              // [E][NN][NV]
   PhysParams<R> pp;
   R dsplit[NMAXT * NMAXT];                  // row-major [i][m], diagonal zeroed
   R dhat[NMAXT * NMAXT];                    // row-major [i][m]
@@ -189,7 +195,81 @@ __device__ __forceinline__ void stg_node(double *dst, const double *src, bool ve
   for (int v = 0; v < NV; ++v) dst[v] = src[v];
 }
 
+// The NV floats of one node record of an FP32 state copy (16-byte records
+// when NV == 4: the copies are allocated by the library).
+template <int NV>
+__device__ __forceinline__ void ldg_rec32(const float *src, float *dst) {
+  if constexpr (NV == 4) {
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(src));
+    dst[0] = t.x;
+    dst[1] = t.y;
+    dst[2] = t.z;
+    dst[3] = t.w;
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dst[v] = __ldg(src + v);
+  }
+}
+template <int NV>
+__device__ __forceinline__ void stg_rec32(float *dst, const float *src) {
+  if constexpr (NV == 4) {
+    *reinterpret_cast<float4 *>(dst) = make_float4(src[0], src[1], src[2], src[3]);
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dst[v] = src[v];
+  }
+}
+
 constexpr int round_up4(int x) { return (x + 3) & ~3; }
+
+// Asynchronous global -> shared copies (cp.async): the copy needs no
+// registers while in flight; cp.async.wait_all makes the executing thread's
+// copies complete, a barrier after it makes them visible to the group.
+__device__ __forceinline__ void cp_async16(void *dst_smem, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst_smem, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// One-dimensional bulk copy global -> shared by the TMA unit
+// (cp.async.bulk, no tensor map), completing on an mbarrier with a
+// transaction count.  Both addresses 16-byte aligned, size a multiple of 16.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  // make the initialised barrier visible to the asynchronous (TMA) proxy
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+// Waits for phase `parity` of the barrier, at most `limit` polls (each
+// try_wait may itself suspend the thread for a short while); false when the
+// limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, int limit) {
+  const unsigned a = smem_u32(bar);
+  for (int i = 0; i < limit; ++i) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 
 // BND = 1: the instantiation for non-periodic meshes and source terms (the
 // Dirichlet states of boundary faces in phase A, the source in phase C);
@@ -224,6 +304,8 @@ struct FusedKernel {
   // (a further 2-3 %; in 2D that costs 6 %).
   static constexpr bool HW_TRACE = true;
   static constexpr bool HW_OWNER = (DIM == 3);
+  // the FP32 copy of an RK stage's output (u32_out): narrowed on the FP64 pipe
+  static constexpr bool HW_OUT = true;
   template <bool HW>
   __device__ __forceinline__ static R narrow(double x) {
     if constexpr (HW) return R(x);
@@ -250,6 +332,17 @@ struct FusedKernel {
   // stage kernel's, FP32 arithmetic 20 %).  FP64 keeps the symmetric pairs:
   // it is bound by GB300's FP64 pipe, where the flux arithmetic is the cost.
   static constexpr bool OWNER_PAIRS = (VOL != VOL_WEAK) && !LINEAR && sizeof(R) == 4;
+  // Euler flux_ranocha in FP32: the owner's DIM (N-1) partner fluxes, taken
+  // two at a time in the halves of float2 registers (ranocha_x2, packed FP32
+  // instructions); partner J of the flattened list is k = 1 + J % (N-1)
+  // steps along direction J / (N-1).  Measured on the 2D Euler level-7
+  // stage kernel: FP32 instructions -36 %, all instructions -7 % (the pairs
+  // cost register moves), 18.35 -> 17.41 us per launch.  2D up to N = 4
+  // (the higher-N kernels spill at their register caps with it); 3D for
+  // N = 4 without boundary support, and only with u and k staged in shared
+  // memory (UK_SMEM below) -- the other 3D kernels still spill with it.
+  static constexpr bool PACKED = OWNER_PAIRS && EQ == EQ_EULER && VFLUX == FLUX_RANOCHA &&
+                                 ((DIM == 2 && N <= 4) || (DIM == 3 && N == 4 && !BND));
   static constexpr int VOL_PER_DIR = (LINEAR || OWNER_PAIRS) ? 0 : (VOL == VOL_WEAK) ? NN : NF * NP;
   static constexpr int SURF_PER_EL = 2 * DIM * NF;
   static constexpr int FV_PER_DIR = (VOL == VOL_SC) ? NF * (N - 1) : 0;
@@ -263,16 +356,30 @@ struct FusedKernel {
   // shared memory of one group of `epg` elements (every array 16-byte aligned)
   static constexpr int n_cons(int epg) { return round_up4(epg * NN * NV); }
   static constexpr int n_vol(int epg) { return round_up4(epg * DIM * VOL_PER_DIR * NV); }
-  static constexpr int n_surf(int epg) { return round_up4(epg * SURF_PER_EL * NV); }
   static constexpr int n_fv(int epg) { return round_up4(epg * DIM * FV_PER_DIR * FV_RECS * NV); }
   static constexpr int n_trace(int epg) { return round_up4(epg * TRACE_PER_EL); }
   static constexpr int n_el(int epg) { return round_up4(epg); }
   static constexpr int N_OPS = round_up4(2 * N * N + N);  // D_split, D_hat, 1/w
-  static constexpr size_t group_smem(int epg) {
-    return sizeof(R) * (size_t)(2 * n_cons(epg) + n_vol(epg) + n_surf(epg) + n_fv(epg) + n_trace(epg) +
+  // FP32 RK stages of the packed 3D kernels: the FP64 u and k of the
+  // group's nodes are copied into shared memory while phases A and B run
+  // (cp.async), so that no thread holds them in registers until phase C.
+  // The packed 3D flux_ranocha needs those registers (without the copies it
+  // spills at the 64-register cap); measured on the 3D shock-capturing
+  // level-5 workload, 1.032 -> 0.990 ms per step.  Without packing the
+  // copies cost more than they save (1.070 ms; 2D: 68.2 -> 70.0 us per step).
+  static constexpr bool UK_SMEM = PACKED && DIM == 3;
+  static constexpr int n_uk(int epg) { return UK_SMEM ? ((epg * NN * NV + 1) & ~1) : 0; }  // doubles
+  static constexpr int N_BAR = UK_SMEM ? 2 : 0;  // doubles: the group's mbarrier (8 bytes, 16-byte slot)
+  static constexpr size_t group_smem_core(int epg) {
+    // (the surface fluxes overwrite the neighbour traces in place: n_surf is not added)
+    return sizeof(R) * (size_t)(2 * n_cons(epg) + n_vol(epg) + n_fv(epg) + n_trace(epg) +
                                 2 * n_el(epg) + N_OPS) +
            sizeof(int) * (size_t)round_up4(epg * 2 * DIM);
   }
+  static constexpr size_t group_smem(int epg) {
+    return group_smem_core(epg) + sizeof(double) * (2 * n_uk(epg) + N_BAR);
+  }
+
   static constexpr int warps_for(int epg) { return (epg * TPE + 31) / 32; }
   // Warp passes of phase B for a group of `epg` elements: items are ordered
   // [volume dir 0 | dir 1 | ... | surface dir 0 | ... | FV dir 0 | ...] and a
@@ -302,7 +409,7 @@ struct FusedKernel {
     long best_cost = -1;
     for (int e = 1; e <= 32; e *= 2) {
       if (warps_for(e) > 8) break;
-      if (e > 1 && group_smem(e) > 48 * 1024) break;
+      if (e > 1 && group_smem_core(e) > 48 * 1024) break;
       // cost per element in 1/1000 units: passes plus idle-lane waste of phases A/C
       const long cost = 1000L * phase_b_passes(e) / e + 1000L * (warps_for(e) * 32 - e * TPE) / (32 * e);
       if (best_cost < 0 || cost < best_cost) {
@@ -323,10 +430,12 @@ struct FusedKernel {
   static constexpr int GT = 32 * WPG;                  // threads per group
   static constexpr int N_CONS = n_cons(EPG);
   static constexpr int N_VOL = n_vol(EPG);
-  static constexpr int N_SURF = n_surf(EPG);
   static constexpr int N_FV = n_fv(EPG);
   static constexpr int N_TRACE = n_trace(EPG);
   static constexpr int N_EL = n_el(EPG);
+  static constexpr int N_UK = n_uk(EPG);
+  // trace items per thread of phase A at the narrowest group (the owners' warps)
+  static constexpr int TR_IT = (EPG * 2 * DIM * NF + 32 * warps_for(EPG) - 1) / (32 * warps_for(EPG));
   static constexpr size_t GROUP_SMEM = group_smem(EPG);
   static constexpr int gpb_pick() {
     int g = 8 / WPG;
@@ -342,6 +451,8 @@ struct FusedKernel {
   static size_t smem_bytes() { return smem_for(EPB); }
 
   struct Smem {
+    double *u64, *k64;  // UK_SMEM: the group's u and k, [el][node][v]
+    uint64_t *bar;      // UK_SMEM: mbarrier of their bulk copy
     R *cons, *prim, *fvol, *fsurf, *ffv, *trace, *alpha, *scale, *dsplit, *dhat, *invw;
     int *conforming;  // [el][face]: 1 = trace holds the neighbour's node, 0 = a mortar flux
     // node records [el][node][v]
@@ -469,15 +580,6 @@ struct FusedKernel {
     }
   }
 
-  // Euler flux_ranocha in FP32: the owner's DIM (N-1) partner fluxes, taken
-  // two at a time in the halves of float2 registers (ranocha_x2, packed FP32
-  // instructions); partner J of the flattened list is k = 1 + J % (N-1)
-  // steps along direction J / (N-1).  Measured on the 2D Euler level-7
-  // stage kernel: FP32 instructions -36 %, all instructions -7 % (the pairs
-  // cost register moves), 18.35 -> 17.41 us per launch.  Used in 2D up to
-  // N = 4 only: the 3D and higher-N kernels spill at their register caps with
-  // it and did not gain (3D shock capturing: 210.9 us either way).
-  static constexpr bool PACKED = OWNER_PAIRS && EQ == EQ_EULER && VFLUX == FLUX_RANOCHA && DIM == 2 && N <= 4;
   template <int J>
   __device__ __forceinline__ static void partner(const Smem &s, int node, const int *coord, int &nm, R &dm) {
     constexpr int O = J / (N - 1), k = 1 + J % (N - 1);
@@ -530,12 +632,15 @@ struct FusedKernel {
     const int gid = threadIdx.y;  // group within the block
     const int gt = threadIdx.x;
     Smem s;
-    s.cons = reinterpret_cast<R *>(smem_raw + gid * GROUP_SMEM);
+    s.u64 = reinterpret_cast<double *>(smem_raw + gid * GROUP_SMEM);
+    s.k64 = s.u64 + N_UK;
+    s.bar = reinterpret_cast<uint64_t *>(s.k64 + N_UK);
+    s.cons = reinterpret_cast<R *>(s.k64 + N_UK + N_BAR);
     s.prim = s.cons + N_CONS;
     s.fvol = s.prim + N_CONS;
-    s.fsurf = s.fvol + N_VOL;
-    s.ffv = s.fsurf + N_SURF;
+    s.ffv = s.fvol + N_VOL;
     s.trace = s.ffv + N_FV;
+    s.fsurf = s.trace;  // each surface item overwrites its own trace record
     s.alpha = s.trace + N_TRACE;
     s.scale = s.alpha + N_EL;
     s.dsplit = s.scale + N_EL;
@@ -556,6 +661,30 @@ struct FusedKernel {
     const bool surface = (mode != MODE_VOLUME);
     const bool vec = p.vec16 != 0;
     const bool use_k = (mode == MODE_RK) && p.use_k;
+    // The connectivity and the geometry are constant: their loads go out
+    // before the wait for the previous kernel below, so that the neighbour
+    // traces of phase A need one global round trip after it, not two (face
+    // table, then the neighbour's node).  nbp[it]: the face-table entry of
+    // this thread's trace item it (items j = gt + it * GTr).
+    constexpr int PER_EL = 2 * DIM * NF;
+    const int n_trace = surface ? ne * PER_EL : 0;
+    int32_t nbp[TR_IT];
+#pragma unroll
+    for (int it = 0; it < TR_IT; ++it) {
+      const int j = gt + it * GTr;
+      nbp[it] = 0;
+      if (j < n_trace) {
+        const int el = j / PER_EL, face = (j - el * PER_EL) / NF;
+        nbp[it] = __ldg(p.face_table + (e0 + el) * (2 * DIM) + face);
+      }
+    }
+    const int my_el = gt / NN, my_node = gt - (gt / NN) * NN;
+    const bool has_node = (gt < EPG * NN) && (my_el < ne);
+    double inv_jac_el = 0.0, dt_el = p.dt;  // the owner's element's J^{-1} and time step
+    if (has_node) {
+      inv_jac_el = __ldg(p.inv_jac + e0 + my_el);
+      if (p.dt_elem) dt_el = __ldg(p.dt_elem + e0 + my_el);
+    }
     if (p.pdl) {
       // programmatic dependent launch: the next kernel in the stream may start
       // launching now (it waits below before its own reads), and this grid
@@ -569,49 +698,105 @@ struct FusedKernel {
     // (el, node) keeps its node's u and k in registers until phase C; all
     // threads stage the neighbours' face nodes (or the mortar fluxes) of the
     // group's faces in shared memory.
-    const int my_el = gt / NN, my_node = gt - (gt / NN) * NN;
-    const bool has_node = (gt < EPG * NN) && (my_el < ne);
     const int64_t g0 = ((e0 + my_el) * NN + my_node) * NV;
+    // FP32 copy of u_in (FP32 kernels inside trixi_rk_steps), else null
+    const float *sh_in = nullptr;
+    if constexpr (sizeof(R) == 4) sh_in = p.u32_in;
     double ureg[NV], kreg[NV];
-    if (has_node) {
-      ldg_node<NV>(p.u_in + g0, ureg, vec);
-      if (use_k) ldg_node<NV>(p.k + g0, kreg, vec);
-    }
-    if (surface) {
-      constexpr int PER_EL = 2 * DIM * NF;
-      const int n_trace = ne * PER_EL;
-      for (int j = gt; j < n_trace; j += GTr) {
-        const int el = j / PER_EL, r = j - (j / PER_EL) * PER_EL;
-        const int face = r / NF, t = r - (r / NF) * NF;
-        const int32_t nb = p.face_table[(e0 + el) * (2 * DIM) + face];
-        double tv[NV];
-        if (nb >= 0) {
-          const int o = face >> 1;
-          const int other = line_node_rt<DIM, N>(o, t, (face & 1) ? 0 : N - 1);
-          ldg_node<NV>(p.u_in + ((int64_t)nb * NN + other) * NV, tv, vec);
-        } else if (BND && nb == FACE_BOUNDARY) {
-          // Dirichlet boundary: the boundary function's state at the face node
-          // plays the neighbour's trace (the surface flux then follows the
-          // interface convention: inner state on the left of an upper face)
-          if constexpr (BND) {
-            const int o = face >> 1;
-            const int own = line_node_rt<DIM, N>(o, t, (face & 1) ? N - 1 : 0);
-            eval_ic<DIM, EQ>(p.bc_kind, p.coords + ((e0 + el) * NN + own) * DIM, p.t, p.bc, tv);
+    R uown[NV];
+    bool bulk = false;  // UK_SMEM: u and k come by one bulk copy each (else by cp.async per thread)
+    if constexpr (UK_SMEM) {
+      if (mode == MODE_RK) {
+        // the group's u (and k) spans, contiguous in global memory
+        const int nval = ne * NN * NV;
+        const double *gu = p.u_in + e0 * NN * NV, *gk = p.k + e0 * NN * NV;
+        const bool a16 = vec && ((e0 * NN * NV) & 1) == 0;  // 16-byte aligned span starts
+        bulk = a16 && (nval & 1) == 0;                        // and 16-byte multiples
+        if (bulk) {
+          if (gt == 0) {
+            const unsigned bytes = 8u * (unsigned)nval;
+            mbar_init(s.bar, 1);
+            mbar_expect_tx(s.bar, use_k ? 2 * bytes : bytes);
+            bulk_g2s(s.u64, gu, bytes, s.bar);
+            if (use_k) bulk_g2s(s.k64, gk, bytes, s.bar);
+          }
+        } else if (a16) {
+          const int nc = nval >> 1;
+          for (int c = gt; c < nc; c += GTr) {
+            cp_async16(s.u64 + 2 * c, gu + 2 * c);
+            if (use_k) cp_async16(s.k64 + 2 * c, gk + 2 * c);
+          }
+          if ((nval & 1) && gt == 0) {
+            cp_async8(s.u64 + nval - 1, gu + nval - 1);
+            if (use_k) cp_async8(s.k64 + nval - 1, gk + nval - 1);
           }
         } else {
-          ldg_node<NV>(p.mortar_flux + ((int64_t)(-nb - 1) * NF + t) * NV, tv, vec);
+          for (int c = gt; c < nval; c += GTr) {
+            cp_async8(s.u64 + c, gu + c);
+            if (use_k) cp_async8(s.k64 + c, gk + c);
+          }
         }
-        R tr[NV];
+      }
+      if (has_node) {
+        if (sh_in != nullptr) {
+          if constexpr (sizeof(R) == 4) ldg_rec32<NV>(sh_in + g0, uown);
+        } else {
+          ldg_node<NV>(p.u_in + g0, ureg, vec);
+        }
+      }
+    } else if (has_node) {
+      ldg_node<NV>(p.u_in + g0, ureg, vec);
+      if (use_k) ldg_node<NV>(p.k + g0, kreg, vec);
+      if constexpr (sizeof(R) == 4)
+        if (sh_in) ldg_rec32<NV>(sh_in + g0, uown);
+    }
+    if (surface) {
 #pragma unroll
-        for (int v = 0; v < NV; ++v) tr[v] = narrow<HW_TRACE>(tv[v]);
+      for (int it = 0; it < TR_IT; ++it) {
+        const int j = gt + it * GTr;
+        if (j >= n_trace) break;
+        const int el = j / PER_EL, r = j - (j / PER_EL) * PER_EL;
+        const int face = r / NF, t = r - (r / NF) * NF;
+        const int32_t nb = nbp[it];
+        R tr[NV];
+        if (sh_in != nullptr && nb >= 0) {
+          // the neighbour's node from the FP32 copy: no conversion
+          const int other = line_node_rt<DIM, N>(face >> 1, t, (face & 1) ? 0 : N - 1);
+          if constexpr (sizeof(R) == 4) ldg_rec32<NV>(sh_in + ((int64_t)nb * NN + other) * NV, tr);
+        } else {
+          double tv[NV];
+          if (nb >= 0) {
+            const int o = face >> 1;
+            const int other = line_node_rt<DIM, N>(o, t, (face & 1) ? 0 : N - 1);
+            ldg_node<NV>(p.u_in + ((int64_t)nb * NN + other) * NV, tv, vec);
+          } else if (BND && nb == FACE_BOUNDARY) {
+            // Dirichlet boundary: the boundary function's state at the face node
+            // plays the neighbour's trace (the surface flux then follows the
+            // interface convention: inner state on the left of an upper face)
+            if constexpr (BND) {
+              const int o = face >> 1;
+              const int own = line_node_rt<DIM, N>(o, t, (face & 1) ? N - 1 : 0);
+              eval_ic<DIM, EQ>(p.bc_kind, p.coords + ((e0 + el) * NN + own) * DIM, p.t, p.bc, tv);
+            }
+          } else {
+            ldg_node<NV>(p.mortar_flux + ((int64_t)(-nb - 1) * NF + t) * NV, tv, vec);
+          }
+#pragma unroll
+          for (int v = 0; v < NV; ++v) tr[v] = narrow<HW_TRACE>(tv[v]);
+        }
         sts_rec<NV>(s.tr(el, face, t), tr);
         if (t == 0) s.conforming[el * 2 * DIM + face] = (nb >= 0 || (BND && nb == FACE_BOUNDARY));
       }
     }
     if (has_node) {
       R uu[NV], ww[NV];
+      if (sh_in != nullptr) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) uu[v] = narrow<HW_OWNER>(ureg[v]);
+        for (int v = 0; v < NV; ++v) uu[v] = uown[v];
+      } else {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) uu[v] = narrow<HW_OWNER>(ureg[v]);
+      }
       P::prim(uu, ww, p.pp);
       sts_rec<NV>(s.c(my_el, my_node), uu);
       sts_rec<NV>(s.w(my_el, my_node), ww);
@@ -621,8 +806,7 @@ struct FusedKernel {
           s.alpha[my_el] = (fabs(a) <= p.atol) ? R(0) : from_double<R>(a);
         }
         // per-element factor of the node phase: -J^{-1} (rhs) or -J^{-1} dt (RK)
-        const double dte = p.dt_elem ? p.dt_elem[e0 + my_el] : p.dt;
-        const double f = -p.inv_jac[e0 + my_el] * (mode == MODE_RK ? dte : 1.0);
+        const double f = -inv_jac_el * (mode == MODE_RK ? dt_el : 1.0);
         s.scale[my_el] = from_double<R>(f);
       }
     }
@@ -717,10 +901,33 @@ struct FusedKernel {
         }
       }
     }
+    if constexpr (UK_SMEM) {
+      if (bulk) {
+        // (phase A's barrier ordered the barrier's initialisation before this)
+        // a few KB from this GPU's memory: the limit is far beyond any
+        // completion time; running out raises the device error word
+        if (!mbar_wait(s.bar, 0, 1 << 22)) {
+          atomicOr(p.err, DEVERR_BULK_WAIT);
+          mbar_wait(s.bar, 0, 1 << 22);  // let the copies in flight land before the block may exit
+        }
+      } else {
+        cp_async_wait_all();
+      }
+    }
     group_sync(gid, p.wpg, GTr);
 
     // phase C: the thread that loaded node q finishes it
     if (!has_node) return;
+    if constexpr (UK_SMEM) {
+      if (mode == MODE_RK) {
+        const int q = (el * NN + node) * NV;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          ureg[v] = s.u64[q + v];
+          if (use_k) kreg[v] = s.k64[q + v];
+        }
+      }
+    }
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
       const int ci = coord[d];
@@ -847,8 +1054,8 @@ struct FusedKernel {
       for (int v = 0; v < NV; ++v) o[v] = to_double(acc[v]);
       stg_node<NV>(p.out + g0, o, vec);
     } else if constexpr (sizeof(R) == sizeof(double)) {
-      const double sc = -p.inv_jac[e0 + el];
-      const double dte = p.dt_elem ? p.dt_elem[e0 + el] : p.dt;
+      const double sc = -inv_jac_el;
+      const double dte = dt_el;
       double src[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) src[v] = 0.0;
@@ -882,7 +1089,7 @@ struct FusedKernel {
         if (p.src_kind != SRC_NONE) {
           source_convergence<DIM, EQ>(p.src, p.bc.gamma, p.coords + ((e0 + el) * NN + node) * DIM, p.t, src,
                                       p.src_kind);
-          const double f = (mode == MODE_RK) ? (p.dt_elem ? p.dt_elem[e0 + el] : p.dt) : 1.0;
+          const double f = (mode == MODE_RK) ? dt_el : 1.0;
 #pragma unroll
           for (int v = 0; v < NV; ++v) src[v] *= f;
         }
@@ -901,6 +1108,13 @@ struct FusedKernel {
       }
       if (mode == MODE_RK) stg_node<NV>(p.k + g0, kk, vec);
       stg_node<NV>(p.out + g0, o, vec);
+      if (p.u32_out) {
+        // the next stage's flux states: u_out narrowed as phase A would narrow it
+        R f[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) f[v] = narrow<HW_OUT>(o[v]);
+        stg_rec32<NV>(p.u32_out + g0, f);
+      }
     }
   }
 };

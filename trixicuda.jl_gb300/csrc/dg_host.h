@@ -23,6 +23,10 @@ struct FusedHost {
   const double *inv_jac = nullptr;
   const double *alpha = nullptr;
   const double *dt_elem = nullptr;
+  // FP32 copies of u_in / u_out (FP32-mixed Euler and MHD RK stages of
+  // trixi_rk_steps); null when absent
+  const float *u32_in = nullptr;
+  float *u32_out = nullptr;
   int *err = nullptr;
   int64_t nelements = 0;
   int mode = 1;
@@ -115,6 +119,7 @@ struct IndicatorHost {
   int variable = 0;    // 0: density_pressure, 1: pressure
   int64_t nelements = 0;
   const double *u = nullptr;
+  const float *u32 = nullptr;  // FP32 copy of u (mixed only): read in place of u when not null
   double *alpha_raw = nullptr;
   double *alpha = nullptr;                 // smoothed output
   const int32_t *face_table = nullptr;     // [E][2*DIM]

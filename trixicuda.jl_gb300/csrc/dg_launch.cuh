@@ -22,6 +22,9 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   p.inv_jac = h.inv_jac;
   p.alpha = h.alpha;
   p.dt_elem = h.dt_elem;
+  // the FP32 state copies exist for the FP32 instantiations only
+  p.u32_in = (sizeof(R) == 4) ? h.u32_in : nullptr;
+  p.u32_out = (sizeof(R) == 4) ? h.u32_out : nullptr;
   p.err = h.err;
   p.nelements = h.nelements;
   p.mode = h.mode;
@@ -62,6 +65,7 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
     // reported is one element group of the warps that hold an element's nodes
     // and is the only one accepted, so the tile tuner has a single candidate
     using A = AdvKernel<DIM, N, R, VOL>;
+    if (h.u32_in || h.u32_out) return cudaErrorNotSupported;  // it keeps no FP32 state copy
     if (h.tile_out) {
       h.tile_out->epg = 1;
       h.tile_out->min_wpg = h.tile_out->def_wpg = h.tile_out->max_warps = (A::NN + 31) / 32;

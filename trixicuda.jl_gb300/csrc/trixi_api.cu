@@ -96,6 +96,10 @@ struct trixi_handle {
   double *d_alpha_raw = nullptr, *d_alpha = nullptr;
   int *d_err = nullptr;
   double *d_scratch_u = nullptr, *d_scratch_u2 = nullptr;  // RK stage buffers of trixi_rk_steps
+  // FP32 copies of the stage states inside trixi_rk_steps (FP32-mixed Euler
+  // and MHD): stage g reads copy g % 2 and writes copy (g + 1) % 2
+  float *d_u32[2] = {nullptr, nullptr};
+  double *d_host_u = nullptr, *d_host_k = nullptr;  // device state and 2N register of trixi_rk_steps_host
   // stage containers (allocated on first use)
   double *d_interfaces_u = nullptr, *d_sfv = nullptr, *d_mortar_u[4] = {nullptr, nullptr, nullptr, nullptr};
   // analysis / initial conditions (allocated on first use)
@@ -170,7 +174,7 @@ void free_all(trixi_handle *h) {
                   h->d_scratch_u, h->d_scratch_u2, h->d_interfaces_u, h->d_sfv, h->d_mortar_u[0], h->d_mortar_u[1],
                   h->d_mortar_u[2], h->d_mortar_u[3], h->d_coords, h->d_acc, h->d_partial, h->d_partial2,
                   h->d_red_out, h->d_vdm, h->d_wa, h->d_w, h->d_bnd_nid, h->d_bnd_side, h->d_bnd_ori,
-                  h->d_boundaries_u};
+                  h->d_boundaries_u, h->d_u32[0], h->d_u32[1], h->d_host_u, h->d_host_k};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -536,7 +540,8 @@ void fill_mortar(const trixi_handle *h, MortarHost &mh, const double *u) {
 
 // fp32: the indicator inside an FP32-mixed rhs; the stage entry point
 // trixi_indicator always computes in FP64
-int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStream_t s, bool fp32 = false) {
+int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStream_t s, bool fp32 = false,
+                  const float *u32 = nullptr) {
   IndicatorHost ih;
   ih.dim = h->dim;
   ih.N = h->N;
@@ -546,6 +551,7 @@ int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStrea
   ih.variable = h->ind_var;
   ih.nelements = h->E;
   ih.u = u;
+  ih.u32 = fp32 ? u32 : nullptr;
   ih.alpha_raw = h->d_alpha_raw;
   ih.alpha = alpha_out;
   ih.face_table = h->d_face_table;
@@ -562,11 +568,12 @@ int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStrea
   return TRIXI_OK;
 }
 
-// Kernels of one rhs evaluation (mode RHS/RK/VOLUME) on u_in.
+// Kernels of one rhs evaluation (mode RHS/RK/VOLUME) on u_in.  u32_in /
+// u32_out: FP32 copies of u_in / out for FP32-mixed RK stages (or null).
 int run_rhs(trixi_handle *h, int mode, const double *u_in, double *out, double *k, double a, double b, double dt,
-            cudaStream_t s, double t = 0.0) {
+            cudaStream_t s, double t = 0.0, const float *u32_in = nullptr, float *u32_out = nullptr) {
   if (h->vol == TRIXI_VOLUME_SHOCK_CAPTURING_HG) {
-    int st = run_indicator(h, u_in, h->d_alpha, s, h->mixed && mode != MODE_VOLUME);
+    int st = run_indicator(h, u_in, h->d_alpha, s, h->mixed && mode != MODE_VOLUME, u32_in);
     if (st) return st;
   }
   if (h->M > 0 && mode != MODE_VOLUME) {
@@ -583,6 +590,8 @@ int run_rhs(trixi_handle *h, int mode, const double *u_in, double *out, double *
   f.rk_b = b;
   f.dt = dt;
   f.t = t;
+  f.u32_in = u32_in;
+  f.u32_out = u32_out;
   TRIXI_CUDA(h, launch_fused(h->dim, h->N, h->eq, h->vol, h->vflux, h->mixed, f, s), "fused rhs");
   return TRIXI_OK;
 }
@@ -764,16 +773,49 @@ int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt, i
   const size_t bytes = sizeof(double) * (size_t)(h->E * h->NN * h->nv);
   if (!h->d_scratch_u) TRIXI_CUDA(h, cudaMalloc(&h->d_scratch_u, bytes), "alloc RK scratch");
   if (!h->d_scratch_u2) TRIXI_CUDA(h, cudaMalloc(&h->d_scratch_u2, bytes), "alloc RK scratch");
+  // FP32-mixed Euler / MHD: each stage also writes its output narrowed to
+  // FP32, and the next stage reads its flux states (and the shock indicator
+  // its input) from that copy instead of narrowing the FP64 state again; the
+  // results are the same bits.  The first stage of a call narrows the
+  // caller's u, which may have changed since the previous call.
+  const bool copies = h->mixed && h->eq != EQ_ADV;
+  if (copies && !h->d_u32[0]) {
+    const size_t fbytes = sizeof(float) * (size_t)(h->E * h->NN * h->nv);
+    TRIXI_CUDA(h, cudaMalloc(&h->d_u32[0], fbytes), "alloc FP32 stage copy");
+    TRIXI_CUDA(h, cudaMalloc(&h->d_u32[1], fbytes), "alloc FP32 stage copy");
+  }
   // the stage inputs and outputs of one step: u -> s1 -> s2 -> s1 -> s2 -> u, so
   // that every step ends in the caller's buffer (u_out never aliases u_in)
   double *const seq[6] = {u, h->d_scratch_u, h->d_scratch_u2, h->d_scratch_u, h->d_scratch_u2, u};
+  const int64_t nstages = 5 * nsteps;
+  int64_t g = 0;  // stage counter of this call
   for (int64_t step = 0; step < nsteps; ++step) {
-    for (int st = 0; st < 5; ++st) {
-      int r = run_rhs(h, MODE_RK, seq[st], seq[st + 1], k, kCK_A[st], kCK_B[st], dt, s, t + kCK_C[st] * dt);
+    for (int st = 0; st < 5; ++st, ++g) {
+      const float *c_in = (copies && g > 0) ? h->d_u32[g & 1] : nullptr;
+      float *c_out = (copies && g + 1 < nstages) ? h->d_u32[(g + 1) & 1] : nullptr;
+      int r = run_rhs(h, MODE_RK, seq[st], seq[st + 1], k, kCK_A[st], kCK_B[st], dt, s, t + kCK_C[st] * dt, c_in,
+                      c_out);
       if (r) return r;
     }
     t += dt;
   }
+  return TRIXI_OK;
+}
+
+int trixi_rk_steps_host(trixi_handle *h, const double *u_in, double *u_out, double t, double dt, int64_t nsteps,
+                        void *wait_event, void *done_event, void *stream) {
+  if (!h) return fail(nullptr, TRIXI_ERR_INVALID_ARGUMENT, "handle is null");
+  if (!u_in || !u_out) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "host state pointer is null");
+  if (nsteps < 0 || !std::isfinite(dt)) return fail(h, TRIXI_ERR_INVALID_ARGUMENT, "nsteps %lld / dt", (long long)nsteps);
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = sizeof(double) * (size_t)(h->E * h->NN * h->nv);
+  if (!h->d_host_u) TRIXI_CUDA(h, cudaMalloc(&h->d_host_u, bytes), "alloc host-path state");
+  if (!h->d_host_k) TRIXI_CUDA(h, cudaMalloc(&h->d_host_k, bytes), "alloc host-path register");
+  TRIXI_CUDA(h, cudaMemcpyAsync(h->d_host_u, u_in, bytes, cudaMemcpyHostToDevice, s), "upload u");
+  if (wait_event) TRIXI_CUDA(h, cudaStreamWaitEvent(s, (cudaEvent_t)wait_event, 0), "wait_event");
+  if (int r = trixi_rk_steps(h, h->d_host_u, h->d_host_k, t, dt, nsteps, stream)) return r;
+  if (done_event) TRIXI_CUDA(h, cudaEventRecord((cudaEvent_t)done_event, s), "done_event");
+  TRIXI_CUDA(h, cudaMemcpyAsync(u_out, h->d_host_u, bytes, cudaMemcpyDeviceToHost, s), "download u");
   return TRIXI_OK;
 }
 

@@ -64,6 +64,7 @@ from .semidiscretization import (
     rhs_gpu,
     rk_stage,
     rk_steps,
+    rk_steps_host,
     semidiscretizeGPU,
     synchronize,
     tile,

@@ -120,6 +120,7 @@ SIGNATURES = {
     "trixi_rhs": (C.c_int, [_VP, _DP, _DP, _D, _VP]),
     "trixi_rk_stage": (C.c_int, [_VP, _DP, _DP, _DP, _D, _D, _D, _D, _VP]),
     "trixi_rk_steps": (C.c_int, [_VP, _DP, _DP, _D, _D, _I64, _VP]),
+    "trixi_rk_steps_host": (C.c_int, [_VP, _DP, _DP, _D, _D, _I64, _VP, _VP, _VP]),
     "trixi_volume_integral": (C.c_int, [_VP, _DP, _DP, _VP]),
     "trixi_prolong2interfaces": (C.c_int, [_VP, _DP, _VP]),
     "trixi_interface_flux": (C.c_int, [_VP, _VP]),

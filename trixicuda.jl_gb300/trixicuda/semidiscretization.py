@@ -408,6 +408,34 @@ def rk_steps(u, k, t, dt, nsteps, semi, stream=None):
           float(dt), int(nsteps), stream=stream)
 
 
+def rk_steps_host(u_in, u_out, t, dt, nsteps, semi, stream=None, wait_event=None, done_event=None):
+    """rk_steps on a state in host memory (C ABI trixi_rk_steps_host): u_in
+    is uploaded to a library-owned device buffer, advanced nsteps
+    CarpenterKennedy2N54 steps and downloaded to u_out, all enqueued on
+    `stream`.  u_in / u_out: contiguous float64 CPU tensors (page-locked for
+    an asynchronous call: synchronise before reading u_out) or numpy arrays;
+    wait_event / done_event: optional torch.cuda.Event ordering hooks (the
+    stream waits for wait_event before the first stage; done_event is
+    recorded after the last one)."""
+    torch = _torch()
+    n = int(math.prod(semi.u_shape()))
+
+    def ptr(a, what):
+        if isinstance(a, torch.Tensor):
+            if a.is_cuda or a.dtype != torch.float64 or not a.is_contiguous() or a.numel() != n:
+                raise ValueError(f"{what}: a contiguous float64 CPU tensor with {n} values is required")
+            return C.c_void_p(a.data_ptr())
+        if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous or a.size != n:
+            raise ValueError(f"{what}: a contiguous float64 array with {n} values is required")
+        return C.c_void_p(a.ctypes.data)
+
+    def ev(e):
+        return C.c_void_p(e.cuda_event) if e is not None else None
+
+    _call(semi, semi._lib.trixi_rk_steps_host, ptr(u_in, "u_in"), ptr(u_out, "u_out"), float(t), float(dt),
+          int(nsteps), ev(wait_event), ev(done_event), stream=stream)
+
+
 def autotune(u, semi, stream=None):
     """Picks the fused kernel's tile (warps per element group, groups per
     block) for this problem by timing every valid tile on u (read only)."""
