@@ -56,8 +56,19 @@ cudaError_t launch_t(const AdjointHost &a, cudaStream_t s) {
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   const int64_t grid = (a.nelements + K::EPB - 1) / K::EPB;
   if (grid <= 0) return cudaSuccess;
-  dg_adjoint_kernel<DIM, N, EQ, VOL><<<(unsigned)grid, K::BLOCK, smem, s>>>(p);
-  return cudaGetLastError();
+  p.pdl = a.pdl;
+  p.u_ready = a.u_ready;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(K::BLOCK);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr_pdl[1];
+  attr_pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr_pdl[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr_pdl;
+  cfg.numAttrs = a.pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, dg_adjoint_kernel<DIM, N, EQ, VOL>, p);
 }
 
 template <int DIM, int N>

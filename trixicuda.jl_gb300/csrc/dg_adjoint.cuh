@@ -225,6 +225,8 @@ struct AdjointParams {
   double dsplit[NMAXT * NMAXT];        // row-major, diagonal zeroed
   double dhat[NMAXT * NMAXT];
   double lhat_l, lhat_r;
+  int pdl;      // launched as a programmatic dependent launch
+  int u_ready;  // u does not depend on the previous kernel: read before griddepcontrol.wait
 };
 
 template <int DIM, int N, int EQ, int VOL>
@@ -273,23 +275,45 @@ struct AdjointKernel {
     auto W = [&](int el, int v, int n) -> double & { return s_w[(el * NV + v) * NN + n]; };
     auto Lm = [&](int el, int v, int n) -> double & { return s_l[(el * NV + v) * NN + n]; };
 
+    // the stage's state, its primitive variables and 1/rho
+    auto load_u = [&]() {
+      for (int q = threadIdx.x; q < epb * NN; q += BLOCK) {
+        const int el = q / NN, n = q - (q / NN) * NN;
+        if (el >= ne) continue;
+        const int64_t g0 = ((e0 + el) * NN + n) * NV;
+        double uu[NV], ww[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) uu[v] = p.u[g0 + v];
+        P::prim(uu, ww, p.pp);
+        s_ir[el * NN + n] = rcp_newton(uu[0]);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          U(el, v, n) = uu[v];
+          W(el, v, n) = ww[v];
+        }
+      }
+    };
+    if (threadIdx.x < ne) s_ij[threadIdx.x] = p.inv_jac[e0 + threadIdx.x];
+    if (p.pdl) {
+      // programmatic dependent launch: the next stage kernel may start
+      // launching; the cotangents (the previous kernel's output) are read
+      // only after the wait.  A stored stage state (u_ready) does not depend
+      // on the previous kernel, so its loads and FP64 work overlap that
+      // kernel's tail.
+      asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+      if (p.u_ready) load_u();
+      asm volatile("griddepcontrol.wait;" ::: "memory");
+      if (!p.u_ready) load_u();
+    } else {
+      load_u();
+    }
     for (int q = threadIdx.x; q < epb * NN; q += BLOCK) {
       const int el = q / NN, n = q - (q / NN) * NN;
       if (el >= ne) continue;
       const int64_t g0 = ((e0 + el) * NN + n) * NV;
-      double uu[NV], ww[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) uu[v] = p.u[g0 + v];
-      P::prim(uu, ww, p.pp);
-      s_ir[el * NN + n] = rcp_newton(uu[0]);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        U(el, v, n) = uu[v];
-        W(el, v, n) = ww[v];
-        Lm(el, v, n) = p.lk_in[g0 + v] + (p.lu_in ? p.rk_b * p.lu_in[g0 + v] : 0.0);
-      }
+      for (int v = 0; v < NV; ++v) Lm(el, v, n) = p.lk_in[g0 + v] + (p.lu_in ? p.rk_b * p.lu_in[g0 + v] : 0.0);
     }
-    if (threadIdx.x < ne) s_ij[threadIdx.x] = p.inv_jac[e0 + threadIdx.x];
     __syncthreads();
 
     constexpr int PER_VOL = epb * VOL_PER_DIR;

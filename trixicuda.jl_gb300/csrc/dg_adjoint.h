@@ -20,6 +20,8 @@ struct AdjointHost {
   double dsplit[HOST_NMAX * HOST_NMAX] = {};
   double dhat[HOST_NMAX * HOST_NMAX] = {};
   double lhat_l = 0, lhat_r = 0;
+  int pdl = 0;      // programmatic dependent launch after the previous stage kernel
+  int u_ready = 0;  // u was written before the previous kernel started (read before the wait)
 };
 
 bool adjoint_supported(int dim, int N, int eq, int vol, int vflux, int sflux, bool has_mortars);

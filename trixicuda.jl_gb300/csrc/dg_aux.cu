@@ -245,7 +245,14 @@ template <int DIM, int N, typename R, typename In = double>
 __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const In *__restrict__ u,
                                                             double *__restrict__ alpha_raw, double gamma_, double amax,
                                                             double amin, double threshold_, double param_s_,
-                                                            IvdmMat ivdm, int mhd, int nv, int variable) {
+                                                            IvdmMat ivdm, int mhd, int nv, int variable,
+                                                            int pdl) {
+  if (pdl) {
+    // programmatic dependent launch: the next kernel may start launching;
+    // u (the previous kernel's output) is read only after this wait
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+  }
   constexpr int NN = (DIM == 1) ? N : (DIM == 2 ? N * N : N * N * N);
   constexpr int WPB = 8;  // warps (elements) per block
   extern __shared__ __align__(16) unsigned char sm_raw[];
@@ -307,6 +314,24 @@ __global__ void __launch_bounds__(256) indicator_raw_kernel(int64_t E, const In 
   if (active && which == 0) alpha_raw[e0 + el] = ind_alpha<R>(sum, clip1, clip2, threshold_, param_s_, amax, amin);
 }
 
+// A launch that may be a programmatic dependent launch (the kernel then
+// executes griddepcontrol.wait before reading its predecessor's output).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_maybe_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                                    cudaStream_t s, bool pdl, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <int DIM, int N>
 static cudaError_t launch_indicator_raw(const IndicatorHost &ih, cudaStream_t s) {
   constexpr int NN = (DIM == 1) ? N : (DIM == 2 ? N * N : N * N * N);
@@ -315,19 +340,19 @@ static cudaError_t launch_indicator_raw(const IndicatorHost &ih, cudaStream_t s)
   std::copy(ih.ivdm, ih.ivdm + HOST_NMAX * HOST_NMAX, iv.m);
   if (ih.mixed && ih.u32) {
     const size_t smem = sizeof(float) * (size_t)(N * N + 8 * 2 * NN);
-    indicator_raw_kernel<DIM, N, float, float><<<(unsigned)grid, 256, smem, s>>>(
-        ih.nelements, ih.u32, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
-        ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable);
+    return launch_maybe_pdl(&indicator_raw_kernel<DIM, N, float, float>, (unsigned)grid, 256, smem, s, ih.pdl != 0,
+                            ih.nelements, ih.u32, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold,
+                            ih.parameter_s, iv, ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable, ih.pdl);
   } else if (ih.mixed) {
     const size_t smem = sizeof(float) * (size_t)(N * N + 8 * 2 * NN);
-    indicator_raw_kernel<DIM, N, float><<<(unsigned)grid, 256, smem, s>>>(
-        ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
-        ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable);
+    return launch_maybe_pdl(&indicator_raw_kernel<DIM, N, float, double>, (unsigned)grid, 256, smem, s, ih.pdl != 0,
+                            ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold,
+                            ih.parameter_s, iv, ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable, ih.pdl);
   } else {
     const size_t smem = sizeof(double) * (size_t)(N * N + 8 * 2 * NN);
-    indicator_raw_kernel<DIM, N, double><<<(unsigned)grid, 256, smem, s>>>(
-        ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold, ih.parameter_s, iv,
-        ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable);
+    return launch_maybe_pdl(&indicator_raw_kernel<DIM, N, double, double>, (unsigned)grid, 256, smem, s, ih.pdl != 0,
+                            ih.nelements, ih.u, ih.alpha_raw, ih.gamma, ih.alpha_max, ih.alpha_min, ih.threshold,
+                            ih.parameter_s, iv, ih.eq == EQ_MHD ? 1 : 0, ih.nv, ih.variable, ih.pdl);
   }
   return cudaGetLastError();
 }
@@ -348,7 +373,11 @@ static cudaError_t launch_indicator_dim(const IndicatorHost &ih, cudaStream_t s)
 // of Trixi's apply_smoothing! over interfaces and mortars.
 __global__ void indicator_smooth_kernel(int dim, int64_t E, const double *__restrict__ alpha_raw,
                                         double *__restrict__ alpha, const int32_t *__restrict__ face_table,
-                                        const int32_t *__restrict__ slot_nbrs, int smooth) {
+                                        const int32_t *__restrict__ slot_nbrs, int smooth, int pdl) {
+  if (pdl) {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+  }
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   double a = alpha_raw[e];
@@ -374,9 +403,9 @@ cudaError_t launch_indicator(const IndicatorHost &ih, cudaStream_t s) {
   cudaError_t e = (ih.dim == 1) ? launch_indicator_dim<1>(ih, s)
                   : (ih.dim == 2) ? launch_indicator_dim<2>(ih, s) : launch_indicator_dim<3>(ih, s);
   if (e != cudaSuccess) return e;
-  indicator_smooth_kernel<<<(unsigned)((ih.nelements + 255) / 256), 256, 0, s>>>(
-      ih.dim, ih.nelements, ih.alpha_raw, ih.alpha, ih.face_table, ih.slot_neighbors, ih.smooth);
-  return cudaGetLastError();
+  return launch_maybe_pdl(&indicator_smooth_kernel, (unsigned)((ih.nelements + 255) / 256), 256, 0, s, ih.pdl != 0,
+                          ih.dim, ih.nelements, (const double *)ih.alpha_raw, ih.alpha, ih.face_table,
+                          ih.slot_neighbors, ih.smooth, ih.pdl);
 }
 
 // ---------------------------------------------------------------------------

@@ -29,9 +29,6 @@ constexpr int MODE_VOLUME = 0;  // du = volume integral only (stage API)
 constexpr int MODE_RHS = 1;     // du = full rhs
 constexpr int MODE_RK = 2;      // k = a k + dt rhs; u_out = u_in + b k
 
-// bits of the device error word (read by trixi_synchronize)
-constexpr int DEVERR_BULK_WAIT = 1;  // a bounded wait for a bulk global->shared copy ran out
-
 // face-table entry of a face on a non-periodic domain boundary (neighbours
 // are >= 0, mortar slots -(slot+1))
 constexpr int32_t FACE_BOUNDARY = INT32_MIN;

@@ -235,40 +235,6 @@ __device__ __forceinline__ void cp_async8(void *dst_smem, const void *src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// One-dimensional bulk copy global -> shared by the TMA unit
-// (cp.async.bulk, no tensor map), completing on an mbarrier with a
-// transaction count.  Both addresses 16-byte aligned, size a multiple of 16.
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-  // make the initialised barrier visible to the asynchronous (TMA) proxy
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-// Waits for phase `parity` of the barrier, at most `limit` polls (each
-// try_wait may itself suspend the thread for a short while); false when the
-// limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, int limit) {
-  const unsigned a = smem_u32(bar);
-  for (int i = 0; i < limit; ++i) {
-    unsigned done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
 
 
 // BND = 1: the instantiation for non-periodic meshes and source terms (the
@@ -369,7 +335,6 @@ struct FusedKernel {
   // copies cost more than they save (1.070 ms; 2D: 68.2 -> 70.0 us per step).
   static constexpr bool UK_SMEM = PACKED && DIM == 3;
   static constexpr int n_uk(int epg) { return UK_SMEM ? ((epg * NN * NV + 1) & ~1) : 0; }  // doubles
-  static constexpr int N_BAR = UK_SMEM ? 2 : 0;  // doubles: the group's mbarrier (8 bytes, 16-byte slot)
   static constexpr size_t group_smem_core(int epg) {
     // (the surface fluxes overwrite the neighbour traces in place: n_surf is not added)
     return sizeof(R) * (size_t)(2 * n_cons(epg) + n_vol(epg) + n_fv(epg) + n_trace(epg) +
@@ -377,7 +342,7 @@ struct FusedKernel {
            sizeof(int) * (size_t)round_up4(epg * 2 * DIM);
   }
   static constexpr size_t group_smem(int epg) {
-    return group_smem_core(epg) + sizeof(double) * (2 * n_uk(epg) + N_BAR);
+    return group_smem_core(epg) + sizeof(double) * 2 * n_uk(epg);
   }
 
   static constexpr int warps_for(int epg) { return (epg * TPE + 31) / 32; }
@@ -452,12 +417,18 @@ struct FusedKernel {
 
   struct Smem {
     double *u64, *k64;  // UK_SMEM: the group's u and k, [el][node][v]
-    uint64_t *bar;      // UK_SMEM: mbarrier of their bulk copy
     R *cons, *prim, *fvol, *fsurf, *ffv, *trace, *alpha, *scale, *dsplit, *dhat, *invw;
     int *conforming;  // [el][face]: 1 = trace holds the neighbour's node, 0 = a mortar flux
     // node records [el][node][v]
     __device__ __forceinline__ R *c(int el, int n) const { return cons + (el * NN + n) * NV; }
     __device__ __forceinline__ R *w(int el, int n) const { return prim + (el * NN + n) * NV; }
+    // record loads and stores (16-byte accesses for 4 variables)
+    __device__ __forceinline__ static void ld(const R *base, int q, R *dst) { lds_rec<NV>(base + q * NV, dst); }
+    __device__ __forceinline__ static void st(R *base, int q, const R *src) { sts_rec<NV>(base + q * NV, src); }
+    __device__ __forceinline__ void ldc(int el, int n, R *dst) const { ld(cons, el * NN + n, dst); }
+    __device__ __forceinline__ void ldw(int el, int n, R *dst) const { ld(prim, el * NN + n, dst); }
+    __device__ __forceinline__ void stc(int el, int n, const R *src) const { st(cons, el * NN + n, src); }
+    __device__ __forceinline__ void stw(int el, int n, const R *src) const { st(prim, el * NN + n, src); }
     // [el][face][t][v]
     __device__ __forceinline__ R *tr(int el, int face, int t) const {
       return trace + ((el * 2 * DIM + face) * NF + t) * NV;
@@ -491,8 +462,8 @@ struct FusedKernel {
     R f[NV];
     if constexpr (VOL == VOL_WEAK) {
       R u[NV], w[NV];
-      lds_rec<NV>(s.c(el, r), u);
-      lds_rec<NV>(s.w(el, r), w);
+      s.ldc(el, r, u);
+      s.ldw(el, r, w);
       P::template flux<O>(u, w, f, p.pp);
     } else {
       const int t = r / NP, pp_ = r - (r / NP) * NP;
@@ -500,10 +471,10 @@ struct FusedKernel {
       pair_nodes<N>(pp_, i, m);
       const int ni = line_node<DIM, N, O>(t, i), nm = line_node<DIM, N, O>(t, m);
       R ui[NV], wi[NV], um[NV], wm[NV];
-      lds_rec<NV>(s.c(el, ni), ui);
-      lds_rec<NV>(s.w(el, ni), wi);
-      lds_rec<NV>(s.c(el, nm), um);
-      lds_rec<NV>(s.w(el, nm), wm);
+      s.ldc(el, ni, ui);
+      s.ldw(el, ni, wi);
+      s.ldc(el, nm, um);
+      s.ldw(el, nm, wm);
       two_point_flux_t<DIM, EQ, R, O, VFLUX>(ui, wi, um, wm, f, p.pp);
     }
     sts_rec<NV>(s.vol(el, O, r), f);
@@ -522,8 +493,8 @@ struct FusedKernel {
 #pragma unroll
       for (int v = 0; v < NV; ++v) un[v] = f[v];
       P::prim(un, wn, p.pp);
-      lds_rec<NV>(s.c(el, own), uo);
-      lds_rec<NV>(s.w(el, own), wo);
+      s.ldc(el, own, uo);
+      s.ldw(el, own, wo);
       if (side == 0)
         two_point_flux<DIM, EQ, R, O, HLL_FAMILY, SC_EC>(p.surface_flux, un, wn, uo, wo, f, p.pp);
       else
@@ -540,10 +511,10 @@ struct FusedKernel {
   __device__ __forceinline__ static void fv_item(const FusedParams<R> &p, const Smem &s, int el, int t, int a) {
     R ul[NV], wl[NV], ur[NV], wr[NV], f[NV];
     const int nl = line_node<DIM, N, O>(t, a), nr = line_node<DIM, N, O>(t, a + 1);
-    lds_rec<NV>(s.c(el, nl), ul);
-    lds_rec<NV>(s.w(el, nl), wl);
-    lds_rec<NV>(s.c(el, nr), ur);
-    lds_rec<NV>(s.w(el, nr), wr);
+    s.ldc(el, nl, ul);
+    s.ldw(el, nl, wl);
+    s.ldc(el, nr, ur);
+    s.ldw(el, nr, wr);
     two_point_flux<DIM, EQ, R, O, HLL_FAMILY, SC_EC>(p.fv_flux, ul, wl, ur, wr, f, p.pp);
     if constexpr (NC) {
       R g[NV];
@@ -571,8 +542,8 @@ struct FusedKernel {
       int m = ci + k;
       if (m >= N) m -= N;
       R um[NV], wm[NV], f[NV];
-      lds_rec<NV>(s.c(el, n0 + m * stride), um);
-      lds_rec<NV>(s.w(el, n0 + m * stride), wm);
+      s.ldc(el, n0 + m * stride, um);
+      s.ldw(el, n0 + m * stride, wm);
       two_point_flux_t<DIM, EQ, R, O, VFLUX>(ui, wi, um, wm, f, p.pp);
       const R dm = drow[m];
 #pragma unroll
@@ -600,8 +571,8 @@ struct FusedKernel {
       partner<J>(s, node, coord, na, da);
       partner<J + 1>(s, node, coord, nb, db);
       R wa[NV], wb[NV];
-      lds_rec<NV>(s.w(el, na), wa);
-      lds_rec<NV>(s.w(el, nb), wb);
+      s.ldw(el, na, wa);
+      s.ldw(el, nb, wb);
       float2 f[NV];
       ranocha_x2<DIM, J / (N - 1), (J + 1) / (N - 1)>(wi, wa, wb, f, p.pp);
       const float2 dd = pk::mk(da, db);
@@ -613,9 +584,9 @@ struct FusedKernel {
       R dm;
       partner<J>(s, node, coord, nm, dm);
       R ui[NV], um[NV], wm[NV], f[NV];
-      lds_rec<NV>(s.c(el, node), ui);
-      lds_rec<NV>(s.c(el, nm), um);
-      lds_rec<NV>(s.w(el, nm), wm);
+      s.ldc(el, node, ui);
+      s.ldc(el, nm, um);
+      s.ldw(el, nm, wm);
       two_point_flux_t<DIM, EQ, R, J / (N - 1), VFLUX>(ui, wi, um, wm, f, p.pp);
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[v] += dm * f[v];
@@ -634,8 +605,7 @@ struct FusedKernel {
     Smem s;
     s.u64 = reinterpret_cast<double *>(smem_raw + gid * GROUP_SMEM);
     s.k64 = s.u64 + N_UK;
-    s.bar = reinterpret_cast<uint64_t *>(s.k64 + N_UK);
-    s.cons = reinterpret_cast<R *>(s.k64 + N_UK + N_BAR);
+    s.cons = reinterpret_cast<R *>(s.k64 + N_UK);
     s.prim = s.cons + N_CONS;
     s.fvol = s.prim + N_CONS;
     s.ffv = s.fvol + N_VOL;
@@ -704,23 +674,13 @@ struct FusedKernel {
     if constexpr (sizeof(R) == 4) sh_in = p.u32_in;
     double ureg[NV], kreg[NV];
     R uown[NV];
-    bool bulk = false;  // UK_SMEM: u and k come by one bulk copy each (else by cp.async per thread)
     if constexpr (UK_SMEM) {
       if (mode == MODE_RK) {
         // the group's u (and k) spans, contiguous in global memory
         const int nval = ne * NN * NV;
         const double *gu = p.u_in + e0 * NN * NV, *gk = p.k + e0 * NN * NV;
         const bool a16 = vec && ((e0 * NN * NV) & 1) == 0;  // 16-byte aligned span starts
-        bulk = a16 && (nval & 1) == 0;                        // and 16-byte multiples
-        if (bulk) {
-          if (gt == 0) {
-            const unsigned bytes = 8u * (unsigned)nval;
-            mbar_init(s.bar, 1);
-            mbar_expect_tx(s.bar, use_k ? 2 * bytes : bytes);
-            bulk_g2s(s.u64, gu, bytes, s.bar);
-            if (use_k) bulk_g2s(s.k64, gk, bytes, s.bar);
-          }
-        } else if (a16) {
+        if (a16) {
           const int nc = nval >> 1;
           for (int c = gt; c < nc; c += GTr) {
             cp_async16(s.u64 + 2 * c, gu + 2 * c);
@@ -798,8 +758,8 @@ struct FusedKernel {
         for (int v = 0; v < NV; ++v) uu[v] = narrow<HW_OWNER>(ureg[v]);
       }
       P::prim(uu, ww, p.pp);
-      sts_rec<NV>(s.c(my_el, my_node), uu);
-      sts_rec<NV>(s.w(my_el, my_node), ww);
+      s.stc(my_el, my_node, uu);
+      s.stw(my_el, my_node, ww);
       if (my_node == 0) {
         if constexpr (VOL == VOL_SC) {
           const double a = p.alpha[e0 + my_el];
@@ -885,8 +845,8 @@ struct FusedKernel {
       // visible after phase A's barrier
       if (has_node) {
         R ui[NV], wi[NV];
-        lds_rec<NV>(s.c(el, node), ui);
-        lds_rec<NV>(s.w(el, node), wi);
+        s.ldc(el, node, ui);
+        s.ldw(el, node, wi);
         if constexpr (PACKED) {
           float2 acc2[NV];
 #pragma unroll
@@ -901,19 +861,7 @@ struct FusedKernel {
         }
       }
     }
-    if constexpr (UK_SMEM) {
-      if (bulk) {
-        // (phase A's barrier ordered the barrier's initialisation before this)
-        // a few KB from this GPU's memory: the limit is far beyond any
-        // completion time; running out raises the device error word
-        if (!mbar_wait(s.bar, 0, 1 << 22)) {
-          atomicOr(p.err, DEVERR_BULK_WAIT);
-          mbar_wait(s.bar, 0, 1 << 22);  // let the copies in flight land before the block may exit
-        }
-      } else {
-        cp_async_wait_all();
-      }
-    }
+    if constexpr (UK_SMEM) cp_async_wait_all();
     group_sync(gid, p.wpg, GTr);
 
     // phase C: the thread that loaded node q finishes it
@@ -982,7 +930,7 @@ struct FusedKernel {
       // (src/solvers/dg_2d_kernel.jl:269-292).  Phi_d(u_i, u_m) is linear in
       // u_m's (B_d, psi), so the sum is Phi_d(u_i, .) of sum_m D_split[i_d, m] (B_d, psi)_m.
       R wo[NV];
-      lds_rec<NV>(s.w(el, node), wo);
+      s.ldw(el, node, wo);
       constexpr int strides[3] = {1, N, N * N};
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {

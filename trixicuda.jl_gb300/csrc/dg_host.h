@@ -129,6 +129,7 @@ struct IndicatorHost {
   double alpha_max = 0.5, alpha_min = 0.001;
   double threshold = 0, parameter_s = 0;
   double ivdm[HOST_NMAX * HOST_NMAX] = {};  // row-major inverse Vandermonde
+  int pdl = 0;  // launch both kernels as programmatic dependent launches
 };
 cudaError_t launch_indicator(const IndicatorHost &ih, cudaStream_t s);
 

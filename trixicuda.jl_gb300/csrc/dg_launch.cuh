@@ -60,15 +60,15 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
   p.lhat_l = R(h.lhat_l);
   p.lhat_r = R(h.lhat_r);
   if constexpr (EQ == EQ_ADV && BND == 0) {
-    // linear advection on periodic / mortar meshes: the dedicated one-thread-
-    // per-node kernel (dg_adv.cuh).  Its block shape is fixed; the tile
-    // reported is one element group of the warps that hold an element's nodes
-    // and is the only one accepted, so the tile tuner has a single candidate
+    // linear advection on periodic / mortar meshes: the dedicated kernel
+    // (dg_adv.cuh).  Its block shape is fixed; the tile reported is that
+    // block and is the only one accepted, so the tile tuner has a single
+    // candidate
     using A = AdvKernel<DIM, N, R, VOL>;
     if (h.u32_in || h.u32_out) return cudaErrorNotSupported;  // it keeps no FP32 state copy
     if (h.tile_out) {
       h.tile_out->epg = 1;
-      h.tile_out->min_wpg = h.tile_out->def_wpg = h.tile_out->max_warps = (A::NN + 31) / 32;
+      h.tile_out->min_wpg = h.tile_out->def_wpg = h.tile_out->max_warps = A::BLOCK / 32;
       h.tile_out->def_gpb = 1;
       h.tile_out->group_smem = 0;
       return cudaSuccess;

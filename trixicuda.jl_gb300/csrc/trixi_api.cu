@@ -552,6 +552,7 @@ int run_indicator(trixi_handle *h, const double *u, double *alpha_out, cudaStrea
   ih.nelements = h->E;
   ih.u = u;
   ih.u32 = fp32 ? u32 : nullptr;
+  ih.pdl = h->fused.pdl;  // chained with the fused kernels as programmatic dependent launches
   ih.alpha_raw = h->d_alpha_raw;
   ih.alpha = alpha_out;
   ih.face_table = h->d_face_table;
@@ -1764,6 +1765,7 @@ AdjointHost adjoint_host(const trixi_handle *h) {
   }
   a.lhat_l = h->fused.lhat_l;
   a.lhat_r = h->fused.lhat_r;
+  a.pdl = h->fused.pdl;
   return a;
 }
 
@@ -2013,6 +2015,7 @@ int trixi_adjoint_backward(trixi_handle *h, const double *uT_bar, double *u0_bar
     const size_t nval = bytes / sizeof(double);
     AdjointHost adj = adjoint_host(h);
     adj.dt = A->dt;
+    adj.u_ready = 1;  // the stored stage states were written by the forward sweep, before these launches
     for (int64_t j = A->n - 1; j >= 0; --j)
       for (int st = 4; st >= 0; --st) {
         adj.u = A->stages_all + ((size_t)j * 5 + st) * nval;
