@@ -207,7 +207,11 @@ int trixi_rk_stage(trixi_handle *h, double *u_out, const double *u_in, double *k
 
 /* nsteps CarpenterKennedy2N54 steps of size dt from time t, in place in u
  * (k is the 2N register).  The stages of a step run u -> s1 -> s2 -> s1 -> s2
- * -> u through two library-owned buffers, so no copy is needed. */
+ * -> u through two library-owned buffers, so no copy is needed.  With
+ * precision FP32-mixed (Euler and ideal GLM-MHD), each stage after the first
+ * of a call reads its flux states from an FP32 copy that the previous stage
+ * wrote (two more library-owned buffers); the results are the bits of the
+ * same stages run one by one through trixi_rk_stage. */
 int trixi_rk_steps(trixi_handle *h, double *u, double *k, double t, double dt,
                    int64_t nsteps, void *stream);
 
