@@ -26,6 +26,15 @@
 // owner thread sums D_split / D_hat times the staged fluxes along each
 // dimension, adds the surface terms, scales by -J^{-1}, and stores du or
 // performs the RK update, in the reference layout.
+//
+// FP32-mixed variants of this plan (each measured; see the constants below):
+// the volume fluxes are not phase-B items but "owner pairs" (the owner thread
+// evaluates its partner fluxes into registers, packed two per FP32
+// instruction stream for Euler flux_ranocha); the surface fluxes overwrite
+// their trace records; inside trixi_rk_steps the flux states and traces come
+// from an FP32 copy of the state that the previous stage wrote; in the packed
+// 3D kernels u and k travel to shared memory by cp.async during phases A-B
+// instead of occupying registers.
 #pragma once
 #include "dg_convert.cuh"
 #include "dg_ic.cuh"
