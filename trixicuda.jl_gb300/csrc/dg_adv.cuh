@@ -114,6 +114,13 @@ struct AdvKernel {
     const int mode = p.mode;
     const bool surface = mode != MODE_VOLUME;
     const bool use_k = mode == MODE_RK && p.use_k;
+    // the block's nodes (and face nodes) are contiguous from element e0 on:
+    // block-relative 32-bit indices against block base pointers
+    const int nvalid = (int)min((int64_t)NODES, (p.nelements - e0) * NN);
+    const int ivalid = surface ? (int)min((int64_t)ITEMS, (p.nelements - e0) * FPE) : 0;
+    const double *ub = p.u_in + e0 * NN;
+    double *const ob = p.out + e0 * NN;
+    double *const kb = (mode == MODE_RK) ? p.k + e0 * NN : nullptr;  // (k is absent outside RK stages)
     int el[NPT], node[NPT];
     bool has[NPT];
 #pragma unroll
@@ -121,7 +128,7 @@ struct AdvKernel {
       const int q = tid + i * BLOCK;
       el[i] = q / NN;
       node[i] = q - el[i] * NN;
-      has[i] = q < NODES && e0 + el[i] < p.nelements;
+      has[i] = q < nvalid;
     }
     // the connectivity, the face-node tables and the geometry are constant:
     // loaded before the wait for the previous kernel, so that the neighbour
@@ -131,16 +138,16 @@ struct AdvKernel {
     bool conforming[IPT];
     uint32_t item[IPT];
     int32_t nbs[IPT];
+    const int32_t *ftb = p.face_table + e0 * (2 * DIM);
 #pragma unroll
     for (int i = 0; i < IPT; ++i) {
       item[i] = 0;
       nbs[i] = 0;
       const int j = tid + i * BLOCK;
-      if (!surface || j >= ITEMS) continue;
-      const int fe = j / FPE, r = j - (j / FPE) * FPE;
-      if (e0 + fe >= p.nelements) continue;
+      if (j >= ivalid) continue;
+      const int fe = j / FPE, r = j - fe * FPE;
       item[i] = __ldg(&tab.face[r]);
-      nbs[i] = __ldg(p.face_table + (e0 + fe) * (2 * DIM) + ((item[i] >> 16) & 7));
+      nbs[i] = __ldg(ftb + fe * (2 * DIM) + ((item[i] >> 16) & 7));
     }
     double inv_jac_e[NPT], dt_e[NPT];
 #pragma unroll
@@ -165,9 +172,9 @@ struct AdvKernel {
       kreg[i] = 0.0;
       ui[i] = R(0);
       if (has[i]) {
-        const int64_t g = (e0 + el[i]) * NN + node[i];
-        ureg[i] = p.u_in[g];
-        if (use_k) kreg[i] = p.k[g];
+        const int q = tid + i * BLOCK;
+        ureg[i] = ub[q];
+        if (use_k) kreg[i] = kb[q];
       }
     }
 #pragma unroll
@@ -175,9 +182,7 @@ struct AdvKernel {
       outer[i] = R(0);
       conforming[i] = true;
       const int j = tid + i * BLOCK;
-      if (!surface || j >= ITEMS) continue;
-      const int fe = j / FPE;
-      if (e0 + fe >= p.nelements) continue;
+      if (j >= ivalid) continue;
       const int32_t nb = nbs[i];
       if (nb >= 0) {
         outer[i] = narrow_hw(p.u_in[(int64_t)nb * NN + ((item[i] >> 8) & 255)]);
@@ -192,7 +197,7 @@ struct AdvKernel {
       // the FP64 pipe carries the neighbours' narrowing and the RK update
       // here, so the owner's value narrows on the integer pipe
       ui[i] = from_double<R>(ureg[i]);
-      s_u[el[i] * NN + node[i]] = ui[i];
+      s_u[tid + i * BLOCK] = ui[i];
       if constexpr (sizeof(R) == 4) {
         // the element's scale, once per element (as phase A of the generic kernel)
         if (node[i] == 0) s_scale[el[i]] = from_double<R>(-inv_jac_e[i] * (mode == MODE_RK ? dt_e[i] : 1.0));
@@ -206,9 +211,8 @@ struct AdvKernel {
 #pragma unroll
       for (int i = 0; i < IPT; ++i) {
         const int j = tid + i * BLOCK;
-        if (j >= ITEMS) continue;
+        if (j >= ivalid) continue;
         const int fe = j / FPE;
-        if (e0 + fe >= p.nelements) continue;
         R f = outer[i];
         if (conforming[i]) {
           const int face = (item[i] >> 16) & 7;
@@ -239,7 +243,7 @@ struct AdvKernel {
       for (int d = 0; d < DIM; ++d) {
         const int ci = coord[d];
         const R *row = s_op + ci * N;
-        const R *line = s_u + el[i] * NN + node[i] - ci * strides[d];
+        const R *line = s_u + (tid + i * BLOCK) - ci * strides[d];
         R sum = R(0);
         if constexpr (VOL == VOL_WEAK) {
 #pragma unroll
@@ -262,29 +266,29 @@ struct AdvKernel {
           if (coord[d] == N - 1) acc += p.lhat_r * fel[(2 * d + 1) * NF + tface[d]];
         }
       }
-      const int64_t g = (e0 + el[i]) * NN + node[i];
+      const int g = tid + i * BLOCK;  // block-relative node index
       if (mode == MODE_VOLUME) {
-        p.out[g] = to_double(acc);
+        ob[g] = to_double(acc);
         continue;
       }
       if constexpr (sizeof(R) == sizeof(double)) {
         const double du = double(acc) * -inv_jac_e[i];
         if (mode == MODE_RHS) {
-          p.out[g] = du;
+          ob[g] = du;
         } else {
           const double kk = (use_k ? p.rk_a * kreg[i] : 0.0) + dt_e[i] * du;
-          p.k[g] = kk;
-          p.out[g] = ureg[i] + p.rk_b * kk;
+          kb[g] = kk;
+          ob[g] = ureg[i] + p.rk_b * kk;
         }
       } else {
         // mixed precision: scale in FP32, widen exactly, accumulate in FP64
         const double dd = to_double(acc * s_scale[el[i]]);
         if (mode == MODE_RHS) {
-          p.out[g] = dd;
+          ob[g] = dd;
         } else {
           const double kk = use_k ? fma(p.rk_a, kreg[i], dd) : dd;
-          p.k[g] = kk;
-          p.out[g] = fma(p.rk_b, kk, ureg[i]);
+          kb[g] = kk;
+          ob[g] = fma(p.rk_b, kk, ureg[i]);
         }
       }
     }
