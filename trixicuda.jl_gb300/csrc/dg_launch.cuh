@@ -77,7 +77,7 @@ cudaError_t launch_one(const FusedHost &h, cudaStream_t s) {
     const int64_t grid = (h.nelements + A::EPB - 1) / A::EPB;
     if (grid <= 0) return cudaSuccess;
     if (grid > 0x7fffffffLL) return cudaErrorInvalidValue;
-    constexpr auto kernel = &dg_adv_kernel<DIM, N, R, VOL>;
+    constexpr auto kernel = adv_entry<DIM, N, R, VOL>();
     if (h.pdl) {
       p.pdl = 1;
       cudaLaunchConfig_t cfg = {};
