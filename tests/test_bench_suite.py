@@ -47,3 +47,22 @@ def test_nan_aware_error():
     assert 0 < r["fp64_rel_err_vs_oracle"] < 1e-12
     r = bench._nan_aware_rel_err(np.array([1.0, np.nan, 3.0, 4.0]), ref)
     assert not r["nan_positions_match"]
+
+
+def test_reference_arm_line(capsys, monkeypatch):
+    """`bench.py --impl reference` prints one JSON line with the contract's
+    keys, timed on the oracle alone (a shortened sample here)."""
+    import json
+    import types
+
+    real = bench.cpu_baseline
+    monkeypatch.setattr(bench, "cpu_baseline", lambda seconds_target=8.0, nthreads=None: real(0.2, nthreads))
+    args = types.SimpleNamespace(steps=1, warmup=1, gpus=1)
+    assert bench.run_reference(args) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "dtype", "config", "impl", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
